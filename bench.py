@@ -1,0 +1,423 @@
+#!/usr/bin/env python
+"""Frame benchmark of the hair pipeline (one JSON line on rank 0).
+
+Workload: config 2 -- 100,000 wavy strands x 64 segments (seeded synthetic
+groom, baked), 1920x1080 camera, 1024^2 16-layer deep opacity map, key
+directional light + 8 point lights, LOD on, filter on, composite.  A step is
+one whole per-groom frame of hair_pass: clear, lod, scan, camera raster,
+clear_dom, lod, scan, DOM depth raster, DOM layers raster, shade, filter,
+composite.
+
+value: camera segments per second (sum over ranks / max time), Gseg/s, with
+the groom resident in HBM and the L2 flushed (256 MB write) before each step.
+e2e:   the same metric through the C ABI per step: host uniform math, the
+       frame call (uniforms and lights from host memory) and a copy of the
+       composited colour + depth into pinned host memory.
+
+--impl reference runs the CPU oracle (a C restatement of the reference's
+passes; the reference itself is a Rust/wgpu plugin that cannot run here) on a
+scaled sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+L2_FLUSH_BYTES = 256 << 20
+MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
+WORKLOAD = ("config2: 100k wavy strands x 64 segs (seeded synthetic, baked), 1920x1080, DOM 1024^2 x16, "
+            "key directional + 8 point lights, LOD on (lambda 3), filter on, composite")
+METRIC = "Gseg/s at 1080p, 6.4M segs (whole hair frame: raster + DOM + shade + filter + composite)"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", type=int, default=2)
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--cpu-scale", type=float, default=0.1,
+                    help="scale of the CPU sample (strand count and pixel count)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class Dist:
+    """Barrier and max-over-ranks for N>1 replicas (no data-path collective)."""
+
+    def __init__(self, world: int, backend: str):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as td
+
+            td.init_process_group(backend=backend)
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+
+        dev = "cuda" if torch.cuda.is_available() and self.td.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x: float) -> float:
+        if self.world == 1:
+            return x
+        import torch
+
+        dev = "cuda" if torch.cuda.is_available() and self.td.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        self.td.all_reduce(t, op=self.td.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.td.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        rows = []
+        for row in csv.reader(io.StringIO(Path(self.path).read_text())):
+            if len(row) >= 9:
+                rows.append([c.strip() for c in row])
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def peaks() -> tuple[float, str]:
+    try:
+        p = json.loads(MEASURED_PEAKS.read_text())
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# Algorithmic bytes of each pass per launch (what roofline.achieved counts).
+def pass_bytes(sc, seg_refs: dict) -> dict:
+    w, h = sc.view.width, sc.view.height
+    px = w * h
+    dw, dh = sc.dom_size
+    tex = dw * dh
+    b = sc.mesh.bundle_count
+    groom_in = b * (16 + 2048 + 16384)
+    return {
+        "clear": 20 * px,
+        "raster_camera": 20 * px + groom_in + 16 * seg_refs["camera_refs"],
+        "clear_dom": 68 * tex,
+        "raster_dom_depth": 4 * tex + groom_in + 16 * seg_refs["dom_refs"],
+        "raster_dom_layers": 68 * tex + groom_in + 16 * seg_refs["dom_refs"],
+        "shade": 12 * px + 20 * px + 4 * 68 * seg_refs["hair_pixels"],
+        "filter": 32 * px + 20 * px,
+        "composite": 20 * px + 40 * px,
+    }
+
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    from bevy_hair_gb300 import abi, configs
+    from bevy_hair_gb300.pipeline import HairRenderer
+
+    torch.cuda.set_device(local)
+    dist = Dist(world, "nccl")
+    stream = torch.cuda.current_stream()
+    sc = configs.CONFIGS[args.config](args.scale)
+    cam, dom = sc.params()
+    lights = sc.light_array()
+    r = HairRenderer(local, stream.cuda_stream)
+    r.ensure_targets(sc.view.width, sc.view.height, *sc.dom_size)
+    g = r.upload(sc.mesh)
+
+    # one frame to count the work it does
+    r.render_groom(g, cam, dom, lights)
+    r.synchronize()
+    ref_c = int(g.read(abi.SLOT_CAMERA, abi.GBUF_INDIRECT)[0])
+    ref_d = int(g.read(abi.SLOT_DOM, abi.GBUF_INDIRECT)[0])
+    seg_c = configs.segments_of(g.read(abi.SLOT_CAMERA, abi.GBUF_REFS), ref_c)
+    seg_d = configs.segments_of(g.read(abi.SLOT_DOM, abi.GBUF_REFS), ref_d)
+    hair_px = int((r.read(abi.BUF_CENTER) != np.uint64(0xFFFFFFFFFFFFFFFF)).sum())
+
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    def frame():
+        r.render_groom(g, cam, dom, lights)
+
+    for _ in range(max(args.warmup, 0)):
+        flush.fill_(1)
+        frame()
+    torch.cuda.synchronize()
+
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    clocks = Clocks(local)
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        starts[i].record(stream)
+        frame()
+        ends[i].record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    dist.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    local_ms = float(np.sum(step_ms))
+    total_ms = dist.max(local_ms)
+    ms_per_step = total_ms / args.steps
+    total_segs = dist.sum(float(seg_c) * args.steps)
+    value = total_segs / (total_ms * 1e-3) / 1e9
+
+    # per-pass breakdown on this rank: events between the pass calls
+    passes = ["clear", "lod_camera", "scan_camera", "raster_camera", "clear_dom", "lod_dom", "scan_dom",
+              "raster_dom_depth", "raster_dom_layers", "shade", "filter", "clear_color", "composite"]
+    reps = max(3, min(args.steps, 10))
+    acc = {p: 0.0 for p in passes}
+    layers = dom.copy()
+    layers["pass_mode"][0] = 2
+    for _ in range(reps):
+        flush.fill_(3)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(passes) + 1)]
+        ev[0].record(stream)
+        calls = [lambda: r.clear(), lambda: r.lod(g, cam, 0), lambda: r.scan(g, cam, 0),
+                 lambda: r.raster(g, cam, 0), lambda: r.clear_dom(), lambda: r.lod(g, dom, 1),
+                 lambda: r.scan(g, dom, 1), lambda: r.raster(g, dom, 1), lambda: r.raster(g, layers, 1),
+                 lambda: r.shade(cam, lights), lambda: r.filter(cam), lambda: r.clear_color(0.0),
+                 lambda: r.composite(cam, True)]
+        for k, call in enumerate(calls):
+            call()
+            ev[k + 1].record(stream)
+        torch.cuda.synchronize()
+        for k, p in enumerate(passes):
+            acc[p] += ev[k].elapsed_time(ev[k + 1]) / reps
+    per_pass = {p: round(v, 4) for p, v in acc.items()}
+    nbytes = pass_bytes(sc, {"camera_refs": ref_c, "dom_refs": ref_d, "hair_pixels": hair_px})
+    dominant = max((p for p in nbytes), key=lambda p: acc[p])
+    peak, peak_kind = peaks()
+    achieved = nbytes[dominant] / (acc[dominant] * 1e-3) / 1e9
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 2), "peak": peak,
+                "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": None, "bytes_per_launch": nbytes[dominant],
+                "note": "raster passes are bound by L2 atomics, not HBM: see per_pass and DESIGN.md"}
+
+    # end to end through the C ABI: host uniforms, frame, colour + depth back to pinned memory
+    color_pin = torch.empty(sc.view.width * sc.view.height * 4, dtype=torch.float32, pin_memory=True)
+    depth_pin = torch.empty(sc.view.width * sc.view.height, dtype=torch.float32, pin_memory=True)
+    lib = r.lib
+    h2d = 2 * abi.HAIR_PARAMS.itemsize + lights.nbytes
+    d2h = color_pin.numel() * 4 + depth_pin.numel() * 4
+
+    def e2e_step():
+        c, d = sc.params()
+        r.render_groom(g, c, d, lights)
+        st1 = lib.hg_copy_out(r.ctx, abi.BUF_COLOR, color_pin.data_ptr(), color_pin.numel() * 4)
+        st2 = lib.hg_copy_out(r.ctx, abi.BUF_DEPTH, depth_pin.data_ptr(), depth_pin.numel() * 4)
+        assert st1 == 0 and st2 == 0
+
+    for _ in range(2):
+        e2e_step()
+    dist.barrier()
+    e2e_total = 0.0
+    for i in range(args.steps):
+        flush.fill_(i & 0xFF)
+        torch.cuda.synchronize()
+        t_s = time.perf_counter()
+        e2e_step()
+        e2e_total += time.perf_counter() - t_s
+    e2e_ms = dist.max(e2e_total * 1e3)
+    e2e_value = total_segs / (e2e_ms * 1e-3) / 1e9
+    launches = 15 * args.steps
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(args, sample=True)
+    g.close()
+    r.close()
+    dist.close()
+    if rank != 0:
+        return None
+    return {
+        "metric": METRIC,
+        "value": round(value, 4),
+        "unit": "Gseg/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+u64",
+        "data": "synthetic (seeded groom, baked by the project's baker; no dataset exists)",
+        "config": {"workload": WORKLOAD if args.config == 2 and args.scale == 1.0 else
+                   f"config{args.config} scale {args.scale}", "width": sc.view.width,
+                   "height": sc.view.height, "dom": list(sc.dom_size), "strands": sc.mesh.strand_count(),
+                   "bundles": sc.mesh.bundle_count, "camera_refs": ref_c, "camera_segments": seg_c,
+                   "dom_refs": ref_d, "dom_segments": seg_d, "hair_pixels": hair_px,
+                   "lights": int(len(lights)), "l2": "flushed between timed steps (256 MB device write)",
+                   "parallelism": f"replicas x{world}"},
+        "per_pass_ms": per_pass,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(e2e_value, 4), "unit": "Gseg/s", "ms_per_step": round(e2e_ms / args.steps, 4),
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": launches,
+        "clocks": clk,
+    }
+
+
+def cpu_baseline(args, sample: bool) -> dict:
+    """The oracle on a scaled copy of the workload, all host cores."""
+    import oracle
+    from bevy_hair_gb300 import configs
+
+    scale = args.cpu_scale
+    sc = configs.CONFIGS[args.config](scale)
+    cam, dom = sc.params()
+    lights = sc.light_array()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    t = time.perf_counter()
+    out = oracle.frame(sc.mesh, cam, dom, lights)
+    dt = time.perf_counter() - t
+    segs = int(out["counts_camera"]["segments"])
+    return {"value": round(segs / dt / 1e9, 6), "unit": "Gseg/s", "cores": threads, "kind": "port",
+            "sample": (f"one whole frame of config{args.config} at scale {scale}: {sc.mesh.strand_count()} "
+                       f"strands, {sc.view.width}x{sc.view.height}, DOM {sc.dom_size[0]}^2, "
+                       f"{segs} camera segments, {dt:.2f} s"),
+            "seconds": round(dt, 3)}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    import oracle
+    from bevy_hair_gb300 import configs
+
+    scale = args.cpu_scale
+    sc = configs.CONFIGS[args.config](scale)
+    cam, dom = sc.params()
+    lights = sc.light_array()
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    for _ in range(min(args.warmup, 1)):
+        oracle.frame(sc.mesh, cam, dom, lights)
+    steps = args.steps
+    t = time.perf_counter()
+    budget = 150.0
+    done = 0
+    segs = 0
+    for _ in range(steps):
+        out = oracle.frame(sc.mesh, cam, dom, lights)
+        segs += int(out["counts_camera"]["segments"])
+        done += 1
+        if time.perf_counter() - t > budget:
+            break
+    dt = time.perf_counter() - t
+    value = segs / dt / 1e9
+    sample = (f"{done} whole frames of config{args.config} at scale {scale} ({sc.mesh.strand_count()} strands, "
+              f"{sc.view.width}x{sc.view.height}, DOM {sc.dom_size[0]}^2) on the CPU oracle")
+    return {
+        "impl": "reference",
+        "metric": METRIC,
+        "value": round(value, 6),
+        "unit": "Gseg/s",
+        "n_gpus": world,
+        "steps": done,
+        "warmup": args.warmup,
+        "ms_per_step": round(dt * 1e3 / max(done, 1), 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32+u64",
+        "data": "synthetic (seeded groom)",
+        "config": {"workload": WORKLOAD, "sample_scale": scale},
+        "cpu_baseline": {"value": round(value, 6), "unit": "Gseg/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 6), "unit": "Gseg/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is a Rust/wgpu Bevy plugin; no Rust toolchain or graphics stack exists here, so "
+                "this arm times the project's C restatement of its passes (oracle/hair_oracle.c)",
+    }
+
+
+def main():
+    args = parse_args()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        line = run_reference(args, rank, world)
+    else:
+        line = run_ours(args, rank, world, local)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

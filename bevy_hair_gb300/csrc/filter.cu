@@ -1,0 +1,227 @@
+// Reconnection filter (filter.wgsl:20-135) and the headless composite
+// (composite.wgsl:162-181 + ALPHA_BLENDING + depth test, pipeline.rs:299-339).
+// The filter's coverage decisions (strip test, depth rejection, "closer")
+// come from float comparisons, so this file is compiled with -fmad=false like
+// the raster to keep them reproducible.
+#include <cuda_runtime.h>
+
+#include "hg_device.cuh"
+#include "hg_internal.h"
+
+namespace hg {
+namespace {
+
+constexpr int kFilterRadius = 5;
+constexpr int kTileX = 32, kTileY = 8;
+constexpr int kHaloX = kTileX + 2 * kFilterRadius, kHaloY = kTileY + 2 * kFilterRadius;
+
+struct FilterArgs {
+    hg_hair_params p;
+    const unsigned long long* center;
+    const unsigned long long* cons;
+    const float4* shaded;
+    float4* filtered;
+    float* filtered_depth;
+};
+
+// screen_tangent (filter.wgsl:9-18)
+__device__ __forceinline__ float2 screen_tangent(const hg_hair_params& p, f3 world, f3 tangent) {
+    Projected a = project_world(p, world);
+    Projected b = project_world(p, add3(world, tangent));
+    float2 d = sub2(b.screen, a.screen);
+    float l = len2(d);
+    if (l < 1e-3f) return make_float2(1.0f, 0.0f);
+    return make_float2(__fdiv_rn(d.x, l), __fdiv_rn(d.y, l));
+}
+
+// One 32x8 tile per CTA; the 42x18 neighbourhood of center/conservative
+// words is staged in shared memory once and read 121 times per pixel.
+__global__ void __launch_bounds__(kTileX* kTileY) filter_kernel(const FilterArgs a) {
+    __shared__ unsigned long long s_center[kHaloY][kHaloX];
+    __shared__ unsigned long long s_cons[kHaloY][kHaloX];
+    const hg_hair_params& p = a.p;
+    const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
+    const int32_t x0 = blockIdx.x * kTileX - kFilterRadius, y0 = blockIdx.y * kTileY - kFilterRadius;
+    const int tid = threadIdx.y * kTileX + threadIdx.x;
+    for (int i = tid; i < kHaloX * kHaloY; i += kTileX * kTileY) {
+        int hx = i % kHaloX, hy = i / kHaloX;
+        int32_t gx = x0 + hx, gy = y0 + hy;
+        unsigned long long c = kEmptyU64, n = kEmptyU64;
+        if (gx >= 0 && gy >= 0 && gx < width && gy < height) {
+            size_t q = (size_t)gy * width + gx;
+            c = __ldg(&a.center[q]);
+            n = __ldg(&a.cons[q]);
+        }
+        s_center[hy][hx] = c;
+        s_cons[hy][hx] = n;
+    }
+    __syncthreads();
+
+    const int32_t px = blockIdx.x * kTileX + threadIdx.x, py = blockIdx.y * kTileY + threadIdx.y;
+    if (px >= width || py >= height) return;
+    const uint32_t pix = (uint32_t)py * (uint32_t)width + (uint32_t)px;
+    const int lx = threadIdx.x + kFilterRadius, ly = threadIdx.y + kFilterRadius;
+    const unsigned long long center_word = s_center[ly][lx], cons_word = s_cons[ly][lx];
+    const bool center_hit = !is_empty(center_word), cons_hit = !is_empty(cons_word);
+    if (!center_hit && !cons_hit) {
+        a.filtered[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        a.filtered_depth[pix] = 0.0f;
+        return;
+    }
+    const unsigned long long w = center_hit ? center_word : cons_word;
+    const uint32_t high = (uint32_t)(w >> 32), low = (uint32_t)w;
+    const f3 tangent = oct_decode(high & 0xffu, low >> 24u);
+    const uint32_t depth_q = high >> 8u;
+    const float view_dist = dequantize_depth(depth_q, p.screen[2], p.screen[3]);
+    const f3 world = reconstruct_world(p, px, py, view_dist);
+    const float2 ts = screen_tangent(p, world, tangent);
+    const float4 cc = __ldg(&a.shaded[pix]);
+
+    const float s_par = fmaxf(p.filter_params[0], 0.05f);
+    const float s_perp = fmaxf(p.filter_params[1], 0.02f);
+    const float sigma_par = (float)kFilterRadius * s_par;
+    const float sigma_perp = (float)kFilterRadius * s_perp;
+    const float sp2 = sigma_par * sigma_par, sq2 = sigma_perp * sigma_perp;
+    const float sigma_c = 0.9f, depth_reject = 1.45e-3f, closer_eps = 5e-4f, strip = 0.5f;
+    const float p_norm = __fdiv_rn(__uint2float_rn(depth_q), 16777214.0f);
+    const bool promote = !center_hit;
+    const bool use_color = !promote && cc.w > 0.0f;
+
+    float ax = 0.0f, ay = 0.0f, az = 0.0f, weight = 0.0f, h_center = 0.0f, h_cons = 0.0f;
+    for (int dy = -kFilterRadius; dy <= kFilterRadius; ++dy) {
+        for (int dx = -kFilterRadius; dx <= kFilterRadius; ++dx) {
+            int32_t qx = px + dx, qy = py + dy;
+            if (qx < 0 || qy < 0 || qx >= width || qy >= height) continue;
+            float2 d = make_float2((float)dx, (float)dy);
+            float d_par = dot2(d, ts);
+            float d_perp = len2(make_float2(d.x - ts.x * d_par, d.y - ts.y * d_par));
+            unsigned long long qc = s_center[ly + dy][lx + dx];
+            bool qc_hit = !is_empty(qc);
+            if (d_perp <= strip) {
+                if (qc_hit) {
+                    h_center += 1.0f;
+                } else if (!is_empty(s_cons[ly + dy][lx + dx])) {
+                    h_cons += 1.0f;
+                }
+            }
+            if (!qc_hit) continue;
+            float q_norm = __fdiv_rn(__uint2float_rn((uint32_t)(qc >> 40)), 16777214.0f);
+            if (fabsf(q_norm - p_norm) > depth_reject) continue;
+            float spatial = expf(__fdiv_rn(-d_par * d_par, sp2) - __fdiv_rn(d_perp * d_perp, sq2));
+            uint32_t qpix = (uint32_t)qy * (uint32_t)width + (uint32_t)qx;
+            float4 qcol = __ldg(&a.shaded[qpix]);
+            float color_w = 1.0f;
+            if (use_color) {
+                f3 dc = {cc.x - qcol.x, cc.y - qcol.y, cc.z - qcol.z};
+                float chroma = len3(dc);
+                color_w = expf(__fdiv_rn(-chroma * chroma, sigma_c * sigma_c));
+            }
+            float wgt = spatial * color_w;
+            ax += qcol.x * wgt;
+            ay += qcol.y * wgt;
+            az += qcol.z * wgt;
+            weight += wgt;
+        }
+    }
+    float cx = cc.x, cy = cc.y, cz = cc.z;
+    if (weight > 1e-5f) {
+        cx = __fdiv_rn(ax, weight);
+        cy = __fdiv_rn(ay, weight);
+        cz = __fdiv_rn(az, weight);
+    }
+    const float coverage = __fdiv_rn(h_center, fmaxf(h_center + h_cons, 1.0f));
+    const float cons_depth = cons_hit ? __fdiv_rn(__uint2float_rn((uint32_t)(cons_word >> 40)), 16777214.0f) : 1.0f;
+    const float center_depth = p_norm;
+    const bool closer = cons_hit && center_hit && (center_depth - cons_depth) >= closer_eps;
+    float alpha = closer ? 1.0f : clampf(coverage, 0.0f, 1.0f);
+    if (promote && weight <= 1e-5f) {
+        alpha = 0.0f;
+        cx = cy = cz = 0.0f;
+    }
+    a.filtered[pix] = make_float4(cx, cy, cz, alpha);
+    a.filtered_depth[pix] = view_dist;
+}
+
+struct CompositeArgs {
+    hg_hair_params p;
+    const float4* color_src;
+    const float* depth_src;
+    float4* color;
+    float* depth;
+};
+
+// composite.wgsl:162-181; blend src*a + dst*(1-a) (alpha: a + dst_a*(1-a)),
+// depth test GreaterEqual when reverse-Z else LessEqual, depth write on.
+__global__ void composite_kernel(const CompositeArgs a) {
+    const hg_hair_params& p = a.p;
+    const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
+    const int32_t px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y * blockDim.y + threadIdx.y;
+    if (px >= width || py >= height) return;
+    const uint32_t pix = (uint32_t)py * (uint32_t)width + (uint32_t)px;
+    const float4 c = __ldg(&a.color_src[pix]);
+    if (c.w < 0.001f) return;
+    const float view_dist = __ldg(&a.depth_src[pix]);
+    const f3 world = reconstruct_world(p, px, py, view_dist);
+    const float4 clip = mat_mul(p.clip_from_world, world.x, world.y, world.z, 1.0f);
+    const float depth = clampf(__fdiv_rn(clip.z, fmaxf(clip.w, 1e-5f)), 0.0f, 1.0f);
+    const float dst_depth = a.depth[pix];
+    const bool pass = p.pass_mode[2] == 1u ? depth >= dst_depth : depth <= dst_depth;
+    if (!pass) return;
+    a.depth[pix] = depth;
+    float4 d = a.color[pix];
+    const float ia = 1.0f - c.w;
+    d.x = c.x * c.w + d.x * ia;
+    d.y = c.y * c.w + d.y * ia;
+    d.z = c.z * c.w + d.z * ia;
+    d.w = c.w * 1.0f + d.w * ia;
+    a.color[pix] = d;
+}
+
+__global__ void clear_color_kernel(float4* __restrict__ color, float* __restrict__ depth, size_t pixels,
+                                   float depth_clear) {
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < pixels; i += stride) {
+        color[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        depth[i] = depth_clear;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_filter(hg_ctx* ctx, const hg_hair_params& p) {
+    FilterArgs a;
+    a.p = p;
+    a.center = ctx->center;
+    a.cons = ctx->cons;
+    a.shaded = ctx->shaded;
+    a.filtered = ctx->filtered;
+    a.filtered_depth = ctx->filtered_depth;
+    dim3 block(kTileX, kTileY);
+    dim3 grid((ctx->width + kTileX - 1) / kTileX, (ctx->height + kTileY - 1) / kTileY);
+    filter_kernel<<<grid, block, 0, ctx->stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_composite(hg_ctx* ctx, const hg_hair_params& p, uint32_t source_filtered) {
+    CompositeArgs a;
+    a.p = p;
+    a.color_src = source_filtered ? ctx->filtered : ctx->shaded;
+    a.depth_src = source_filtered ? ctx->filtered_depth : ctx->shaded_depth;
+    a.color = ctx->color;
+    a.depth = ctx->depth;
+    dim3 block(32, 8);
+    dim3 grid((ctx->width + 31) / 32, (ctx->height + 7) / 8);
+    composite_kernel<<<grid, block, 0, ctx->stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_clear_color(hg_ctx* ctx, float depth_clear) {
+    size_t pixels = (size_t)ctx->width * ctx->height;
+    int threads = 256;
+    int blocks = (int)std::min<size_t>((pixels + threads - 1) / threads, (size_t)ctx->sm_count * 8);
+    if (blocks < 1) blocks = 1;
+    clear_color_kernel<<<blocks, threads, 0, ctx->stream>>>(ctx->color, ctx->depth, pixels, depth_clear);
+    return cudaGetLastError();
+}
+
+}  // namespace hg

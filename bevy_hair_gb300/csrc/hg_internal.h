@@ -1,0 +1,73 @@
+// Internal state of a hairgb context and the kernel launchers each
+// translation unit provides.  Not part of the C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+
+#include "../../include/hairgb.h"
+
+struct hg_groom {
+    hg_gpu_bundle* bundles = nullptr;
+    float4* layers = nullptr;  // 2 float4 per GpuLayer
+    float4* style = nullptr;
+    uint32_t bundle_count = 0;   // as uploaded (may be 0)
+    uint32_t layer_count = 0;
+    uint32_t style_count = 0;
+    uint32_t strand_total = 0;   // sum of strand_count
+    uint32_t ref_capacity = 1;   // max(strand_total, 1), scan.wgsl:14 capacity
+    hg_lod_record* lod[2] = {nullptr, nullptr};
+    hg_strand_ref* refs[2] = {nullptr, nullptr};
+    uint32_t* indirect[2] = {nullptr, nullptr};  // (total, 1, 1, 0)
+    uint32_t* offsets[2] = {nullptr, nullptr};   // exclusive scan of n_lod, bundle_count + 1
+};
+
+struct hg_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    uint32_t width = 0, height = 0, dom_w = 0, dom_h = 0;
+    unsigned long long* center = nullptr;
+    unsigned long long* cons = nullptr;
+    uint32_t* beta = nullptr;
+    uint32_t* dom = nullptr;
+    float4* shaded = nullptr;
+    float* shaded_depth = nullptr;
+    float4* filtered = nullptr;
+    float* filtered_depth = nullptr;
+    float4* color = nullptr;
+    float* depth = nullptr;
+    uint32_t* err = nullptr;       // device error word
+    hg_light* lights = nullptr;    // device copy, HG_MAX_LIGHTS
+    // Pinned staging ring for the light list; slot k is reused only after
+    // the event recorded behind its last copy has completed.
+    static constexpr int kLightSlots = 8;
+    hg_light* lights_host = nullptr;  // kLightSlots * HG_MAX_LIGHTS
+    cudaEvent_t light_events[kLightSlots] = {};
+    int light_slot = 0;
+    int sm_count = 0;
+    std::string last_error;
+};
+
+namespace hg {
+
+// raster.cu
+cudaError_t launch_clear(hg_ctx* ctx);
+cudaError_t launch_clear_dom(hg_ctx* ctx);
+cudaError_t launch_lod(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot);
+cudaError_t launch_scan(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot);
+cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot, const float* scene);
+
+// shade.cu
+cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights, uint32_t ortho, float exposure,
+                         uint32_t model);
+
+// filter.cu
+cudaError_t launch_filter(hg_ctx* ctx, const hg_hair_params& p);
+cudaError_t launch_composite(hg_ctx* ctx, const hg_hair_params& p, uint32_t source_filtered);
+cudaError_t launch_clear_color(hg_ctx* ctx, float depth_clear);
+
+}  // namespace hg

@@ -1,0 +1,653 @@
+// Visibility passes: clear, clear_dom, lod, scan and raster (camera G-buffer
+// and deep-opacity map).  Everything here feeds the integer visibility
+// outputs, so this file is compiled with -fmad=false and follows the float
+// semantics of hg_device.cuh.
+//
+// Reference passes: clear.wgsl, clear_dom.wgsl, lod.wgsl, scan.wgsl,
+// raster.wgsl (src/render/shaders/).
+#include <cuda_runtime.h>
+
+#include "hg_device.cuh"
+#include "hg_internal.h"
+
+namespace hg {
+namespace {
+
+// ------------------------------------------------------------------ clear
+
+// clear.wgsl:7-16.  Four pixels per thread with 16-byte stores.
+__global__ void clear_kernel(unsigned long long* __restrict__ center, unsigned long long* __restrict__ cons,
+                             uint32_t* __restrict__ beta, size_t pixels) {
+    size_t quads = pixels / 4;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    const ulonglong2 e2 = make_ulonglong2(kEmptyU64, kEmptyU64);
+    const uint4 e4 = make_uint4(0xffffffffu, 0xffffffffu, 0xffffffffu, 0xffffffffu);
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < quads; q += stride) {
+        reinterpret_cast<ulonglong2*>(center)[2 * q] = e2;
+        reinterpret_cast<ulonglong2*>(center)[2 * q + 1] = e2;
+        reinterpret_cast<ulonglong2*>(cons)[2 * q] = e2;
+        reinterpret_cast<ulonglong2*>(cons)[2 * q + 1] = e2;
+        reinterpret_cast<uint4*>(beta)[q] = e4;
+    }
+    size_t tail = quads * 4 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tail < pixels) {
+        center[tail] = kEmptyU64;
+        cons[tail] = kEmptyU64;
+        beta[tail] = 0xffffffffu;
+    }
+}
+
+// clear_dom.wgsl:8-21: words below `texels` are front depths, the rest counters.
+__global__ void clear_dom_kernel(uint32_t* __restrict__ dom, size_t texels, size_t words) {
+    size_t quads = words / 4;
+    size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t q = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q < quads; q += stride) {
+        size_t w = q * 4;
+        uint4 v;
+        v.x = w + 0 < texels ? kDomEmpty : 0u;
+        v.y = w + 1 < texels ? kDomEmpty : 0u;
+        v.z = w + 2 < texels ? kDomEmpty : 0u;
+        v.w = w + 3 < texels ? kDomEmpty : 0u;
+        reinterpret_cast<uint4*>(dom)[q] = v;
+    }
+    size_t tail = quads * 4 + (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (tail < words) dom[tail] = tail < texels ? kDomEmpty : 0u;
+}
+
+// ------------------------------------------------------------------ lod
+
+__device__ __forceinline__ f3 to_world(const hg_hair_params& p, f3 q) {
+    float4 r = mat_mul(p.world_from_model, q.x, q.y, q.z, 1.0f);
+    return {r.x, r.y, r.z};
+}
+__device__ __forceinline__ f3 dir_world(const hg_hair_params& p, f3 d) {
+    float4 r = mat_mul(p.world_from_model, d.x, d.y, d.z, 0.0f);
+    return safe_normalize({r.x, r.y, r.z});
+}
+
+// control_points_for_lod (common.wgsl:231-238); the power-of-two snap is
+// evaluated exactly from the highest set bit of c - 1.
+__device__ __forceinline__ uint32_t control_points_for_lod(float l) {
+    float c_raw = fmaxf(floorf(__fsqrt_rn(clampf(l, 0.0f, 1.0f)) * 127.0f), (float)kLayerCount);
+    if (c_raw < 3.0f) return f2u(fmaxf(c_raw, 2.0f));
+    uint32_t c1 = f2u(c_raw - 1.0f);
+    uint32_t snapped = (1u << (31 - __clz(c1))) + 1u;
+    return snapped < 127u ? snapped : 127u;
+}
+
+// lod.wgsl:6-59, one warp per bundle (two of the 64 cage corners per lane).
+__global__ void lod_kernel(const hg_hair_params p, const hg_gpu_bundle* __restrict__ bundles,
+                           const float4* __restrict__ layers, hg_lod_record* __restrict__ out, uint32_t count) {
+    uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t lane = threadIdx.x & 31u;
+    if (b >= count) return;
+    hg_gpu_bundle bundle = bundles[b];
+    float mnx = 1e20f, mny = 1e20f, mxx = -1e20f, mxy = -1e20f;
+    bool front = false;
+    for (uint32_t c = lane; c < 64u; c += 32u) {
+        float4 pa = __ldg(&layers[2u * (bundle.layer_offset + c)]);
+        f3 world = to_world(p, xyz(pa));
+        float4 clip = mat_mul(p.clip_from_world, world.x, world.y, world.z, 1.0f);
+        float dist = dot3(sub3(world, mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2])),
+                          mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]));
+        if (clip.w > 0.0f && dist > 0.0f) front = true;
+        Projected pr = project_world(p, world);
+        mnx = fminf(mnx, pr.screen.x);
+        mny = fminf(mny, pr.screen.y);
+        mxx = fmaxf(mxx, pr.screen.x);
+        mxy = fmaxf(mxy, pr.screen.y);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mnx = fminf(mnx, __shfl_xor_sync(0xffffffffu, mnx, o));
+        mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
+        mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
+        mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+    }
+    bool any_front = __any_sync(0xffffffffu, front);
+    if (lane != 0) return;
+    bool culled = !any_front || mxx < 0.0f || mxy < 0.0f || mnx > p.screen[0] || mny > p.screen[1];
+    uint32_t n_lod = 0u, cps = kLayerCount;
+    if (!culled) {
+        if (p.pass_mode[3] == 1u) {
+            n_lod = bundle.strand_count;
+            cps = control_points_for_lod(1.0f);
+        } else if (p.flags[0] == 0u) {
+            n_lod = bundle.strand_count;
+            cps = 127u;
+        } else {
+            float2 d = make_float2(mxx - mnx, mxy - mny);
+            float diag = len2(d);
+            float l = clampf(__fdiv_rn(diag, fmaxf(p.screen[1], 1.0f)) * p.appearance[2], 0.0f, 1.0f);
+            float delta = __uint2float_rn(pcg(b ^ 0x9e3779b9u)) * (1.0f / 4294967296.0f);
+            float n = __uint2float_rn(bundle.strand_count);
+            float raw = ceilf(l * (n + delta));
+            n_lod = f2u(clampf(raw, 1.0f, n));
+            cps = control_points_for_lod(l);
+        }
+    }
+    out[b] = hg_lod_record{n_lod, cps, bundle.strand_count, 0u};
+}
+
+// ------------------------------------------------------------------ scan
+
+// scan.wgsl:6-24 in two parallel steps.  Step 1 (one CTA): exclusive scan of
+// n_lod into offsets and the indirect arguments (total, 1, 1) with the total
+// clamped to the refs capacity.
+constexpr int kScanThreads = 1024;
+
+__global__ void __launch_bounds__(kScanThreads) scan_offsets_kernel(const hg_lod_record* __restrict__ lod,
+                                                                    uint32_t count, uint32_t capacity,
+                                                                    uint32_t* __restrict__ offsets,
+                                                                    uint32_t* __restrict__ indirect) {
+    __shared__ uint32_t warp_sums[32];
+    __shared__ uint32_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    for (uint32_t base = 0; base < count; base += kScanThreads) {
+        uint32_t i = base + threadIdx.x;
+        uint32_t v = i < count ? lod[i].n_lod : 0u;
+        uint32_t incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        if (lane == 31) warp_sums[warp] = incl;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t s = warp_sums[lane];
+            uint32_t si = s;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                uint32_t y = __shfl_up_sync(0xffffffffu, si, o);
+                if (lane >= (uint32_t)o) si += y;
+            }
+            warp_sums[lane] = si - s;  // exclusive warp offsets
+        }
+        __syncthreads();
+        uint32_t c = carry;
+        if (i < count) offsets[i] = c + warp_sums[warp] + incl - v;
+        __syncthreads();
+        if (threadIdx.x == kScanThreads - 1) carry = c + warp_sums[warp] + incl;
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        uint32_t total = carry < capacity ? carry : capacity;
+        offsets[count] = carry;
+        indirect[0] = total;
+        indirect[1] = 1u;
+        indirect[2] = 1u;
+        indirect[3] = 0u;
+    }
+}
+
+// Step 2: one warp per bundle writes its StrandRefs (bundle-major order, as
+// the serial loop does); entries at or past the capacity are dropped.
+__global__ void scan_expand_kernel(const hg_lod_record* __restrict__ lod, const uint32_t* __restrict__ offsets,
+                                   uint32_t count, uint32_t capacity, hg_strand_ref* __restrict__ refs) {
+    uint32_t lane = threadIdx.x & 31u;
+    uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < count; b += warps) {
+        hg_lod_record rec = lod[b];
+        uint32_t off = offsets[b];
+        for (uint32_t s = lane; s < rec.n_lod; s += 32u) {
+            uint32_t i = off + s;
+            if (i >= capacity) break;
+            reinterpret_cast<uint4*>(refs)[i] = make_uint4(b, s, rec.n_lod, rec.control_points);
+        }
+    }
+}
+
+// ------------------------------------------------------------------ raster
+
+constexpr int kRasterWarps = 4;
+constexpr int kRasterThreads = kRasterWarps * 32;
+
+struct alignas(16) StrandSmem {
+    float4 lp[16];     // layer sample: position, ao
+    float4 lt[16];     // layer tangent
+    float4 cp[128];    // control point: model position + ao, then world position + in_front
+    float4 ct[128];    // control point tangent: model, then world
+    float4 cu[128];    // uv, w, ao
+    float2 cs[128];    // projected screen position
+    int32_t off[132];  // camera: exclusive sample offset per segment
+    int32_t sn[128];   // camera: DDA step count per segment
+};
+
+struct RasterArgs {
+    hg_hair_params p;
+    const hg_gpu_bundle* bundles;
+    const float4* layers;
+    const float4* style;
+    const hg_strand_ref* refs;
+    const uint32_t* indirect;
+    unsigned long long* center;
+    unsigned long long* cons;
+    uint32_t* beta;
+    uint32_t* dom;
+    const float* scene;
+    uint32_t* err;
+    uint32_t bundle_count;
+};
+
+// sample_style (raster.wgsl:34-60)
+__device__ __forceinline__ f3 sample_style(const float4* __restrict__ style, uint32_t offset, float2 uv, float w) {
+    float u = clampf(uv.x, 0.0f, 1.0f) * (float)(kStyleU - 1u);
+    float v = clampf(uv.y, 0.0f, 1.0f) * (float)(kStyleV - 1u);
+    float ww = clampf(w, 0.0f, 1.0f) * (float)(kStyleW - 1u);
+    uint32_t u0 = f2u(floorf(u)), v0 = f2u(floorf(v)), w0 = f2u(floorf(ww));
+    uint32_t u1 = min(u0 + 1u, kStyleU - 1u), v1 = min(v0 + 1u, kStyleV - 1u), w1 = min(w0 + 1u, kStyleW - 1u);
+    float tu = u - __uint2float_rn(u0), tv = v - __uint2float_rn(v0), tw = ww - __uint2float_rn(w0);
+    auto at = [&](uint32_t iu, uint32_t iv, uint32_t iw) {
+        return xyz(__ldg(&style[offset + (iw * kStyleV + iv) * kStyleU + iu]));
+    };
+    f3 c00 = mix3(at(u0, v0, w0), at(u1, v0, w0), tu);
+    f3 c01 = mix3(at(u0, v1, w0), at(u1, v1, w0), tu);
+    f3 c10 = mix3(at(u0, v0, w1), at(u1, v0, w1), tu);
+    f3 c11 = mix3(at(u0, v1, w1), at(u1, v1, w1), tu);
+    return mix3(mix3(c00, c01, tv), mix3(c10, c11, tv), tw);
+}
+
+__device__ __forceinline__ f3 hermite(f3 p0, f3 p1, f3 m0, f3 m1, float t) {
+    float t2 = t * t;
+    float t3 = t2 * t;
+    float h00 = (2.0f * t3 - 3.0f * t2) + 1.0f;
+    float h10 = (t3 - 2.0f * t2) + t;
+    float h01 = -2.0f * t3 + 3.0f * t2;
+    float h11 = t3 - t2;
+    return add3(add3(add3(mul3s(p0, h00), mul3s(m0, h10)), mul3s(p1, h01)), mul3s(m1, h11));
+}
+
+__device__ __forceinline__ float4 bilinear4(float4 c00, float4 c10, float4 c01, float4 c11, float2 uv) {
+    float u = uv.x, v = uv.y;
+    float w00 = (1.0f - u) * (1.0f - v), w10 = u * (1.0f - v), w01 = (1.0f - u) * v, w11 = u * v;
+    float4 r;
+    r.x = ((c00.x * w00 + c10.x * w10) + c01.x * w01) + c11.x * w11;
+    r.y = ((c00.y * w00 + c10.y * w10) + c01.y * w01) + c11.y * w11;
+    r.z = ((c00.z * w00 + c10.z * w10) + c01.z * w01) + c11.z * w11;
+    r.w = ((c00.w * w00 + c10.w * w10) + c01.w * w01) + c11.w * w11;
+    return r;
+}
+
+__device__ __forceinline__ float4 shfl_up4(float4 v, int d) {
+    return make_float4(__shfl_up_sync(0xffffffffu, v.x, d), __shfl_up_sync(0xffffffffu, v.y, d),
+                       __shfl_up_sync(0xffffffffu, v.z, d), __shfl_up_sync(0xffffffffu, v.w, d));
+}
+__device__ __forceinline__ float4 shfl_down4(float4 v, int d) {
+    return make_float4(__shfl_down_sync(0xffffffffu, v.x, d), __shfl_down_sync(0xffffffffu, v.y, d),
+                       __shfl_down_sync(0xffffffffu, v.z, d), __shfl_down_sync(0xffffffffu, v.w, d));
+}
+
+// Strand generation (raster.wgsl:231-317) for one warp.  Leaves world-space
+// control points, tangents, uvw/ao and screen positions in shared memory.
+__device__ __forceinline__ uint32_t generate_strand(const RasterArgs& a, StrandSmem& sm, const hg_strand_ref& ref,
+                                                    const hg_gpu_bundle& bundle, uint32_t lane) {
+    const hg_hair_params& p = a.p;
+    float2 uv = pcg_uv(ref.strand ^ (ref.bundle * 0x85ebca6bu));
+    // Layer samples on lanes 0..15; neighbours come over shuffles.
+    float4 loaded = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (lane < kLayerCount) {
+        const float4* c = a.layers + 2u * (bundle.layer_offset + lane * 4u);
+        loaded = bilinear4(__ldg(c), __ldg(c + 2), __ldg(c + 4), __ldg(c + 6), uv);
+    }
+    float4 prev_l = shfl_up4(loaded, 1);
+    float4 next_l = shfl_down4(loaded, 1);
+    if (lane < kLayerCount) {
+        f3 curr = xyz(loaded);
+        f3 prev = lane == 0u ? curr : xyz(prev_l);
+        f3 next = lane + 1u >= kLayerCount ? curr : xyz(next_l);
+        f3 t = calc_tangent(lane, kLayerCount, prev, curr, next);
+        sm.lp[lane] = loaded;
+        sm.lt[lane] = make_float4(t.x, t.y, t.z, 0.0f);
+    }
+    __syncwarp();
+
+    uint32_t ncp = min(max(ref.control_points, 2u), 127u);
+    float den = __uint2float_rn(max(ncp - 1u, 1u));
+    // eval_cp (raster.wgsl:62-75), control point j on lane j % 32.
+    for (uint32_t idx = lane; idx < ncp; idx += 32u) {
+        float w = __fdiv_rn(__uint2float_rn(idx), den);
+        float layers_f = w * (float)(kLayerCount - 1u);
+        uint32_t i0 = min(f2u(floorf(layers_f)), kLayerCount - 1u);
+        uint32_t i1 = min(i0 + 1u, kLayerCount - 1u);
+        float t = layers_f - __uint2float_rn(i0);
+        float4 la = sm.lp[i0], lb = sm.lp[i1];
+        f3 base = hermite(xyz(la), xyz(lb), xyz(sm.lt[i0]), xyz(sm.lt[i1]), t);
+        float ao = mixf(la.w, lb.w, t);
+        f3 res = sample_style(a.style, bundle.style_offset, uv, w);
+        f3 pos = add3(base, res);
+        sm.cp[idx] = make_float4(pos.x, pos.y, pos.z, ao);
+        sm.cu[idx] = make_float4(uv.x, uv.y, w, ao);
+    }
+    __syncwarp();
+
+    // Control-point tangents (raster.wgsl:286-317), then world space and projection.
+    f3 wp[4], wt[4];
+    float2 sc[4];
+    bool fr[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        uint32_t idx = lane + 32u * k;
+        if (idx < ncp) {
+            f3 curr = xyz(sm.cp[idx]);
+            f3 prev = idx > 0u ? xyz(sm.cp[idx - 1u]) : curr;
+            f3 next = idx + 1u < ncp ? xyz(sm.cp[idx + 1u]) : curr;
+            f3 tm = safe_normalize(calc_tangent(idx, ncp, prev, curr, next));
+            wp[k] = to_world(p, curr);
+            wt[k] = dir_world(p, tm);
+            Projected pr = project_world(p, wp[k]);
+            sc[k] = pr.screen;
+            fr[k] = pr.in_front;
+        }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        uint32_t idx = lane + 32u * k;
+        if (idx < ncp) {
+            sm.cp[idx] = make_float4(wp[k].x, wp[k].y, wp[k].z, fr[k] ? 1.0f : 0.0f);
+            sm.ct[idx] = make_float4(wt[k].x, wt[k].y, wt[k].z, 0.0f);
+            sm.cs[idx] = sc[k];
+        }
+    }
+    __syncwarp();
+    return ncp;
+}
+
+// write_pixel's atomics (raster.wgsl:109-115) for one pixel of a sample whose
+// payload is already known.
+__device__ __forceinline__ void camera_write(const RasterArgs& a, int32_t px, int32_t py, int32_t width,
+                                             int32_t height, float clip_depth, unsigned long long payload,
+                                             bool center_hit, uint32_t beta_word) {
+    if (px < 0 || py < 0 || px >= width || py >= height) return;
+    uint32_t pix = (uint32_t)py * (uint32_t)width + (uint32_t)px;
+    if (a.scene) {
+        float scene = __ldg(&a.scene[pix]);
+        if (a.p.pass_mode[2] == 1u ? clip_depth < scene : clip_depth > scene) return;
+    }
+    atomicMin(&a.cons[pix], payload);
+    if (center_hit) {
+        atomicMin(&a.center[pix], payload);
+        atomicMin(&a.beta[pix], beta_word);
+    }
+}
+
+// Camera raster of one generated strand.  The DDA of every segment
+// (raster.wgsl:192-223) is flattened into one list of samples so the 32 lanes
+// share the work evenly; each sample computes its payload once
+// (raster.wgsl:83-108) and writes the centre pixel plus, on a diagonal step,
+// the two side pixels.
+__device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& sm, uint32_t ncp, float beta,
+                                              uint32_t lane) {
+    const hg_hair_params& p = a.p;
+    const int32_t nseg = (int32_t)ncp - 1;
+    int32_t carry = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        int32_t j = (int32_t)lane + 32 * k;
+        int32_t cnt = 0;
+        if (j < nseg) {
+            float4 pa = sm.cp[j], pb = sm.cp[j + 1];
+            int32_t n = 0;
+            if (pa.w != 0.0f || pb.w != 0.0f) {
+                float2 A = sm.cs[j], B = sm.cs[j + 1];
+                float2 d = sub2(B, A);
+                int32_t steps = f2i(ceilf(fmaxf(fabsf(d.x), fabsf(d.y))));
+                n = min(max(steps, 1), 96);
+                cnt = n + 1;
+            }
+            sm.sn[j] = n;
+        }
+        int32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if ((int32_t)lane >= o) incl += y;
+        }
+        if (j < nseg) sm.off[j] = carry + incl - cnt;
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    if (lane == 0) sm.off[nseg] = carry;
+    __syncwarp();
+
+    const int32_t total = carry;
+    const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
+    const float diameter = fmaxf(p.appearance[3], 0.05f);
+    const f3 cam = mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2]);
+    const f3 fwd = mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]);
+    const uint32_t beta_q = f2u(clampf(beta, 0.0f, 1.0f) * 255.0f + 0.5f);
+    for (int32_t s = (int32_t)lane; s < total; s += 32) {
+        // segment j with off[j] <= s < off[j+1]
+        int32_t lo = 0, hi = nseg - 1;
+        while (lo < hi) {
+            int32_t mid = (lo + hi + 1) >> 1;
+            if (sm.off[mid] <= s) lo = mid; else hi = mid - 1;
+        }
+        const int32_t j = lo;
+        const int32_t i = s - sm.off[j];
+        const int32_t n = sm.sn[j];
+        const float2 A = sm.cs[j], B = sm.cs[j + 1];
+        const float fn = __int2float_rn(n);
+        const float t = __fdiv_rn(__int2float_rn(i), fn);
+        const float2 scr = mix2(A, B, t);
+        const int32_t px = f2i(floorf(scr.x)), py = f2i(floorf(scr.y));
+        const float2 ctr = make_float2(__int2float_rn(px) + 0.5f, __int2float_rn(py) + 0.5f);
+        const float2 seg = sub2(B, A);
+        const float denom = fmaxf(dot2(seg, seg), 1e-6f);
+        const float closest = clampf(__fdiv_rn(dot2(sub2(ctr, A), seg), denom), 0.0f, 1.0f);
+        const float2 onl = make_float2(A.x + seg.x * closest, A.y + seg.y * closest);
+        const bool center_hit = len2(sub2(ctr, onl)) <= diameter * 0.5f;
+
+        // Payload (write_pixel, raster.wgsl:83-108); identical for the side pixels.
+        const float4 c0 = sm.cp[j], c1 = sm.cp[j + 1];
+        const f3 world = mix3(xyz(c0), xyz(c1), t);
+        const float dist = dot3(sub3(world, cam), fwd);
+        if (dist <= p.screen[2]) continue;
+        const float4 t0 = sm.ct[j], t1 = sm.ct[j + 1];
+        const f3 tangent = safe_normalize(mix3(xyz(t0), xyz(t1), t));
+        const float4 u0 = sm.cu[j], u1 = sm.cu[j + 1];
+        const f3 uvw = mix3(xyz(u0), xyz(u1), t);
+        const float ao = mixf(u0.w, u1.w, t);
+        float clip_depth = 0.0f;
+        if (a.scene) {
+            float4 clip = mat_mul(p.clip_from_world, world.x, world.y, world.z, 1.0f);
+            clip_depth = __fdiv_rn(clip.z, fmaxf(clip.w, 1e-5f));
+        }
+        const uint32_t depth = quantize_depth(dist, p.screen[2], p.screen[3]);
+        const uint32_t oct = oct_encode(tangent);
+        uint32_t ao_q = f2u(clampf(ao, 0.0f, 1.0f) * 63.0f + 0.5f);
+        if (p.flags[2] == 0u) ao_q = 63u;
+        const unsigned long long payload =
+            pack_gb(depth, oct & 0xffu, oct >> 8u, quant63(uvw.x), quant63(uvw.y), quant63(uvw.z), ao_q);
+        const uint32_t beta_word = (depth << 8u) | beta_q;
+        camera_write(a, px, py, width, height, clip_depth, payload, center_hit, beta_word);
+        if (i > 0) {
+            const float tp = __fdiv_rn(__int2float_rn(i - 1), fn);
+            const float2 prev = mix2(A, B, tp);
+            const int32_t qx = f2i(floorf(prev.x)), qy = f2i(floorf(prev.y));
+            if (qx != px && qy != py) {
+                camera_write(a, qx, py, width, height, clip_depth, payload, false, beta_word);
+                camera_write(a, px, qy, width, height, clip_depth, payload, false, beta_word);
+            }
+        }
+    }
+}
+
+// write_dom_pixel (raster.wgsl:118-148)
+template <int MODE>
+__device__ __forceinline__ void dom_write(const RasterArgs& a, int32_t px, int32_t py, int32_t width, int32_t height,
+                                          f3 world) {
+    const hg_hair_params& p = a.p;
+    if (px < 0 || py < 0 || px >= width || py >= height) return;
+    const float near_ = p.screen[2], far_ = p.screen[3];
+    float dist = dot3(sub3(world, mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2])),
+                      mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]));
+    if (dist <= near_ || dist >= far_) return;
+    uint32_t dom_w = f2u(p.dom_info[0]);
+    uint32_t pix = (uint32_t)py * dom_w + (uint32_t)px;
+    uint32_t q = quantize_depth(dist, near_, far_);
+    if (MODE == 1) {
+        atomicMin(&a.dom[pix], q);
+        return;
+    }
+    uint32_t front_q = __ldcg(&a.dom[pix]);
+    if (front_q == kDomEmpty) return;
+    float z_front = dequantize_depth(front_q, near_, far_);
+    float thickness = __fdiv_rn(fmaxf(far_ - near_, 1e-3f), (float)kDomLayers);
+    float tt = __fdiv_rn(fmaxf(dist - z_front, 0.0f), thickness);
+    uint32_t slice = min(f2u(tt), kDomLayers - 1u);
+    uint32_t pixels = dom_w * f2u(p.dom_info[1]);
+    atomicAdd(&a.dom[pixels + pix * kDomLayers + slice], 1u);
+}
+
+// draw_dom_segment (raster.wgsl:150-190), one segment per lane.
+template <int MODE>
+__device__ __forceinline__ void raster_dom(const RasterArgs& a, StrandSmem& sm, uint32_t ncp, uint32_t lane) {
+    const hg_hair_params& p = a.p;
+    const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
+    for (uint32_t j = lane; j + 1u < ncp; j += 32u) {
+        float4 c0 = sm.cp[j], c1 = sm.cp[j + 1u];
+        if (c0.w == 0.0f && c1.w == 0.0f) continue;
+        float2 A = sm.cs[j], B = sm.cs[j + 1u];
+        int32_t x0 = f2i(floorf(A.x)), y0 = f2i(floorf(A.y));
+        int32_t x1 = f2i(floorf(B.x)), y1 = f2i(floorf(B.y));
+        int32_t dx = iabs(isub(x1, x0)), dy = iabs(isub(y1, y0));
+        int32_t sx = x0 < x1 ? 1 : -1, sy = y0 < y1 ? 1 : -1;
+        int32_t err = isub(dx, dy);
+        float2 seg = sub2(B, A);
+        float seg_len2 = fmaxf(dot2(seg, seg), 1e-6f);
+        bool skip = j != 0u && (x0 != x1 || y0 != y1);
+        f3 p0 = xyz(c0), p1 = xyz(c1);
+        const int32_t ndy = (int32_t)(0u - (uint32_t)dy);
+        for (int step = 0; step < 1024; ++step) {
+            if (!skip) {
+                float2 ctr = make_float2(__int2float_rn(x0) + 0.5f, __int2float_rn(y0) + 0.5f);
+                float t = clampf(__fdiv_rn(dot2(sub2(ctr, A), seg), seg_len2), 0.0f, 1.0f);
+                dom_write<MODE>(a, x0, y0, width, height, mix3(p0, p1, t));
+            }
+            skip = false;
+            if (x0 == x1 && y0 == y1) break;
+            int32_t e2 = iadd(err, err);
+            if (e2 > ndy) {
+                err = isub(err, dy);
+                x0 = iadd(x0, sx);
+            }
+            if (e2 < dx) {
+                err = iadd(err, dx);
+                y0 = iadd(y0, sy);
+            }
+        }
+    }
+}
+
+// raster.wgsl:225-337: one warp per strand ref, persistent over the refs.
+template <int MODE>
+__global__ void __launch_bounds__(kRasterThreads) raster_kernel(const RasterArgs a) {
+    __shared__ StrandSmem smem[kRasterWarps];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    StrandSmem& sm = smem[warp];
+    const uint32_t total = a.indirect[0];
+    const uint32_t nwarps = gridDim.x * kRasterWarps;
+    for (uint32_t r = blockIdx.x * kRasterWarps + warp; r < total; r += nwarps) {
+        const hg_strand_ref ref = a.refs[r];
+        if (ref.bundle >= a.bundle_count) {
+            if (lane == 0) atomicOr(a.err, kErrBadRef);
+            continue;
+        }
+        const hg_gpu_bundle bundle = a.bundles[ref.bundle];
+        const uint32_t ncp = generate_strand(a, sm, ref, bundle, lane);
+        if (MODE == 0) {
+            float beta = __fdiv_rn(__uint2float_rn(ref.n_lod), __uint2float_rn(max(bundle.strand_count, 1u)));
+            raster_camera(a, sm, ncp, beta, lane);
+        } else {
+            raster_dom<MODE>(a, sm, ncp, lane);
+        }
+        __syncwarp();
+    }
+}
+
+int blocks_for(hg_ctx* ctx, const void* fn, int threads, size_t work_items, int per_block_items) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
+    if (per_sm < 1) per_sm = 1;
+    size_t need = (work_items + per_block_items - 1) / per_block_items;
+    size_t cap = (size_t)ctx->sm_count * per_sm;
+    size_t b = need < cap ? need : cap;
+    return b < 1 ? 1 : (int)b;
+}
+
+}  // namespace
+
+cudaError_t launch_clear(hg_ctx* ctx) {
+    size_t pixels = (size_t)ctx->width * ctx->height;
+    int threads = 256;
+    int blocks = (int)std::min<size_t>((pixels / 4 + threads - 1) / threads + 1, (size_t)ctx->sm_count * 8);
+    clear_kernel<<<blocks, threads, 0, ctx->stream>>>(ctx->center, ctx->cons, ctx->beta, pixels);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_clear_dom(hg_ctx* ctx) {
+    size_t texels = (size_t)ctx->dom_w * ctx->dom_h;
+    size_t words = texels * (1 + kDomLayers);
+    int threads = 256;
+    int blocks = (int)std::min<size_t>((words / 4 + threads - 1) / threads + 1, (size_t)ctx->sm_count * 8);
+    clear_dom_kernel<<<blocks, threads, 0, ctx->stream>>>(ctx->dom, texels, words);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lod(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot) {
+    uint32_t count = std::min(p.pass_mode[1], g->bundle_count);
+    if (count == 0) return cudaSuccess;
+    int threads = 256;
+    int blocks = (int)((count * 32u + threads - 1) / threads);
+    lod_kernel<<<blocks, threads, 0, ctx->stream>>>(p, g->bundles, g->layers, g->lod[slot], count);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scan(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot) {
+    uint32_t count = std::min(p.pass_mode[1], g->bundle_count);
+    scan_offsets_kernel<<<1, kScanThreads, 0, ctx->stream>>>(g->lod[slot], count, g->ref_capacity, g->offsets[slot],
+                                                            g->indirect[slot]);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || count == 0) return e;
+    int threads = 256;
+    int blocks = (int)std::min<uint32_t>((count * 32u + threads - 1) / threads, (uint32_t)ctx->sm_count * 8u);
+    scan_expand_kernel<<<blocks, threads, 0, ctx->stream>>>(g->lod[slot], g->offsets[slot], count, g->ref_capacity,
+                                                            g->refs[slot]);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot, const float* scene) {
+    if (g->bundle_count == 0) return cudaSuccess;
+    RasterArgs a;
+    a.p = p;
+    a.bundles = g->bundles;
+    a.layers = g->layers;
+    a.style = g->style;
+    a.refs = g->refs[slot];
+    a.indirect = g->indirect[slot];
+    a.center = ctx->center;
+    a.cons = ctx->cons;
+    a.beta = ctx->beta;
+    a.dom = ctx->dom;
+    a.scene = scene;
+    a.err = ctx->err;
+    a.bundle_count = g->bundle_count;
+    uint32_t mode = p.pass_mode[0];
+    const void* fn = mode == 0 ? (const void*)raster_kernel<0>
+                     : mode == 1 ? (const void*)raster_kernel<1>
+                                 : (const void*)raster_kernel<2>;
+    int blocks = blocks_for(ctx, fn, kRasterThreads, g->ref_capacity, kRasterWarps);
+    if (mode == 0) {
+        raster_kernel<0><<<blocks, kRasterThreads, 0, ctx->stream>>>(a);
+    } else if (mode == 1) {
+        raster_kernel<1><<<blocks, kRasterThreads, 0, ctx->stream>>>(a);
+    } else {
+        raster_kernel<2><<<blocks, kRasterThreads, 0, ctx->stream>>>(a);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace hg

@@ -1,0 +1,370 @@
+// Shade pass: per-pixel Karis-fit Marschner R/TT/TRT with Zinke dual
+// scattering and the deep-opacity optical depth toward the key light
+// (shade.wesl:31-593).  Output colour is compared with a tolerance, so this
+// file compiles with FMA contraction on.
+#include <cuda_runtime.h>
+
+#include "hg_device.cuh"
+#include "hg_internal.h"
+
+namespace hg {
+namespace {
+
+constexpr float kIor = 1.55f;
+constexpr float kDensityFront = 0.7f;
+constexpr float kDensityBack = 0.7f;
+constexpr int kScatterSteps = 8;
+
+struct Lobes {
+    f3 r, tt, trt;
+};
+struct Shape {
+    f3 alpha, beta;
+};
+struct Dual {
+    Lobes fwd;
+    f3 a_f, beta_f2, a_back, delta_b, sigma_b2;
+};
+
+__device__ __forceinline__ f3 spl(float s) { return {s, s, s}; }
+__device__ __forceinline__ f3 vmul(f3 a, f3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+__device__ __forceinline__ f3 vdiv(f3 a, f3 b) { return {a.x / b.x, a.y / b.y, a.z / b.z}; }
+__device__ __forceinline__ f3 vexp(f3 a) { return {expf(a.x), expf(a.y), expf(a.z)}; }
+__device__ __forceinline__ f3 vsqrt(f3 a) { return {sqrtf(a.x), sqrtf(a.y), sqrtf(a.z)}; }
+__device__ __forceinline__ f3 vmaxs(f3 a, float s) { return {fmaxf(a.x, s), fmaxf(a.y, s), fmaxf(a.z, s)}; }
+__device__ __forceinline__ f3 vmins(f3 a, float s) { return {fminf(a.x, s), fminf(a.y, s), fminf(a.z, s)}; }
+__device__ __forceinline__ f3 ld3(const float* v) { return {v[0], v[1], v[2]}; }
+__device__ __forceinline__ f3 cross3(f3 a, f3 b) {
+    return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+// gaussian3 (shade.wesl:51-54)
+__device__ __forceinline__ f3 gaussian3(f3 b, f3 x) {
+    f3 bb = vmaxs(b, 1e-3f);
+    const float k = 2.50662827f;  // sqrt(2 pi)
+    f3 num = vexp(vdiv(vmul(mul3s(x, -0.5f), x), vmul(bb, bb)));
+    return vdiv(num, mul3s(bb, k));
+}
+
+// fresnel (shade.wesl:56-60), the fifth power by multiplication.
+__device__ __forceinline__ float fresnel(float cos_t) {
+    const float r0 = (1.0f - kIor) / (1.0f + kIor);
+    const float f0 = r0 * r0;
+    float m = 1.0f - clampf(cos_t, 0.0f, 1.0f);
+    float m2 = m * m;
+    return f0 + (1.0f - f0) * (m2 * m2 * m);
+}
+
+// absorption_from_color (shade.wesl:70-77)
+__device__ __forceinline__ f3 absorption_from_color(f3 c, float roughness) {
+    float b = clampf(roughness, 0.0f, 1.0f);
+    float b2 = b * b;
+    float b3 = b2 * b;
+    float d = 5.969f - 0.215f * b + 2.532f * b2 - 10.73f * b3 + 5.574f * b2 * b2 + 0.245f * b3 * b2;
+    f3 l = {logf(clampf(c.x, 1e-4f, 1.0f)) / d, logf(clampf(c.y, 1e-4f, 1.0f)) / d,
+            logf(clampf(c.z, 1e-4f, 1.0f)) / d};
+    return vmul(l, l);
+}
+
+// azimuthal (shade.wesl:94-116)
+__device__ __forceinline__ Lobes azimuthal(float cos_theta_d, float cos_phi, f3 sigma_a) {
+    float cos_half_phi = sqrtf(clampf(0.5f + 0.5f * cos_phi, 0.0f, 1.0f));
+    float n_r = 0.25f * cos_half_phi * fresnel(cos_theta_d * cos_half_phi);
+    float inv_ctd = 1.0f / cos_theta_d;
+    float eta = 1.19f * inv_ctd + 0.36f * cos_theta_d;
+    float a = 1.0f / eta;
+    float h = cos_half_phi * (1.0f + a * (0.6f - 0.8f * cos_phi));
+    float f_tt = fresnel(cos_theta_d * sqrtf(clampf(1.0f - h * h, 0.0f, 1.0f)));
+    float path = 2.0f * sqrtf(clampf(1.0f - h * h * a * a, 0.0f, 1.0f)) * inv_ctd;
+    float k_tt = expf(-3.65f * cos_phi - 3.98f) * (1.0f - f_tt) * (1.0f - f_tt);
+    float f_trt = fresnel(cos_theta_d * 0.5f);
+    float k_trt = expf(17.0f * cos_phi - 16.78f) * (1.0f - f_trt) * (1.0f - f_trt) * f_trt;
+    float trt_path = 3.2f * inv_ctd;
+    Lobes r;
+    r.r = spl(n_r);
+    r.tt = {expf(-sigma_a.x * path) * k_tt, expf(-sigma_a.y * path) * k_tt, expf(-sigma_a.z * path) * k_tt};
+    r.trt = {expf(-sigma_a.x * trt_path) * k_trt, expf(-sigma_a.y * trt_path) * k_trt,
+             expf(-sigma_a.z * trt_path) * k_trt};
+    return r;
+}
+
+__device__ __forceinline__ Shape lobe_shape(float roughness, float tilt) {
+    float b = clampf(roughness * roughness, 0.02f, 1.0f);
+    return {{tilt, -0.5f * tilt, -1.5f * tilt}, {b, 0.5f * b, 2.0f * b}};
+}
+
+__device__ __forceinline__ f3 lobe_mean(const Lobes& l, f3 total, f3 q) {
+    f3 num = add3(add3(mul3s(l.r, q.x), mul3s(l.tt, q.y)), mul3s(l.trt, q.z));
+    return vdiv(num, vmaxs(total, 1e-5f));
+}
+
+// dual_scatter (shade.wesl:153-190)
+__device__ Dual dual_scatter(float cos_theta_d, f3 sigma_a, const Shape& shape) {
+    Lobes fwd = {spl(0.0f), spl(0.0f), spl(0.0f)}, back = fwd;
+#pragma unroll 2
+    for (int i = 0; i < kScatterSteps; ++i) {
+        float u = ((float)i + 0.5f) / (float)kScatterSteps;
+        Lobes b = azimuthal(cos_theta_d, cosf(u * 0.5f * kPi), sigma_a);
+        Lobes f = azimuthal(cos_theta_d, cosf((1.0f + u) * 0.5f * kPi), sigma_a);
+        back.r = add3(back.r, b.r);
+        back.tt = add3(back.tt, b.tt);
+        back.trt = add3(back.trt, b.trt);
+        fwd.r = add3(fwd.r, f.r);
+        fwd.tt = add3(fwd.tt, f.tt);
+        fwd.trt = add3(fwd.trt, f.trt);
+    }
+    const float w = kPi / (float)kScatterSteps;
+    fwd = {mul3s(fwd.r, w), mul3s(fwd.tt, w), mul3s(fwd.trt, w)};
+    back = {mul3s(back.r, w), mul3s(back.tt, w), mul3s(back.trt, w)};
+    Dual d;
+    d.fwd = fwd;
+    f3 a_f = vmins(add3(add3(fwd.r, fwd.tt), fwd.trt), 0.95f);
+    f3 a_b = add3(add3(back.r, back.tt), back.trt);
+    f3 beta2 = vmul(shape.beta, shape.beta);
+    f3 beta_f2 = lobe_mean(fwd, a_f, beta2);
+    f3 alpha_b = lobe_mean(back, a_b, shape.alpha);
+    f3 beta_b2 = lobe_mean(back, a_b, beta2);
+    f3 af2 = vmul(a_f, a_f);
+    f3 rest = {1.0f - af2.x, 1.0f - af2.y, 1.0f - af2.z};
+    f3 ab2 = vmul(a_b, a_b);
+    f3 ab3 = vmul(ab2, a_b);
+    f3 rr = vmul(rest, rest);
+    f3 rest3 = vmul(rr, rest);
+    f3 a_back = add3(vdiv(vmul(a_b, af2), rest), vdiv(vmul(ab3, af2), rest3));
+    f3 t1 = {1.0f - 2.0f * ab2.x / rr.x, 1.0f - 2.0f * ab2.y / rr.y, 1.0f - 2.0f * ab2.z / rr.z};
+    f3 num2 = add3(mul3s(rr, 2.0f), vmul(mul3s(af2, 4.0f), ab2));
+    f3 delta_b = add3(vmul(alpha_b, t1), vdiv(vmul(alpha_b, num2), rest3));
+    f3 beta_f = vsqrt(beta_f2), beta_b = vsqrt(beta_b2);
+    f3 lead = add3(spl(1.0f), mul3s(af2, kDensityBack));
+    f3 s1 = vsqrt(add3(mul3s(beta_f2, 2.0f), beta_b2));
+    f3 s2 = vsqrt(add3(mul3s(beta_f2, 2.0f), mul3s(beta_b2, 3.0f)));
+    f3 numer = vmul(lead, add3(vmul(a_b, s1), vmul(ab3, s2)));
+    f3 den = vmaxs(add3(a_b, vmul(ab3, add3(mul3s(beta_f, 2.0f), mul3s(beta_b, 3.0f)))), 1e-5f);
+    f3 sigma_b = vdiv(numer, den);
+    d.a_f = a_f;
+    d.beta_f2 = beta_f2;
+    d.a_back = a_back;
+    d.delta_b = delta_b;
+    d.sigma_b2 = vmul(sigma_b, sigma_b);
+    return d;
+}
+
+// hair_bsdf (shade.wesl:193-244)
+__device__ f3 hair_bsdf(f3 tangent, f3 view, f3 light, f3 sigma_a, const Shape& shape, const Dual& ds, float depth) {
+    f3 t = safe_normalize(tangent);
+    f3 v = safe_normalize(view);
+    f3 l = safe_normalize(light);
+    float sin_i = clampf(dot3(t, l), -1.0f, 1.0f);
+    float sin_o = clampf(dot3(t, v), -1.0f, 1.0f);
+    float theta_i = asinf(sin_i);
+    float theta_o = asinf(sin_o);
+    float theta_h = theta_i + theta_o;
+    float cos_theta_d = fmaxf(cosf(0.5f * fabsf(theta_i - theta_o)), 1e-3f);
+    f3 t_i = sub3(l, mul3s(t, sin_i));
+    f3 t_o = sub3(v, mul3s(t, sin_o));
+    float proj = sqrtf(fmaxf(dot3(t_i, t_i) * dot3(t_o, t_o), 1e-8f));
+    float cos_phi = clampf(dot3(t_i, t_o) / proj, -1.0f, 1.0f);
+    Lobes n = azimuthal(cos_theta_d, cos_phi, sigma_a);
+    f3 x = spl(theta_h);
+    f3 m = gaussian3(shape.beta, sub3(x, shape.alpha));
+    f3 single = add3(add3(mul3s(n.r, m.x), mul3s(n.tt, m.y)), mul3s(n.trt, m.z));
+    f3 g = gaussian3(vsqrt(ds.sigma_b2), sub3(x, ds.delta_b));
+    f3 back = mul3s(vmul(ds.a_back, g), 2.0f / kPi);
+    float direct = expf(-depth);
+    f3 color = mul3s(add3(single, mul3s(back, kDensityBack)), direct);
+    if (depth > 1e-3f) {
+        f3 sigma_f2 = mul3s(ds.beta_f2, depth);
+        f3 transmit = {powf(ds.a_f.x, depth), powf(ds.a_f.y, depth), powf(ds.a_f.z, depth)};
+        f3 beta2 = vmul(shape.beta, shape.beta);
+        f3 g0 = gaussian3(vsqrt(add3(spl(beta2.x), sigma_f2)), sub3(x, spl(shape.alpha.x)));
+        f3 g1 = gaussian3(vsqrt(add3(spl(beta2.y), sigma_f2)), sub3(x, spl(shape.alpha.y)));
+        f3 g2 = gaussian3(vsqrt(add3(spl(beta2.z), sigma_f2)), sub3(x, spl(shape.alpha.z)));
+        f3 spread = add3(add3(vmul(g0, ds.fwd.r), vmul(g1, ds.fwd.tt)), vmul(g2, ds.fwd.trt));
+        f3 gb = gaussian3(vsqrt(add3(ds.sigma_b2, sigma_f2)), sub3(x, ds.delta_b));
+        f3 back_spread = mul3s(vmul(ds.a_back, gb), 2.0f / kPi);
+        f3 inner = add3(mul3s(spread, 1.0f / kPi), mul3s(back_spread, kPi * kDensityBack));
+        color = add3(color, vmul(mul3s(transmit, (1.0f - direct) * kDensityFront), inner));
+    }
+    return color;
+}
+
+// dom_texel_visibility (shade.wesl:262-277)
+__device__ __forceinline__ float dom_texel_visibility(const uint32_t* __restrict__ dom, float sigma, int32_t x,
+                                                      int32_t y, float dist, float near_, float far_,
+                                                      uint32_t dom_w, uint32_t dom_h) {
+    if (x < 0 || y < 0 || x >= (int32_t)dom_w || y >= (int32_t)dom_h) return 1.0f;
+    uint32_t pix = (uint32_t)y * dom_w + (uint32_t)x;
+    uint32_t front_q = __ldg(&dom[pix]);
+    if (front_q == kDomEmpty) return 1.0f;
+    float z_front = dequantize_depth(front_q, near_, far_);
+    float thickness = fmaxf(far_ - near_, 1e-3f) / (float)kDomLayers;
+    float rel = fmaxf((dist - z_front) - thickness * 0.05f, 0.0f);
+    float t = rel / thickness;
+    // Counters start at word dom_w*dom_h, which need not be 16-byte aligned.
+    const uint32_t* c = dom + (size_t)dom_w * dom_h + (size_t)pix * kDomLayers;
+    float occ = 0.0f;
+#pragma unroll
+    for (int k = 0; k < (int)kDomLayers; ++k) {
+        float i = (float)k;
+        if (!(i < t)) break;
+        float count = __uint2float_rn(__ldg(c + k));
+        occ += i + 1.0f <= t ? count : count * (t - i);
+    }
+    return expf(-occ * sigma);
+}
+
+// dom_visibility (shade.wesl:279-310)
+__device__ float dom_visibility(const hg_hair_params& p, const uint32_t* __restrict__ dom, f3 world, float beta) {
+    if (p.flags[3] == 0u) return 1.0f;
+    float4 clip = mat_mul(p.light_clip_from_world, world.x, world.y, world.z, 1.0f);
+    if (clip.w <= 0.0f) return 1.0f;
+    float nx = clip.x / clip.w, ny = clip.y / clip.w;
+    float ux = nx * 0.5f + 0.5f, uy = 1.0f - (ny * 0.5f + 0.5f);
+    if (ux < 0.0f || uy < 0.0f || ux > 1.0f || uy > 1.0f) return 1.0f;
+    uint32_t dom_w = f2u(p.dom_info[0]), dom_h = f2u(p.dom_info[1]);
+    float near_ = p.dom_info[2], far_ = p.dom_info[3];
+    float dist = dot3(sub3(world, ld3(p.light_eye)), ld3(p.light_forward)) -
+                 (-logf(fmaxf(beta, 1e-4f)) * p.filter_params[2]);
+    float fx = ux * (float)dom_w - 0.5f, fy = uy * (float)dom_h - 0.5f;
+    float flx = floorf(fx), fly = floorf(fy);
+    int32_t x0 = f2i(flx), y0 = f2i(fly);
+    float tx = fx - flx, ty = fy - fly;
+    float sigma = p.filter_params[3];
+    float v00 = dom_texel_visibility(dom, sigma, x0, y0, dist, near_, far_, dom_w, dom_h);
+    float v10 = dom_texel_visibility(dom, sigma, x0 + 1, y0, dist, near_, far_, dom_w, dom_h);
+    float v01 = dom_texel_visibility(dom, sigma, x0, y0 + 1, dist, near_, far_, dom_w, dom_h);
+    float v11 = dom_texel_visibility(dom, sigma, x0 + 1, y0 + 1, dist, near_, far_, dom_w, dom_h);
+    return mixf(mixf(v00, v10, tx), mixf(v01, v11, tx), ty);
+}
+
+// Smooth range window and inverse-square falloff (Karis 2013; Lagarde and
+// de Rousiers 2014), standing in for bevy_pbr's getDistanceAttenuation.
+__device__ __forceinline__ float range_window(float dist2, float inv_range2) {
+    float factor = dist2 * inv_range2;
+    float s = clampf(1.0f - factor * factor, 0.0f, 1.0f);
+    return s * s;
+}
+
+struct ShadeArgs {
+    hg_hair_params p;
+    const unsigned long long* center;
+    const uint32_t* beta;
+    const uint32_t* dom;
+    const hg_light* lights;
+    float4* shaded;
+    float* shaded_depth;
+    uint32_t n_lights;
+    uint32_t ortho;
+    float exposure;
+};
+
+// fs (shade.wesl:523-593).  Lights arrive sorted by kind (point, spot,
+// directional, rect), the order the reference's loops visit them.
+__global__ void __launch_bounds__(256) shade_kernel(const ShadeArgs a) {
+    const hg_hair_params& p = a.p;
+    const uint32_t width = f2u(p.screen[0]), height = f2u(p.screen[1]);
+    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= width || y >= height) return;
+    const uint32_t pix = y * width + x;
+    const unsigned long long word = __ldg(&a.center[pix]);
+    if (is_empty(word)) {
+        a.shaded[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        a.shaded_depth[pix] = 0.0f;
+        return;
+    }
+    const uint32_t low = (uint32_t)word, high = (uint32_t)(word >> 32);
+    const uint32_t depth_q = high >> 8u;
+    const float view_dist = dequantize_depth(depth_q, p.screen[2], p.screen[3]);
+    const f3 world = reconstruct_world(p, (int32_t)x, (int32_t)y, view_dist);
+    const f3 tangent = oct_decode(high & 0xffu, low >> 24u);
+    const float uvw_z = (float)((low >> 6u) & 0x3fu) / 63.0f;
+    const float beta = (float)(__ldg(&a.beta[pix]) & 0xffu) / 255.0f;
+    const float roughness = fmaxf(p.appearance[0] * (0.65f + 0.7f * uvw_z), 0.04f);
+    const float tilt = p.appearance[1];
+    const float ascale = 0.65f + 0.35f * uvw_z;
+    const f3 albedo = {p.albedo[0] * ascale, p.albedo[1] * ascale, p.albedo[2] * ascale};
+    f3 view;
+    if (a.ortho) {
+        view = safe_normalize(mk3(p.clip_from_world[2], p.clip_from_world[6], p.clip_from_world[10]));
+    } else {
+        view = safe_normalize(sub3(ld3(p.camera_pos), world));
+    }
+
+    // direct_light (shade.wesl:429-521)
+    const Shape shape = lobe_shape(roughness, tilt);
+    const float tv = dot3(tangent, view);
+    const float cos_theta_o = sqrtf(fmaxf(1.0f - tv * tv, 1e-6f));
+    const f3 sigma_a = absorption_from_color(albedo, roughness);
+    const Dual ds = dual_scatter(cos_theta_o, sigma_a, shape);
+    f3 color = spl(0.0f);
+    bool dom_left = true;
+    for (uint32_t i = 0; i < a.n_lights; ++i) {
+        const hg_light& L = a.lights[i];
+        const uint32_t kind = L.kind;
+        if (kind == HG_LIGHT_POINT || kind == HG_LIGHT_SPOT) {
+            f3 to_l = sub3(ld3(L.position), world);
+            float dist2 = dot3(to_l, to_l);
+            f3 incident = safe_normalize(to_l);
+            float inv_r2 = 1.0f / fmaxf(L.range * L.range, 1e-8f);
+            float att = range_window(dist2, inv_r2) / fmaxf(dist2, 1e-4f);
+            if (kind == HG_LIGHT_SPOT) {
+                float cd = dot3(mul3s(ld3(L.direction), -1.0f), incident);
+                float sm = clampf(cd * L.spot[0] + L.spot[1], 0.0f, 1.0f);
+                att *= sm * sm;
+            }
+            if (att > 0.0f) {
+                f3 lobe = hair_bsdf(tangent, view, incident, sigma_a, shape, ds, 0.0f);
+                color = add3(color, mul3s(vmul(lobe, ld3(L.color)), att));
+            }
+        } else if (kind == HG_LIGHT_DIRECTIONAL) {
+            float depth = 0.0f;
+            if (dom_left && (L.flags & HG_LIGHT_CASTS_SHADOWS)) {
+                depth = -logf(fmaxf(dom_visibility(p, a.dom, world, beta), 1e-6f));
+                dom_left = false;
+            }
+            f3 lobe = hair_bsdf(tangent, view, ld3(L.direction), sigma_a, shape, ds, depth);
+            color = add3(color, vmul(lobe, ld3(L.color)));
+        } else if (kind == HG_LIGHT_RECT) {
+            f3 to_c = sub3(ld3(L.position), world);
+            float dist2 = fmaxf(dot3(to_c, to_c), 1e-4f);
+            f3 incident = mul3s(to_c, rsqrtf(dist2));
+            f3 normal = safe_normalize(cross3(ld3(L.up), ld3(L.right)));
+            float facing = fmaxf(dot3(normal, incident), 0.0f);
+            float solid = L.spot[0] * L.spot[1] * facing / dist2;
+            float range2 = fmaxf(L.range * L.range, 1e-4f);
+            float falloff = range_window(dist2, 1.0f / range2);
+            if (solid * falloff > 0.0f) {
+                f3 lobe = hair_bsdf(tangent, view, incident, sigma_a, shape, ds, 0.0f);
+                color = add3(color, mul3s(vmul(lobe, ld3(L.color)), solid * falloff));
+            }
+        }
+    }
+    color = mul3s(color, a.exposure);
+    a.shaded[pix] = make_float4(color.x, color.y, color.z, 1.0f);
+    a.shaded_depth[pix] = view_dist;
+}
+
+}  // namespace
+
+cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights, uint32_t ortho, float exposure,
+                         uint32_t model) {
+    (void)model;
+    ShadeArgs a;
+    a.p = p;
+    a.center = ctx->center;
+    a.beta = ctx->beta;
+    a.dom = ctx->dom;
+    a.lights = ctx->lights;
+    a.shaded = ctx->shaded;
+    a.shaded_depth = ctx->shaded_depth;
+    a.n_lights = n_lights;
+    a.ortho = ortho;
+    a.exposure = exposure;
+    dim3 block(32, 8);
+    dim3 grid((ctx->width + 31) / 32, (ctx->height + 7) / 8);
+    shade_kernel<<<grid, block, 0, ctx->stream>>>(a);
+    return cudaGetLastError();
+}
+
+}  // namespace hg

@@ -1,0 +1,286 @@
+/*
+ * hairgb.h -- C ABI of the GB300 (sm_103a) strand-hair pipeline.
+ *
+ * This library replaces the compute passes that bevy_hair's render host
+ * records per groom in `hair_pass` (src/render/pass.rs:259-657): clear, lod,
+ * scan, raster (camera), clear_dom + lod + scan + raster (deep opacity map,
+ * two modes), shade, filter and composite.  The host keeps the ECS glue
+ * (extract/prepare) and the uniform math (make_params, light_fit) and calls
+ * the entry points below instead of recording wgpu passes.
+ *
+ * Conventions
+ *  - Every entry point returns hg_status.  No entry point aborts, traps or
+ *    prints; hg_last_error() holds a one-line message for the last failure.
+ *  - All GPU work of one context is ordered on one CUDA stream (the one given
+ *    to hg_create, or a stream the context creates).  Calls enqueue work and
+ *    return; hg_synchronize() waits and reports device-side error words.
+ *  - Device memory is owned by the library.  Host arrays are read during the
+ *    call only.  Pointers returned by hg_buffer() stay valid until the next
+ *    hg_ensure_targets() that changes a size, or hg_destroy().
+ *  - Struct layouts are the reference's std140/std430 layouts byte for byte
+ *    (see the static asserts at the end of this header).
+ */
+#ifndef HAIRGB_H
+#define HAIRGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HG_ABI_VERSION 1u
+
+/* Layers per bundle cage; src/mesh.rs:10, common.wgsl:1. */
+#define HG_LAYER_COUNT 16u
+/* Style volume 8 x 8 x 16 texels per bundle; src/mesh.rs:11-14. */
+#define HG_STYLE_TEXELS 1024u
+/* Opacity slices behind each deep-opacity texel; src/render/pass.rs:24. */
+#define HG_DOM_LAYERS 16u
+/* Maximum lights in one shade call. */
+#define HG_MAX_LIGHTS 256u
+
+typedef enum hg_status {
+    HG_OK = 0,
+    HG_INVALID_ARG = 1,
+    HG_OUT_OF_MEMORY = 2,
+    HG_CUDA_ERROR = 3,
+    HG_CAPACITY_EXCEEDED = 4,
+    HG_DEVICE_TIMEOUT = 5,
+    HG_NOT_READY = 6,
+    HG_DEVICE_ERROR = 7
+} hg_status;
+
+/* HairParams uniform, 432 bytes (src/render/pass.rs:42-60,
+ * src/render/shaders/common.wgsl:10-28).  Matrices are column-major
+ * (glam to_cols_array_2d), so element [c*4 + r] is row r of column c. */
+typedef struct hg_hair_params {
+    float clip_from_world[16];
+    float world_from_clip[16];
+    float world_from_model[16];
+    float light_clip_from_world[16];
+    float camera_pos[4];
+    float camera_forward[4];
+    float screen[4];        /* width, height, near, far */
+    float appearance[4];    /* roughness, tilt, lambda, center_diameter */
+    float filter_params[4]; /* s_par, s_perp, dom_scale, dom_sigma */
+    float albedo[4];
+    uint32_t flags[4];      /* lod, filter, ambient_occlusion, deep_opacity */
+    uint32_t pass_mode[4];  /* mode (0 camera, 1 DOM depth, 2 DOM layers), bundle_count, reverse_z, dom_lod */
+    float light_eye[4];
+    float light_forward[4];
+    float dom_info[4];      /* dom_w, dom_h, light near, light far */
+} hg_hair_params;
+
+/* GpuBundle (src/render/pass.rs:71-78), 16 bytes. */
+typedef struct hg_gpu_bundle {
+    uint32_t layer_offset;
+    uint32_t style_offset;
+    uint32_t strand_count;
+    uint32_t pad;
+} hg_gpu_bundle;
+
+/* GpuLayer (src/render/pass.rs:64-69), 32 bytes: position + baked AO, tangent. */
+typedef struct hg_gpu_layer {
+    float pos_ao[4];
+    float tangent[4];
+} hg_gpu_layer;
+
+/* LodRecord (common.wgsl:42-47). */
+typedef struct hg_lod_record {
+    uint32_t n_lod;
+    uint32_t control_points;
+    uint32_t strand_count;
+    uint32_t pad;
+} hg_lod_record;
+
+/* StrandRef (common.wgsl:49-54). */
+typedef struct hg_strand_ref {
+    uint32_t bundle;
+    uint32_t strand;
+    uint32_t n_lod;
+    uint32_t control_points;
+} hg_strand_ref;
+
+/* Which LOD/refs/indirect set of a groom a pass uses.  A groom holds one set
+ * for the camera view and one for the deep-opacity view, like GpuGroom's
+ * camera_lod/camera_refs and dom_lod/dom_refs (src/render/pass.rs:80-96). */
+typedef enum hg_view_slot {
+    HG_SLOT_CAMERA = 0,
+    HG_SLOT_DOM = 1
+} hg_view_slot;
+
+typedef enum hg_light_kind {
+    HG_LIGHT_POINT = 0,
+    HG_LIGHT_SPOT = 1,
+    HG_LIGHT_DIRECTIONAL = 2,
+    HG_LIGHT_RECT = 3
+} hg_light_kind;
+
+#define HG_LIGHT_CASTS_SHADOWS 1u
+
+/* One light of the shade pass.  Replaces bevy_pbr's clustered light list,
+ * directional list and rect-light list that shade.wesl:452-518 reads.
+ *  point/spot: position, range (attenuation window), color = colour x intensity
+ *  spot:       direction = unit axis pointing away from the light,
+ *              spot[0..1] = angular scale/offset (cone mask clamp(cd*s+o,0,1)^2)
+ *  directional: direction = unit vector toward the light (direction_to_light),
+ *              color = colour x illuminance; CASTS_SHADOWS marks the light
+ *              that receives the deep-opacity optical depth (the first such)
+ *  rect:       position = centre, right/up = half axes, spot[0..1] = width,
+ *              height, range
+ * 112 bytes. */
+typedef struct hg_light {
+    uint32_t kind;
+    uint32_t flags;
+    float range;
+    float pad0;
+    float position[4];
+    float color[4];
+    float direction[4];
+    float spot[4];
+    float right[4];
+    float up[4];
+} hg_light;
+
+/* What the shade pass reads besides HairParams and the G-buffer.  The
+ * reference takes these from Bevy's view bind groups (shade.wesl:1-11). */
+typedef struct hg_shade_desc {
+    const hg_light* lights;   /* host array, light_count entries */
+    uint32_t light_count;
+    uint32_t ortho;           /* 1 when the camera projection is orthographic */
+    float exposure;           /* view.exposure */
+    uint32_t shade_model;     /* 0: Karis fit (shade.wesl), 1: learned surrogate */
+} hg_shade_desc;
+
+/* Buffers a context owns. */
+typedef enum hg_buffer_id {
+    HG_BUF_CENTER = 0,          /* u64[W*H] center-sample G-buffer */
+    HG_BUF_CONSERVATIVE = 1,    /* u64[W*H] conservative G-buffer */
+    HG_BUF_BETA = 2,            /* u32[W*H] (depth << 8 | beta8) side channel */
+    HG_BUF_DOM = 3,             /* u32[DW*DH*(1+16)] front depths, then 16 counters per texel */
+    HG_BUF_SHADED = 4,          /* float4[W*H] */
+    HG_BUF_SHADED_DEPTH = 5,    /* float[W*H] view distance */
+    HG_BUF_FILTERED = 6,        /* float4[W*H] */
+    HG_BUF_FILTERED_DEPTH = 7,  /* float[W*H] */
+    HG_BUF_COLOR = 8,           /* float4[W*H] composite target */
+    HG_BUF_DEPTH = 9            /* float[W*H] composite depth attachment */
+} hg_buffer_id;
+
+/* Groom buffers held on the device. */
+typedef enum hg_groom_buffer_id {
+    HG_GBUF_LOD = 0,        /* hg_lod_record[bundle_count] of the slot */
+    HG_GBUF_REFS = 1,       /* hg_strand_ref[max(strands,1)] of the slot */
+    HG_GBUF_INDIRECT = 2    /* u32[4]: (total refs, 1, 1, 0) of the slot */
+} hg_groom_buffer_id;
+
+typedef struct hg_ctx hg_ctx;
+typedef struct hg_groom hg_groom;
+
+/* Per-groom frame description: the per-groom body of hair_pass
+ * (src/render/pass.rs:375-643). */
+typedef struct hg_frame_desc {
+    const hg_hair_params* camera;       /* pass_mode.x == 0 */
+    const hg_hair_params* dom;          /* pass_mode.x == 1; may be NULL when flags[3]==0 */
+    const float* scene_depth;           /* device float[W*H] or NULL (no scene depth test) */
+    hg_shade_desc shade;
+    uint32_t composite;                 /* 1: blend into HG_BUF_COLOR/HG_BUF_DEPTH */
+    uint32_t clear_color;               /* 1: reset HG_BUF_COLOR to 0 and HG_BUF_DEPTH to the
+                                           far value of camera->pass_mode[2] before compositing */
+} hg_frame_desc;
+
+/* ---------------------------------------------------------------- context */
+
+/* device: CUDA ordinal.  stream: a cudaStream_t, or NULL for a stream the
+ * context creates and owns. */
+hg_status hg_create(int device, void* stream, hg_ctx** out);
+hg_status hg_destroy(hg_ctx* ctx);
+const char* hg_status_string(hg_status status);
+const char* hg_last_error(const hg_ctx* ctx);
+uint32_t hg_abi_version(void);
+
+/* Waits for the context's stream and reads the device error word.  Returns
+ * HG_DEVICE_ERROR (with the word in *device_error) when a kernel reported a
+ * bounds or capacity violation.  device_error may be NULL. */
+hg_status hg_synchronize(hg_ctx* ctx, uint32_t* device_error);
+
+/* Screen and deep-opacity targets; ensure_targets (src/render/pass.rs:789-815).
+ * The reference fixes the map at 512x512 (pass.rs:22); here it is a parameter. */
+hg_status hg_ensure_targets(hg_ctx* ctx, uint32_t width, uint32_t height,
+                            uint32_t dom_width, uint32_t dom_height);
+hg_status hg_buffer(hg_ctx* ctx, hg_buffer_id id, void** device_ptr, size_t* bytes);
+/* Copies a context buffer to host memory (bytes must equal its size). */
+hg_status hg_copy_out(hg_ctx* ctx, hg_buffer_id id, void* host, size_t bytes);
+/* Copies host memory into a context buffer (used to feed a pass its inputs). */
+hg_status hg_copy_in(hg_ctx* ctx, hg_buffer_id id, const void* host, size_t bytes);
+
+/* ---------------------------------------------------------------- grooms */
+
+/* GpuGroom::upload (src/render/pass.rs:98-167).  style is float4[style_count]
+ * (xyz residual, w unused).  Offsets are validated: every bundle needs
+ * layer_offset + 64 <= layer_count and style_offset + 1024 <= style_count. */
+hg_status hg_groom_upload(hg_ctx* ctx,
+                          const hg_gpu_bundle* bundles, uint32_t bundle_count,
+                          const hg_gpu_layer* layers, uint32_t layer_count,
+                          const float* style, uint32_t style_count,
+                          hg_groom** out);
+hg_status hg_groom_destroy(hg_ctx* ctx, hg_groom* groom);
+hg_status hg_groom_buffer(hg_ctx* ctx, hg_groom* groom, hg_view_slot slot,
+                          hg_groom_buffer_id id, void** device_ptr, size_t* bytes);
+/* Copies a groom buffer of a slot to host memory (bytes must equal its size). */
+hg_status hg_groom_copy_out(hg_ctx* ctx, hg_groom* groom, hg_view_slot slot,
+                            hg_groom_buffer_id id, void* host, size_t bytes);
+
+/* ---------------------------------------------------------------- passes */
+
+/* clear.wgsl:7-16: center = conservative = ~0, beta = 0xffffffff. */
+hg_status hg_clear(hg_ctx* ctx);
+/* clear_dom.wgsl:8-21: front depths = 0xffffffff, counters = 0. */
+hg_status hg_clear_dom(hg_ctx* ctx);
+/* lod.wgsl:6-59 into the slot's LodRecords. */
+hg_status hg_lod(hg_ctx* ctx, hg_groom* groom, const hg_hair_params* params, hg_view_slot slot);
+/* scan.wgsl:6-24: LodRecords -> StrandRefs + indirect (total,1,1). */
+hg_status hg_scan(hg_ctx* ctx, hg_groom* groom, const hg_hair_params* params, hg_view_slot slot);
+/* raster.wgsl:225-337 over the slot's refs.  params->pass_mode[0] selects the
+ * camera G-buffer (0) or the deep-opacity map (1 depth, 2 layers).
+ * scene_depth: device float[W*H] scene depth (raster.wgsl:93-100) or NULL. */
+hg_status hg_raster(hg_ctx* ctx, hg_groom* groom, const hg_hair_params* params,
+                    hg_view_slot slot, const float* scene_depth);
+/* shade.wesl:523-593 (Karis model) over every pixel. */
+hg_status hg_shade(hg_ctx* ctx, const hg_hair_params* params, const hg_shade_desc* desc);
+/* filter.wgsl:20-135. */
+hg_status hg_filter(hg_ctx* ctx, const hg_hair_params* params);
+/* composite.wgsl:162-181 plus the ALPHA_BLENDING blend state and the depth
+ * test of pipeline.rs:299-339, into HG_BUF_COLOR / HG_BUF_DEPTH.
+ * source_filtered selects filtered (1) or shaded (0) colour. */
+hg_status hg_composite(hg_ctx* ctx, const hg_hair_params* params, uint32_t source_filtered);
+/* Fills HG_BUF_COLOR with 0 and HG_BUF_DEPTH with depth_clear. */
+hg_status hg_clear_color(hg_ctx* ctx, float depth_clear);
+
+/* The whole per-groom sequence of hair_pass: clear, lod, scan, raster; when
+ * camera->flags[3] (deep_opacity): clear_dom, lod, scan, raster mode 1,
+ * raster mode 2; shade; filter when camera->flags[1]; composite. */
+hg_status hg_groom_frame(hg_ctx* ctx, hg_groom* groom, const hg_frame_desc* desc);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#ifdef __cplusplus
+static_assert(sizeof(hg_hair_params) == 432, "HairParams is 432 bytes (pipeline.rs:12)");
+static_assert(sizeof(hg_gpu_bundle) == 16, "GpuBundle is 16 bytes");
+static_assert(sizeof(hg_gpu_layer) == 32, "GpuLayer is 32 bytes");
+static_assert(sizeof(hg_lod_record) == 16, "LodRecord is 16 bytes");
+static_assert(sizeof(hg_strand_ref) == 16, "StrandRef is 16 bytes");
+static_assert(sizeof(hg_light) == 112, "hg_light is 112 bytes");
+#else
+_Static_assert(sizeof(hg_hair_params) == 432, "HairParams is 432 bytes (pipeline.rs:12)");
+_Static_assert(sizeof(hg_gpu_bundle) == 16, "GpuBundle is 16 bytes");
+_Static_assert(sizeof(hg_gpu_layer) == 32, "GpuLayer is 32 bytes");
+_Static_assert(sizeof(hg_lod_record) == 16, "LodRecord is 16 bytes");
+_Static_assert(sizeof(hg_strand_ref) == 16, "StrandRef is 16 bytes");
+_Static_assert(sizeof(hg_light) == 112, "hg_light is 112 bytes");
+#endif
+
+#endif /* HAIRGB_H */

@@ -1,0 +1,94 @@
+/*
+ * hair_oracle.h -- CPU oracle for the hair pipeline.  TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of bevy_hair's per-frame compute passes, used by the
+ * tests as the parity checker and by bench.py as the timed CPU baseline.  The
+ * product (libhairgb.so and the bevy_hair_gb300 package) never links, loads or
+ * calls it.
+ *
+ * Pinning: the reference cannot run here (it is a Rust/wgpu crate; no Rust
+ * toolchain and no graphics stack).  The oracle's helper functions are pinned
+ * against every known-answer test the reference holds for this path
+ * (src/gbuffer.rs:65-104, src/lod.rs:76-134, tests/golden/reference_kat.json).
+ * The raster, deep-opacity, shade, filter and composite pixel outputs have no
+ * reference test; for them the oracle defines the result ("parity unpinned"
+ * beyond the helper KATs).
+ *
+ * Float semantics the oracle defines (WGSL leaves them to the backend):
+ *  - f32 IEEE round-to-nearest, no FMA contraction (-ffp-contract=off), no FTZ;
+ *  - expressions evaluate left to right as written in the WGSL source;
+ *  - M * v sums columns in order: ((c0*x + c1*y) + c2*z) + c3*w;
+ *  - dot = ((ax*bx + ay*by) + az*bz); length = sqrt(dot); inverseSqrt(x) =
+ *    1/sqrt(x) with two correctly rounded steps; normalize(v) = v*inverseSqrt;
+ *  - mix(a, b, t) = a*(1-t) + b*t;  clamp(x, l, h) = min(max(x, l), h) with
+ *    IEEE minNum/maxNum (fminf/fmaxf);
+ *  - u32(f)/i32(f) truncate toward zero and saturate; NaN converts to 0;
+ *  - i32 add/sub wrap (two's complement);
+ *  - control_points_for_lod's pow(2, floor(log2(c - 1))) is evaluated exactly
+ *    (c - 1 is an integer in [15, 126]): 2^(index of the highest set bit).
+ */
+#ifndef HAIR_ORACLE_H
+#define HAIR_ORACLE_H
+
+#include <stdint.h>
+#include "../include/hairgb.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct oracle_counts {
+    uint64_t samples;        /* DDA samples (camera) or Bresenham visits (DOM) */
+    uint64_t cons_min;       /* atomicMin on conservative */
+    uint64_t center_min;     /* atomicMin on center */
+    uint64_t beta_min;       /* atomicMin on beta */
+    uint64_t dom_min;        /* mode 1 atomicMin */
+    uint64_t dom_add;        /* mode 2 atomicAdd */
+    uint64_t segments;       /* segments drawn (ncp - 1 per ref) */
+} oracle_counts;
+
+void oracle_set_threads(int n);
+int oracle_get_threads(void);
+
+/* helpers pinned by the reference KATs */
+uint32_t oracle_pcg(uint32_t x);
+uint64_t oracle_pack_gb(uint32_t depth, uint32_t tx, uint32_t ty, uint32_t u, uint32_t v, uint32_t w, uint32_t ao);
+void oracle_unpack_gb(uint64_t word, uint32_t out[7]);
+uint32_t oracle_pack_beta(uint32_t depth, float beta);
+uint32_t oracle_quantize_depth(float dist, float near_, float far_);
+float oracle_dequantize_depth(uint32_t depth, float near_, float far_);
+uint32_t oracle_control_points_for_lod(float l);
+float oracle_lod_selection(float extent, float screen_h, float lambda);
+uint32_t oracle_strand_count_lod(float l, uint32_t strand_count, float delta, int culled);
+float oracle_dom_optical_depth(const uint32_t* layers, uint32_t n_layers, float t);
+float oracle_depth_correction(float beta);
+void oracle_oct_encode(const float n[3], uint32_t out[2]);
+void oracle_oct_decode(uint32_t tx, uint32_t ty, float out[3]);
+
+/* passes */
+void oracle_clear(uint64_t* center, uint64_t* cons, uint32_t* beta, uint64_t pixels);
+void oracle_clear_dom(uint32_t* dom, uint64_t texels);
+void oracle_lod(const hg_hair_params* p, const hg_gpu_bundle* bundles, const hg_gpu_layer* layers,
+                hg_lod_record* lod_out);
+void oracle_scan(const hg_hair_params* p, const hg_lod_record* lod, hg_strand_ref* refs,
+                 uint32_t capacity, uint32_t indirect[4]);
+/* Control points of one strand as the raster generates them (model space):
+ * pos_ao[ncp*4], tan[ncp*4], uvw_ao[ncp*4].  Returns ncp. */
+uint32_t oracle_strand_points(const hg_gpu_bundle* bundles, const hg_gpu_layer* layers, const float* style,
+                              const hg_strand_ref* ref, float* pos_ao, float* tan, float* uvw_ao);
+void oracle_raster(const hg_hair_params* p, const hg_gpu_bundle* bundles, const hg_gpu_layer* layers,
+                   const float* style, const hg_strand_ref* refs, uint32_t n_refs,
+                   uint64_t* center, uint64_t* cons, uint32_t* beta, uint32_t* dom,
+                   const float* scene_depth, oracle_counts* counts);
+void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_t* beta, const uint32_t* dom,
+                  const hg_light* lights, uint32_t n_lights, uint32_t ortho, float exposure,
+                  float* shaded, float* shaded_depth);
+void oracle_filter(const hg_hair_params* p, const uint64_t* center, const uint64_t* cons,
+                   const float* shaded, const float* shaded_depth, float* filtered, float* filtered_depth);
+void oracle_composite(const hg_hair_params* p, const float* color_src, const float* depth_src,
+                      float* color_dst, float* depth_dst);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
