@@ -188,7 +188,12 @@ def run_ours(args, rank, world, local):
 
     torch.cuda.set_device(local)
     dist = Dist(world, "nccl")
-    stream = torch.cuda.current_stream()
+    # A dedicated stream shared by the library, the L2 flush and the timing
+    # events (the legacy default stream has handle 0, which hg_create would
+    # read as "make your own stream").
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    assert stream.cuda_stream != 0
     sc = configs.CONFIGS[args.config](args.scale)
     cam, dom = sc.params()
     lights = sc.light_array()

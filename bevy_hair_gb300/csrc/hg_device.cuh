@@ -103,8 +103,12 @@ __device__ __forceinline__ uint32_t quantize_depth(float dist, float near_, floa
     return r < 0x00fffffeu ? r : 0x00fffffeu;
 }
 
+// Explicitly rounded operations: the view distance is an output (shaded_depth,
+// filtered_depth), so it stays exact even in translation units built with FMA
+// contraction.
 __device__ __forceinline__ float dequantize_depth(uint32_t depth, float near_, float far_) {
-    return mixf(near_, far_, __fdiv_rn(__uint2float_rn(depth), 16777214.0f));
+    float t = __fdiv_rn(__uint2float_rn(depth), 16777214.0f);
+    return __fadd_rn(__fmul_rn(near_, __fsub_rn(1.0f, t)), __fmul_rn(far_, t));
 }
 
 __device__ __forceinline__ uint32_t quant63(float c) {
