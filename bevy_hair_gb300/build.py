@@ -26,11 +26,15 @@ BUILD_DIR = PKG / "_build"
 GENCODE = "-gencode=arch=compute_103a,code=sm_103a"
 NVCC_COMMON = [
     GENCODE, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-    "-prec-div=true", "-prec-sqrt=true", "-ftz=false",
     f"-I{ROOT / 'include'}",
 ]
+EXACT_FLAGS = ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]
 # Translation units whose float arithmetic feeds integer outputs.
 EXACT_UNITS = {"raster.cu", "filter.cu"}
+# Shading colour is compared within a tolerance; its exact outputs (view
+# distance, reconstructed position, decoded tangent) use explicitly rounded
+# intrinsics, which -use_fast_math does not change.
+FAST_UNITS = {"shade.cu"}
 CUDA_UNITS = ["api.cu", "raster.cu", "shade.cu", "filter.cu"]
 
 
@@ -69,7 +73,12 @@ def build_cuda(verbose_ptxas: bool = False, force: bool = False) -> Path:
         if not force and not _stale(obj, [src, *headers]):
             continue
         flags = list(NVCC_COMMON)
-        flags.append("-fmad=false" if unit in EXACT_UNITS else "-fmad=true")
+        if unit in EXACT_UNITS:
+            flags += EXACT_FLAGS
+        elif unit in FAST_UNITS:
+            flags.append("-use_fast_math")
+        else:
+            flags += ["-prec-div=true", "-prec-sqrt=true"]
         if verbose_ptxas:
             flags.append("-Xptxas=-v")
         jobs.append([nv, *flags, "-c", str(src), "-o", str(obj)])

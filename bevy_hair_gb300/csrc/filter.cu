@@ -34,11 +34,15 @@ __device__ __forceinline__ float2 screen_tangent(const hg_hair_params& p, f3 wor
     return make_float2(__fdiv_rn(d.x, l), __fdiv_rn(d.y, l));
 }
 
-// One 32x8 tile per CTA; the 42x18 neighbourhood of center/conservative
-// words is staged in shared memory once and read 121 times per pixel.
+// One 32x8 tile per CTA.  The 42x18 neighbourhood is staged in shared memory
+// once: per texel the centre word's normalised depth f32(depth)/16777214 (the
+// exact value filter.wgsl:94 computes per tap; -1 marks an empty centre with a
+// conservative hit, -2 both empty) and the shaded colour.  Coverage decisions
+// use exact arithmetic; the colour weights only scale colour, so they use the
+// fast exponential.
 __global__ void __launch_bounds__(kTileX* kTileY) filter_kernel(const FilterArgs a) {
-    __shared__ unsigned long long s_center[kHaloY][kHaloX];
-    __shared__ unsigned long long s_cons[kHaloY][kHaloX];
+    __shared__ float s_norm[kHaloY][kHaloX];
+    __shared__ float4 s_col[kHaloY][kHaloX];
     const hg_hair_params& p = a.p;
     const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
     const int32_t x0 = blockIdx.x * kTileX - kFilterRadius, y0 = blockIdx.y * kTileY - kFilterRadius;
@@ -46,28 +50,34 @@ __global__ void __launch_bounds__(kTileX* kTileY) filter_kernel(const FilterArgs
     for (int i = tid; i < kHaloX * kHaloY; i += kTileX * kTileY) {
         int hx = i % kHaloX, hy = i / kHaloX;
         int32_t gx = x0 + hx, gy = y0 + hy;
-        unsigned long long c = kEmptyU64, n = kEmptyU64;
+        float nrm = -2.0f;
+        float4 col = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         if (gx >= 0 && gy >= 0 && gx < width && gy < height) {
             size_t q = (size_t)gy * width + gx;
-            c = __ldg(&a.center[q]);
-            n = __ldg(&a.cons[q]);
+            unsigned long long c = __ldg(&a.center[q]);
+            if (!is_empty(c)) {
+                nrm = __fdiv_rn(__uint2float_rn((uint32_t)(c >> 40)), 16777214.0f);
+                col = __ldg(&a.shaded[q]);
+            } else if (!is_empty(__ldg(&a.cons[q]))) {
+                nrm = -1.0f;
+            }
         }
-        s_center[hy][hx] = c;
-        s_cons[hy][hx] = n;
+        s_norm[hy][hx] = nrm;
+        s_col[hy][hx] = col;
     }
     __syncthreads();
 
     const int32_t px = blockIdx.x * kTileX + threadIdx.x, py = blockIdx.y * kTileY + threadIdx.y;
     if (px >= width || py >= height) return;
     const uint32_t pix = (uint32_t)py * (uint32_t)width + (uint32_t)px;
-    const int lx = threadIdx.x + kFilterRadius, ly = threadIdx.y + kFilterRadius;
-    const unsigned long long center_word = s_center[ly][lx], cons_word = s_cons[ly][lx];
+    const unsigned long long center_word = __ldg(&a.center[pix]), cons_word = __ldg(&a.cons[pix]);
     const bool center_hit = !is_empty(center_word), cons_hit = !is_empty(cons_word);
     if (!center_hit && !cons_hit) {
         a.filtered[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         a.filtered_depth[pix] = 0.0f;
         return;
     }
+    const int lx = threadIdx.x + kFilterRadius, ly = threadIdx.y + kFilterRadius;
     const unsigned long long w = center_hit ? center_word : cons_word;
     const uint32_t high = (uint32_t)(w >> 32), low = (uint32_t)w;
     const f3 tangent = oct_decode(high & 0xffu, low >> 24u);
@@ -81,42 +91,45 @@ __global__ void __launch_bounds__(kTileX* kTileY) filter_kernel(const FilterArgs
     const float s_perp = fmaxf(p.filter_params[1], 0.02f);
     const float sigma_par = (float)kFilterRadius * s_par;
     const float sigma_perp = (float)kFilterRadius * s_perp;
-    const float sp2 = sigma_par * sigma_par, sq2 = sigma_perp * sigma_perp;
-    const float sigma_c = 0.9f, depth_reject = 1.45e-3f, closer_eps = 5e-4f, strip = 0.5f;
+    // exp(-x) = 2^(-x log2 e): the weights' scales folded into one factor each
+    const float k_par = 1.4426950408889634f / (sigma_par * sigma_par);
+    const float k_perp = 1.4426950408889634f / (sigma_perp * sigma_perp);
+    const float k_col = 1.4426950408889634f / (0.9f * 0.9f);
+    const float depth_reject = 1.45e-3f, closer_eps = 5e-4f, strip = 0.5f;
     const float p_norm = __fdiv_rn(__uint2float_rn(depth_q), 16777214.0f);
     const bool promote = !center_hit;
     const bool use_color = !promote && cc.w > 0.0f;
 
     float ax = 0.0f, ay = 0.0f, az = 0.0f, weight = 0.0f, h_center = 0.0f, h_cons = 0.0f;
+#pragma unroll 1
     for (int dy = -kFilterRadius; dy <= kFilterRadius; ++dy) {
+        const int32_t qy = py + dy;
+        if (qy < 0 || qy >= height) continue;
+#pragma unroll
         for (int dx = -kFilterRadius; dx <= kFilterRadius; ++dx) {
-            int32_t qx = px + dx, qy = py + dy;
-            if (qx < 0 || qy < 0 || qx >= width || qy >= height) continue;
-            float2 d = make_float2((float)dx, (float)dy);
-            float d_par = dot2(d, ts);
-            float d_perp = len2(make_float2(d.x - ts.x * d_par, d.y - ts.y * d_par));
-            unsigned long long qc = s_center[ly + dy][lx + dx];
-            bool qc_hit = !is_empty(qc);
+            const int32_t qx = px + dx;
+            if (qx < 0 || qx >= width) continue;
+            const float fdx = (float)dx, fdy = (float)dy;
+            const float d_par = fdx * ts.x + fdy * ts.y;
+            const float ex = fdx - ts.x * d_par, ey = fdy - ts.y * d_par;
+            const float d_perp = __fsqrt_rn(ex * ex + ey * ey);
+            const float nrm = s_norm[ly + dy][lx + dx];
             if (d_perp <= strip) {
-                if (qc_hit) {
+                if (nrm >= 0.0f) {
                     h_center += 1.0f;
-                } else if (!is_empty(s_cons[ly + dy][lx + dx])) {
+                } else if (nrm == -1.0f) {
                     h_cons += 1.0f;
                 }
             }
-            if (!qc_hit) continue;
-            float q_norm = __fdiv_rn(__uint2float_rn((uint32_t)(qc >> 40)), 16777214.0f);
-            if (fabsf(q_norm - p_norm) > depth_reject) continue;
-            float spatial = expf(__fdiv_rn(-d_par * d_par, sp2) - __fdiv_rn(d_perp * d_perp, sq2));
-            uint32_t qpix = (uint32_t)qy * (uint32_t)width + (uint32_t)qx;
-            float4 qcol = __ldg(&a.shaded[qpix]);
-            float color_w = 1.0f;
+            if (nrm < 0.0f) continue;
+            if (fabsf(nrm - p_norm) > depth_reject) continue;
+            const float4 qcol = s_col[ly + dy][lx + dx];
+            float e = d_par * d_par * k_par + d_perp * d_perp * k_perp;
             if (use_color) {
-                f3 dc = {cc.x - qcol.x, cc.y - qcol.y, cc.z - qcol.z};
-                float chroma = len3(dc);
-                color_w = expf(__fdiv_rn(-chroma * chroma, sigma_c * sigma_c));
+                const float cx = cc.x - qcol.x, cy = cc.y - qcol.y, cz = cc.z - qcol.z;
+                e += (cx * cx + cy * cy + cz * cz) * k_col;
             }
-            float wgt = spatial * color_w;
+            const float wgt = exp2f(-e);
             ax += qcol.x * wgt;
             ay += qcol.y * wgt;
             az += qcol.z * wgt;
@@ -125,9 +138,10 @@ __global__ void __launch_bounds__(kTileX* kTileY) filter_kernel(const FilterArgs
     }
     float cx = cc.x, cy = cc.y, cz = cc.z;
     if (weight > 1e-5f) {
-        cx = __fdiv_rn(ax, weight);
-        cy = __fdiv_rn(ay, weight);
-        cz = __fdiv_rn(az, weight);
+        const float inv = 1.0f / weight;
+        cx = ax * inv;
+        cy = ay * inv;
+        cz = az * inv;
     }
     const float coverage = __fdiv_rn(h_center, fmaxf(h_center + h_cons, 1.0f));
     const float cons_depth = cons_hit ? __fdiv_rn(__uint2float_rn((uint32_t)(cons_word >> 40)), 16777214.0f) : 1.0f;

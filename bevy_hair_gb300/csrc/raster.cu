@@ -204,16 +204,21 @@ __global__ void scan_expand_kernel(const hg_lod_record* __restrict__ lod, const 
 
 constexpr int kRasterWarps = 4;
 constexpr int kRasterThreads = kRasterWarps * 32;
+constexpr int kRasterMinBlocks = 7;  // 28 warps per SM: registers <= 73, shared memory 7 x 26.8 KB
 
+// Per-warp shared memory, 6.7 KB.  The layer samples are needed only while
+// control points are generated, so they share storage with the sample offsets.
 struct alignas(16) StrandSmem {
-    float4 lp[16];     // layer sample: position, ao
-    float4 lt[16];     // layer tangent
-    float4 cp[128];    // control point: model position + ao, then world position + in_front
-    float4 ct[128];    // control point tangent: model, then world
-    float4 cu[128];    // uv, w, ao
-    float2 cs[128];    // projected screen position
-    int32_t off[132];  // camera: exclusive sample offset per segment
-    int32_t sn[128];   // camera: DDA step count per segment
+    float4 cp[128];  // control point: model position, then world position + in_front flag
+    float4 ct[128];  // camera: world tangent xyz + w (uvw.z)
+    float4 cs[128];  // screen xy, ao, DDA step count n of the segment starting here (int bits)
+    union {
+        struct {
+            float4 lp[16];  // layer sample: position, ao
+            float4 lt[16];  // layer tangent
+        } gen;
+        int32_t off[132];  // camera: exclusive sample offset per segment
+    } u;
 };
 
 struct RasterArgs {
@@ -280,12 +285,27 @@ __device__ __forceinline__ float4 shfl_down4(float4 v, int d) {
                        __shfl_down_sync(0xffffffffu, v.z, d), __shfl_down_sync(0xffffffffu, v.w, d));
 }
 
+__device__ __forceinline__ f3 shfl_up3(f3 v) {
+    return {__shfl_up_sync(0xffffffffu, v.x, 1), __shfl_up_sync(0xffffffffu, v.y, 1),
+            __shfl_up_sync(0xffffffffu, v.z, 1)};
+}
+__device__ __forceinline__ f3 shfl_down3(f3 v) {
+    return {__shfl_down_sync(0xffffffffu, v.x, 1), __shfl_down_sync(0xffffffffu, v.y, 1),
+            __shfl_down_sync(0xffffffffu, v.z, 1)};
+}
+__device__ __forceinline__ f3 shfl_idx3(f3 v, int src) {
+    return {__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src),
+            __shfl_sync(0xffffffffu, v.z, src)};
+}
+
 // Strand generation (raster.wgsl:231-317) for one warp.  Leaves world-space
-// control points, tangents, uvw/ao and screen positions in shared memory.
+// control points (+ in_front), screen positions and, for the camera pass,
+// world tangents, w and ao in shared memory.  The DOM passes need positions
+// only, so they skip the tangents.
+template <int MODE>
 __device__ __forceinline__ uint32_t generate_strand(const RasterArgs& a, StrandSmem& sm, const hg_strand_ref& ref,
-                                                    const hg_gpu_bundle& bundle, uint32_t lane) {
+                                                    const hg_gpu_bundle& bundle, float2 uv, uint32_t lane) {
     const hg_hair_params& p = a.p;
-    float2 uv = pcg_uv(ref.strand ^ (ref.bundle * 0x85ebca6bu));
     // Layer samples on lanes 0..15; neighbours come over shuffles.
     float4 loaded = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (lane < kLayerCount) {
@@ -299,57 +319,70 @@ __device__ __forceinline__ uint32_t generate_strand(const RasterArgs& a, StrandS
         f3 prev = lane == 0u ? curr : xyz(prev_l);
         f3 next = lane + 1u >= kLayerCount ? curr : xyz(next_l);
         f3 t = calc_tangent(lane, kLayerCount, prev, curr, next);
-        sm.lp[lane] = loaded;
-        sm.lt[lane] = make_float4(t.x, t.y, t.z, 0.0f);
+        sm.u.gen.lp[lane] = loaded;
+        sm.u.gen.lt[lane] = make_float4(t.x, t.y, t.z, 0.0f);
     }
     __syncwarp();
 
-    uint32_t ncp = min(max(ref.control_points, 2u), 127u);
-    float den = __uint2float_rn(max(ncp - 1u, 1u));
-    // eval_cp (raster.wgsl:62-75), control point j on lane j % 32.
-    for (uint32_t idx = lane; idx < ncp; idx += 32u) {
-        float w = __fdiv_rn(__uint2float_rn(idx), den);
-        float layers_f = w * (float)(kLayerCount - 1u);
-        uint32_t i0 = min(f2u(floorf(layers_f)), kLayerCount - 1u);
-        uint32_t i1 = min(i0 + 1u, kLayerCount - 1u);
-        float t = layers_f - __uint2float_rn(i0);
-        float4 la = sm.lp[i0], lb = sm.lp[i1];
-        f3 base = hermite(xyz(la), xyz(lb), xyz(sm.lt[i0]), xyz(sm.lt[i1]), t);
-        float ao = mixf(la.w, lb.w, t);
-        f3 res = sample_style(a.style, bundle.style_offset, uv, w);
-        f3 pos = add3(base, res);
-        sm.cp[idx] = make_float4(pos.x, pos.y, pos.z, ao);
-        sm.cu[idx] = make_float4(uv.x, uv.y, w, ao);
-    }
-    __syncwarp();
-
-    // Control-point tangents (raster.wgsl:286-317), then world space and projection.
-    f3 wp[4], wt[4];
-    float2 sc[4];
-    bool fr[4];
+    const uint32_t ncp = min(max(ref.control_points, 2u), 127u);
+    const float den = __uint2float_rn(max(ncp - 1u, 1u));
+    // eval_cp (raster.wgsl:62-75): control point j lives on lane j % 32, slot j / 32.
+    f3 mp[4];
+    float wk[4], aok[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        uint32_t idx = lane + 32u * k;
+        const uint32_t idx = lane + 32u * k;
+        mp[k] = mk3(0.0f, 0.0f, 0.0f);
+        wk[k] = aok[k] = 0.0f;
         if (idx < ncp) {
-            f3 curr = xyz(sm.cp[idx]);
-            f3 prev = idx > 0u ? xyz(sm.cp[idx - 1u]) : curr;
-            f3 next = idx + 1u < ncp ? xyz(sm.cp[idx + 1u]) : curr;
-            f3 tm = safe_normalize(calc_tangent(idx, ncp, prev, curr, next));
-            wp[k] = to_world(p, curr);
-            wt[k] = dir_world(p, tm);
-            Projected pr = project_world(p, wp[k]);
-            sc[k] = pr.screen;
-            fr[k] = pr.in_front;
+            float w = __fdiv_rn(__uint2float_rn(idx), den);
+            float layers_f = w * (float)(kLayerCount - 1u);
+            uint32_t i0 = min(f2u(floorf(layers_f)), kLayerCount - 1u);
+            uint32_t i1 = min(i0 + 1u, kLayerCount - 1u);
+            float t = layers_f - __uint2float_rn(i0);
+            float4 la = sm.u.gen.lp[i0], lb = sm.u.gen.lp[i1];
+            f3 base = hermite(xyz(la), xyz(lb), xyz(sm.u.gen.lt[i0]), xyz(sm.u.gen.lt[i1]), t);
+            f3 res = sample_style(a.style, bundle.style_offset, uv, w);
+            mp[k] = add3(base, res);
+            wk[k] = w;
+            aok[k] = mixf(la.w, lb.w, t);
         }
     }
-    __syncwarp();
+
+    // Control-point tangents (raster.wgsl:286-317): neighbours j-1 and j+1 are
+    // the next lane down/up of the same slot, or lane 31 / lane 0 of the
+    // adjacent slot.  Then world space and projection, stored once.
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-        uint32_t idx = lane + 32u * k;
+        const uint32_t idx = lane + 32u * k;
+        f3 prev = mp[k], next = mp[k];
+        if (MODE == 0) {
+            prev = shfl_up3(mp[k]);
+            next = shfl_down3(mp[k]);
+            if (k > 0) {
+                f3 w31 = shfl_idx3(mp[k > 0 ? k - 1 : 0], 31);
+                if (lane == 0) prev = w31;
+            }
+            if (k < 3) {
+                f3 w0 = shfl_idx3(mp[k < 3 ? k + 1 : 3], 0);
+                if (lane == 31) next = w0;
+            }
+        }
         if (idx < ncp) {
-            sm.cp[idx] = make_float4(wp[k].x, wp[k].y, wp[k].z, fr[k] ? 1.0f : 0.0f);
-            sm.ct[idx] = make_float4(wt[k].x, wt[k].y, wt[k].z, 0.0f);
-            sm.cs[idx] = sc[k];
+            const f3 curr = mp[k];
+            const f3 wp = to_world(p, curr);
+            const Projected pr = project_world(p, wp);
+            sm.cp[idx] = make_float4(wp.x, wp.y, wp.z, pr.in_front ? 1.0f : 0.0f);
+            if (MODE == 0) {
+                f3 pp = idx > 0u ? prev : curr;
+                f3 nn = idx + 1u < ncp ? next : curr;
+                f3 tm = safe_normalize(calc_tangent(idx, ncp, pp, curr, nn));
+                f3 wt = dir_world(p, tm);
+                sm.ct[idx] = make_float4(wt.x, wt.y, wt.z, wk[k]);
+                sm.cs[idx] = make_float4(pr.screen.x, pr.screen.y, aok[k], 0.0f);
+            } else {
+                sm.cs[idx] = make_float4(pr.screen.x, pr.screen.y, 0.0f, 0.0f);
+            }
         }
     }
     __syncwarp();
@@ -374,13 +407,20 @@ __device__ __forceinline__ void camera_write(const RasterArgs& a, int32_t px, in
     }
 }
 
+__device__ __forceinline__ bool on_screen(int32_t x, int32_t y, int32_t w, int32_t h) {
+    return x >= 0 && y >= 0 && x < w && y < h;
+}
+
 // Camera raster of one generated strand.  The DDA of every segment
 // (raster.wgsl:192-223) is flattened into one list of samples so the 32 lanes
-// share the work evenly; each sample computes its payload once
-// (raster.wgsl:83-108) and writes the centre pixel plus, on a diagonal step,
-// the two side pixels.
-__device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& sm, uint32_t ncp, float beta,
-                                              uint32_t lane) {
+// share the work evenly.  Consecutive samples sit on consecutive lanes, so the
+// previous step's pixel (for the diagonal side pixels) comes from the
+// neighbouring lane, or from lane 31 of the previous round; it is the same
+// floor(mix(a, b, (i-1)/n)) the DDA loop carries.  Each sample computes its
+// payload once (raster.wgsl:83-108) and writes the centre pixel and, on a
+// diagonal step, the two side pixels.
+__device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& sm, uint32_t ncp, float2 uv,
+                                              float beta, uint32_t lane) {
     const hg_hair_params& p = a.p;
     const int32_t nseg = (int32_t)ncp - 1;
     int32_t carry = 0;
@@ -392,13 +432,13 @@ __device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& s
             float4 pa = sm.cp[j], pb = sm.cp[j + 1];
             int32_t n = 0;
             if (pa.w != 0.0f || pb.w != 0.0f) {
-                float2 A = sm.cs[j], B = sm.cs[j + 1];
-                float2 d = sub2(B, A);
-                int32_t steps = f2i(ceilf(fmaxf(fabsf(d.x), fabsf(d.y))));
+                float4 A = sm.cs[j], B = sm.cs[j + 1];
+                float dx = B.x - A.x, dy = B.y - A.y;
+                int32_t steps = f2i(ceilf(fmaxf(fabsf(dx), fabsf(dy))));
                 n = min(max(steps, 1), 96);
                 cnt = n + 1;
             }
-            sm.sn[j] = n;
+            sm.cs[j].w = __int_as_float(n);
         }
         int32_t incl = cnt;
 #pragma unroll
@@ -406,50 +446,63 @@ __device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& s
             int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
             if ((int32_t)lane >= o) incl += y;
         }
-        if (j < nseg) sm.off[j] = carry + incl - cnt;
+        if (j < nseg) sm.u.off[j] = carry + incl - cnt;
         carry += __shfl_sync(0xffffffffu, incl, 31);
     }
-    if (lane == 0) sm.off[nseg] = carry;
+    if (lane == 0) sm.u.off[nseg] = carry;
     __syncwarp();
 
     const int32_t total = carry;
     const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
-    const float diameter = fmaxf(p.appearance[3], 0.05f);
+    const float half_diameter = fmaxf(p.appearance[3], 0.05f) * 0.5f;
     const f3 cam = mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2]);
     const f3 fwd = mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]);
     const uint32_t beta_q = f2u(clampf(beta, 0.0f, 1.0f) * 255.0f + 0.5f);
-    for (int32_t s = (int32_t)lane; s < total; s += 32) {
+    const bool ao_on = p.flags[2] != 0u;
+    int32_t carry_px = 0, carry_py = 0;
+    for (int32_t base = 0; base < total; base += 32) {
+        const int32_t s = min(base + (int32_t)lane, total - 1);
+        const bool active = base + (int32_t)lane < total;
         // segment j with off[j] <= s < off[j+1]
         int32_t lo = 0, hi = nseg - 1;
         while (lo < hi) {
             int32_t mid = (lo + hi + 1) >> 1;
-            if (sm.off[mid] <= s) lo = mid; else hi = mid - 1;
+            if (sm.u.off[mid] <= s) lo = mid; else hi = mid - 1;
         }
         const int32_t j = lo;
-        const int32_t i = s - sm.off[j];
-        const int32_t n = sm.sn[j];
-        const float2 A = sm.cs[j], B = sm.cs[j + 1];
-        const float fn = __int2float_rn(n);
-        const float t = __fdiv_rn(__int2float_rn(i), fn);
-        const float2 scr = mix2(A, B, t);
-        const int32_t px = f2i(floorf(scr.x)), py = f2i(floorf(scr.y));
-        const float2 ctr = make_float2(__int2float_rn(px) + 0.5f, __int2float_rn(py) + 0.5f);
-        const float2 seg = sub2(B, A);
-        const float denom = fmaxf(dot2(seg, seg), 1e-6f);
-        const float closest = clampf(__fdiv_rn(dot2(sub2(ctr, A), seg), denom), 0.0f, 1.0f);
-        const float2 onl = make_float2(A.x + seg.x * closest, A.y + seg.y * closest);
-        const bool center_hit = len2(sub2(ctr, onl)) <= diameter * 0.5f;
+        const int32_t i = s - sm.u.off[j];
+        const float4 A = sm.cs[j], B = sm.cs[j + 1];
+        const int32_t n = __float_as_int(A.w);
+        const float t = __fdiv_rn(__int2float_rn(i), __int2float_rn(n));
+        const float sx = mixf(A.x, B.x, t), sy = mixf(A.y, B.y, t);
+        const int32_t px = f2i(floorf(sx)), py = f2i(floorf(sy));
+        int32_t qx = __shfl_up_sync(0xffffffffu, px, 1), qy = __shfl_up_sync(0xffffffffu, py, 1);
+        if (lane == 0) {
+            qx = carry_px;
+            qy = carry_py;
+        }
+        carry_px = __shfl_sync(0xffffffffu, px, 31);
+        carry_py = __shfl_sync(0xffffffffu, py, 31);
+        if (!active) continue;
+        const bool side = i > 0 && qx != px && qy != py;
+        if (!on_screen(px, py, width, height) &&
+            !(side && (on_screen(qx, py, width, height) || on_screen(px, qy, width, height))))
+            continue;
 
-        // Payload (write_pixel, raster.wgsl:83-108); identical for the side pixels.
+        const float cx = __int2float_rn(px) + 0.5f, cy = __int2float_rn(py) + 0.5f;
+        const float gx = B.x - A.x, gy = B.y - A.y;
+        const float denom = fmaxf(gx * gx + gy * gy, 1e-6f);
+        const float closest = clampf(__fdiv_rn((cx - A.x) * gx + (cy - A.y) * gy, denom), 0.0f, 1.0f);
+        const float ox = cx - (A.x + gx * closest), oy = cy - (A.y + gy * closest);
+        const bool center_hit = __fsqrt_rn(ox * ox + oy * oy) <= half_diameter;
+
+        // Payload (write_pixel, raster.wgsl:83-108); the side pixels reuse it.
         const float4 c0 = sm.cp[j], c1 = sm.cp[j + 1];
         const f3 world = mix3(xyz(c0), xyz(c1), t);
         const float dist = dot3(sub3(world, cam), fwd);
         if (dist <= p.screen[2]) continue;
         const float4 t0 = sm.ct[j], t1 = sm.ct[j + 1];
         const f3 tangent = safe_normalize(mix3(xyz(t0), xyz(t1), t));
-        const float4 u0 = sm.cu[j], u1 = sm.cu[j + 1];
-        const f3 uvw = mix3(xyz(u0), xyz(u1), t);
-        const float ao = mixf(u0.w, u1.w, t);
         float clip_depth = 0.0f;
         if (a.scene) {
             float4 clip = mat_mul(p.clip_from_world, world.x, world.y, world.z, 1.0f);
@@ -457,20 +510,14 @@ __device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& s
         }
         const uint32_t depth = quantize_depth(dist, p.screen[2], p.screen[3]);
         const uint32_t oct = oct_encode(tangent);
-        uint32_t ao_q = f2u(clampf(ao, 0.0f, 1.0f) * 63.0f + 0.5f);
-        if (p.flags[2] == 0u) ao_q = 63u;
-        const unsigned long long payload =
-            pack_gb(depth, oct & 0xffu, oct >> 8u, quant63(uvw.x), quant63(uvw.y), quant63(uvw.z), ao_q);
+        const uint32_t ao_q = ao_on ? f2u(clampf(mixf(A.z, B.z, t), 0.0f, 1.0f) * 63.0f + 0.5f) : 63u;
+        const unsigned long long payload = pack_gb(depth, oct & 0xffu, oct >> 8u, quant63(mixf(uv.x, uv.x, t)),
+                                                   quant63(mixf(uv.y, uv.y, t)), quant63(mixf(t0.w, t1.w, t)), ao_q);
         const uint32_t beta_word = (depth << 8u) | beta_q;
         camera_write(a, px, py, width, height, clip_depth, payload, center_hit, beta_word);
-        if (i > 0) {
-            const float tp = __fdiv_rn(__int2float_rn(i - 1), fn);
-            const float2 prev = mix2(A, B, tp);
-            const int32_t qx = f2i(floorf(prev.x)), qy = f2i(floorf(prev.y));
-            if (qx != px && qy != py) {
-                camera_write(a, qx, py, width, height, clip_depth, payload, false, beta_word);
-                camera_write(a, px, qy, width, height, clip_depth, payload, false, beta_word);
-            }
+        if (side) {
+            camera_write(a, qx, py, width, height, clip_depth, payload, false, beta_word);
+            camera_write(a, px, qy, width, height, clip_depth, payload, false, beta_word);
         }
     }
 }
@@ -510,7 +557,8 @@ __device__ __forceinline__ void raster_dom(const RasterArgs& a, StrandSmem& sm, 
     for (uint32_t j = lane; j + 1u < ncp; j += 32u) {
         float4 c0 = sm.cp[j], c1 = sm.cp[j + 1u];
         if (c0.w == 0.0f && c1.w == 0.0f) continue;
-        float2 A = sm.cs[j], B = sm.cs[j + 1u];
+        float4 A4 = sm.cs[j], B4 = sm.cs[j + 1u];
+        float2 A = make_float2(A4.x, A4.y), B = make_float2(B4.x, B4.y);
         int32_t x0 = f2i(floorf(A.x)), y0 = f2i(floorf(A.y));
         int32_t x1 = f2i(floorf(B.x)), y1 = f2i(floorf(B.y));
         int32_t dx = iabs(isub(x1, x0)), dy = iabs(isub(y1, y0));
@@ -544,7 +592,7 @@ __device__ __forceinline__ void raster_dom(const RasterArgs& a, StrandSmem& sm, 
 
 // raster.wgsl:225-337: one warp per strand ref, persistent over the refs.
 template <int MODE>
-__global__ void __launch_bounds__(kRasterThreads) raster_kernel(const RasterArgs a) {
+__global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) raster_kernel(const RasterArgs a) {
     __shared__ StrandSmem smem[kRasterWarps];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     StrandSmem& sm = smem[warp];
@@ -557,10 +605,11 @@ __global__ void __launch_bounds__(kRasterThreads) raster_kernel(const RasterArgs
             continue;
         }
         const hg_gpu_bundle bundle = a.bundles[ref.bundle];
-        const uint32_t ncp = generate_strand(a, sm, ref, bundle, lane);
+        const float2 uv = pcg_uv(ref.strand ^ (ref.bundle * 0x85ebca6bu));
+        const uint32_t ncp = generate_strand<MODE>(a, sm, ref, bundle, uv, lane);
         if (MODE == 0) {
             float beta = __fdiv_rn(__uint2float_rn(ref.n_lod), __uint2float_rn(max(bundle.strand_count, 1u)));
-            raster_camera(a, sm, ncp, beta, lane);
+            raster_camera(a, sm, ncp, uv, beta, lane);
         } else {
             raster_dom<MODE>(a, sm, ncp, lane);
         }

@@ -260,7 +260,7 @@ struct ShadeArgs {
 
 // fs (shade.wesl:523-593).  Lights arrive sorted by kind (point, spot,
 // directional, rect), the order the reference's loops visit them.
-__global__ void __launch_bounds__(256) shade_kernel(const ShadeArgs a) {
+__global__ void __launch_bounds__(256, 3) shade_kernel(const ShadeArgs a) {
     const hg_hair_params& p = a.p;
     const uint32_t width = f2u(p.screen[0]), height = f2u(p.screen[1]);
     const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
