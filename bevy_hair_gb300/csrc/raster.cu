@@ -389,24 +389,6 @@ __device__ __forceinline__ uint32_t generate_strand(const RasterArgs& a, StrandS
     return ncp;
 }
 
-// write_pixel's atomics (raster.wgsl:109-115) for one pixel of a sample whose
-// payload is already known.
-__device__ __forceinline__ void camera_write(const RasterArgs& a, int32_t px, int32_t py, int32_t width,
-                                             int32_t height, float clip_depth, unsigned long long payload,
-                                             bool center_hit, uint32_t beta_word) {
-    if (px < 0 || py < 0 || px >= width || py >= height) return;
-    uint32_t pix = (uint32_t)py * (uint32_t)width + (uint32_t)px;
-    if (a.scene) {
-        float scene = __ldg(&a.scene[pix]);
-        if (a.p.pass_mode[2] == 1u ? clip_depth < scene : clip_depth > scene) return;
-    }
-    atomicMin(&a.cons[pix], payload);
-    if (center_hit) {
-        atomicMin(&a.center[pix], payload);
-        atomicMin(&a.beta[pix], beta_word);
-    }
-}
-
 __device__ __forceinline__ bool on_screen(int32_t x, int32_t y, int32_t w, int32_t h) {
     return x >= 0 && y >= 0 && x < w && y < h;
 }
@@ -485,9 +467,20 @@ __device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& s
         carry_py = __shfl_sync(0xffffffffu, py, 31);
         if (!active) continue;
         const bool side = i > 0 && qx != px && qy != py;
-        if (!on_screen(px, py, width, height) &&
-            !(side && (on_screen(qx, py, width, height) || on_screen(px, qy, width, height))))
-            continue;
+        const bool on0 = on_screen(px, py, width, height);
+        const bool on1 = side && on_screen(qx, py, width, height);
+        const bool on2 = side && on_screen(px, qy, width, height);
+        if (!(on0 || on1 || on2)) continue;
+        const uint32_t pix0 = (uint32_t)py * (uint32_t)width + (uint32_t)px;
+        const uint32_t pix1 = (uint32_t)py * (uint32_t)width + (uint32_t)qx;
+        const uint32_t pix2 = (uint32_t)qy * (uint32_t)width + (uint32_t)px;
+        // Current words, read from L2 before the payload is known.  Buffers only
+        // decrease during the pass, so a stale read is an upper bound: an atomicMin
+        // is skipped only when it cannot change the word.
+        const unsigned long long cur_c0 = on0 ? __ldcg(&a.cons[pix0]) : 0ull;
+        const unsigned long long cur_m0 = on0 ? __ldcg(&a.center[pix0]) : 0ull;
+        const unsigned long long cur_c1 = on1 ? __ldcg(&a.cons[pix1]) : 0ull;
+        const unsigned long long cur_c2 = on2 ? __ldcg(&a.cons[pix2]) : 0ull;
 
         const float cx = __int2float_rn(px) + 0.5f, cy = __int2float_rn(py) + 0.5f;
         const float gx = B.x - A.x, gy = B.y - A.y;
@@ -496,56 +489,78 @@ __device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& s
         const float ox = cx - (A.x + gx * closest), oy = cy - (A.y + gy * closest);
         const bool center_hit = __fsqrt_rn(ox * ox + oy * oy) <= half_diameter;
 
-        // Payload (write_pixel, raster.wgsl:83-108); the side pixels reuse it.
+        // write_pixel (raster.wgsl:83-115): depth first; the rest of the payload
+        // only when some word can still take it.
         const float4 c0 = sm.cp[j], c1 = sm.cp[j + 1];
         const f3 world = mix3(xyz(c0), xyz(c1), t);
         const float dist = dot3(sub3(world, cam), fwd);
         if (dist <= p.screen[2]) continue;
+        const uint32_t depth = quantize_depth(dist, p.screen[2], p.screen[3]);
+        const unsigned long long lower = (unsigned long long)depth << 40;  // smallest payload with this depth
+        bool w0 = on0 && lower < cur_c0;
+        bool wm = on0 && center_hit && depth <= (uint32_t)(cur_m0 >> 40);
+        bool w1 = on1 && lower < cur_c1;
+        bool w2 = on2 && lower < cur_c2;
+        if (!(w0 || wm || w1 || w2)) continue;
+        if (a.scene) {
+            const float4 clip = mat_mul(p.clip_from_world, world.x, world.y, world.z, 1.0f);
+            const float clip_depth = __fdiv_rn(clip.z, fmaxf(clip.w, 1e-5f));
+            const bool rev = p.pass_mode[2] == 1u;
+            auto hidden = [&](uint32_t pix) {
+                const float scene = __ldg(&a.scene[pix]);
+                return rev ? clip_depth < scene : clip_depth > scene;
+            };
+            if ((w0 || wm) && hidden(pix0)) w0 = wm = false;
+            if (w1 && hidden(pix1)) w1 = false;
+            if (w2 && hidden(pix2)) w2 = false;
+            if (!(w0 || wm || w1 || w2)) continue;
+        }
         const float4 t0 = sm.ct[j], t1 = sm.ct[j + 1];
         const f3 tangent = safe_normalize(mix3(xyz(t0), xyz(t1), t));
-        float clip_depth = 0.0f;
-        if (a.scene) {
-            float4 clip = mat_mul(p.clip_from_world, world.x, world.y, world.z, 1.0f);
-            clip_depth = __fdiv_rn(clip.z, fmaxf(clip.w, 1e-5f));
-        }
-        const uint32_t depth = quantize_depth(dist, p.screen[2], p.screen[3]);
         const uint32_t oct = oct_encode(tangent);
         const uint32_t ao_q = ao_on ? f2u(clampf(mixf(A.z, B.z, t), 0.0f, 1.0f) * 63.0f + 0.5f) : 63u;
         const unsigned long long payload = pack_gb(depth, oct & 0xffu, oct >> 8u, quant63(mixf(uv.x, uv.x, t)),
                                                    quant63(mixf(uv.y, uv.y, t)), quant63(mixf(t0.w, t1.w, t)), ao_q);
-        const uint32_t beta_word = (depth << 8u) | beta_q;
-        camera_write(a, px, py, width, height, clip_depth, payload, center_hit, beta_word);
-        if (side) {
-            camera_write(a, qx, py, width, height, clip_depth, payload, false, beta_word);
-            camera_write(a, px, qy, width, height, clip_depth, payload, false, beta_word);
+        if (w0 && payload < cur_c0) atomicMin(&a.cons[pix0], payload);
+        if (wm) {
+            if (payload < cur_m0) atomicMin(&a.center[pix0], payload);
+            atomicMin(&a.beta[pix0], (depth << 8u) | beta_q);
         }
+        if (w1 && payload < cur_c1) atomicMin(&a.cons[pix1], payload);
+        if (w2 && payload < cur_c2) atomicMin(&a.cons[pix2], payload);
     }
 }
 
-// write_dom_pixel (raster.wgsl:118-148)
+// write_dom_pixel (raster.wgsl:118-148) for the Bresenham pixel (px, py) of
+// the segment p0-p1 (screen a -> a + seg).  The texel's front depth is read
+// before the sample position is computed; mode 1 skips an atomicMin that
+// cannot lower it (the map only decreases during the pass).
 template <int MODE>
 __device__ __forceinline__ void dom_write(const RasterArgs& a, int32_t px, int32_t py, int32_t width, int32_t height,
-                                          f3 world) {
+                                          float2 A, float2 seg, float seg_len2, f3 p0, f3 p1) {
     const hg_hair_params& p = a.p;
     if (px < 0 || py < 0 || px >= width || py >= height) return;
+    const uint32_t dom_w = f2u(p.dom_info[0]);
+    const uint32_t pix = (uint32_t)py * dom_w + (uint32_t)px;
+    const uint32_t cur = __ldcg(&a.dom[pix]);
+    if (MODE == 2 && cur == kDomEmpty) return;
+    const float2 ctr = make_float2(__int2float_rn(px) + 0.5f, __int2float_rn(py) + 0.5f);
+    const float t = clampf(__fdiv_rn(dot2(sub2(ctr, A), seg), seg_len2), 0.0f, 1.0f);
+    const f3 world = mix3(p0, p1, t);
     const float near_ = p.screen[2], far_ = p.screen[3];
-    float dist = dot3(sub3(world, mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2])),
-                      mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]));
+    const float dist = dot3(sub3(world, mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2])),
+                            mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]));
     if (dist <= near_ || dist >= far_) return;
-    uint32_t dom_w = f2u(p.dom_info[0]);
-    uint32_t pix = (uint32_t)py * dom_w + (uint32_t)px;
-    uint32_t q = quantize_depth(dist, near_, far_);
     if (MODE == 1) {
-        atomicMin(&a.dom[pix], q);
+        const uint32_t q = quantize_depth(dist, near_, far_);
+        if (q < cur) atomicMin(&a.dom[pix], q);
         return;
     }
-    uint32_t front_q = __ldcg(&a.dom[pix]);
-    if (front_q == kDomEmpty) return;
-    float z_front = dequantize_depth(front_q, near_, far_);
-    float thickness = __fdiv_rn(fmaxf(far_ - near_, 1e-3f), (float)kDomLayers);
-    float tt = __fdiv_rn(fmaxf(dist - z_front, 0.0f), thickness);
-    uint32_t slice = min(f2u(tt), kDomLayers - 1u);
-    uint32_t pixels = dom_w * f2u(p.dom_info[1]);
+    const float z_front = dequantize_depth(cur, near_, far_);
+    const float thickness = __fdiv_rn(fmaxf(far_ - near_, 1e-3f), (float)kDomLayers);
+    const float tt = __fdiv_rn(fmaxf(dist - z_front, 0.0f), thickness);
+    const uint32_t slice = min(f2u(tt), kDomLayers - 1u);
+    const uint32_t pixels = dom_w * f2u(p.dom_info[1]);
     atomicAdd(&a.dom[pixels + pix * kDomLayers + slice], 1u);
 }
 
@@ -570,11 +585,7 @@ __device__ __forceinline__ void raster_dom(const RasterArgs& a, StrandSmem& sm, 
         f3 p0 = xyz(c0), p1 = xyz(c1);
         const int32_t ndy = (int32_t)(0u - (uint32_t)dy);
         for (int step = 0; step < 1024; ++step) {
-            if (!skip) {
-                float2 ctr = make_float2(__int2float_rn(x0) + 0.5f, __int2float_rn(y0) + 0.5f);
-                float t = clampf(__fdiv_rn(dot2(sub2(ctr, A), seg), seg_len2), 0.0f, 1.0f);
-                dom_write<MODE>(a, x0, y0, width, height, mix3(p0, p1, t));
-            }
+            if (!skip) dom_write<MODE>(a, x0, y0, width, height, A, seg, seg_len2, p0, p1);
             skip = false;
             if (x0 == x1 && y0 == y1) break;
             int32_t e2 = iadd(err, err);
