@@ -204,9 +204,9 @@ __global__ void scan_expand_kernel(const hg_lod_record* __restrict__ lod, const 
 
 constexpr int kRasterWarps = 4;
 constexpr int kRasterThreads = kRasterWarps * 32;
-constexpr int kRasterMinBlocks = 7;  // 28 warps per SM: registers <= 73, shared memory 7 x 26.8 KB
+constexpr int kRasterMinBlocks = 7;  // 28 warps per SM: registers <= 73, shared memory 7 x 27.7 KB
 
-// Per-warp shared memory, 6.7 KB.  The layer samples are needed only while
+// Per-warp shared memory, 6.9 KB.  The layer samples are needed only while
 // control points are generated, so they share storage with the sample offsets.
 struct alignas(16) StrandSmem {
     float4 cp[128];  // control point: model position, then world position + in_front flag
@@ -219,6 +219,7 @@ struct alignas(16) StrandSmem {
         } gen;
         int32_t off[132];  // camera: exclusive sample offset per segment
     } u;
+    int32_t q[64];  // camera: queued sample indices (at most 63 between flushes)
 };
 
 struct RasterArgs {
@@ -389,8 +390,163 @@ __device__ __forceinline__ uint32_t generate_strand(const RasterArgs& a, StrandS
     return ncp;
 }
 
+// The largest x with sqrt_rn(x) <= r, so that sqrt_rn(d) <= r  <=>  d <= x for
+// every d >= 0 (sqrt_rn is monotone).  Found from r*r by stepping one ulp at a
+// time; a handful of steps at most, bounded here by 8 each way.
+__device__ __forceinline__ float sqrt_bound(float r) {
+    float x = r * r;
+    for (int k = 0; k < 8 && __fsqrt_rn(x) > r; ++k) x = nextafterf(x, 0.0f);
+    for (int k = 0; k < 8; ++k) {
+        const float up = nextafterf(x, __int_as_float(0x7f800000));
+        if (!(__fsqrt_rn(up) <= r)) break;
+        x = up;
+    }
+    return x;
+}
+
 __device__ __forceinline__ bool on_screen(int32_t x, int32_t y, int32_t w, int32_t h) {
     return x >= 0 && y >= 0 && x < w && y < h;
+}
+
+struct CamConst {
+    int32_t width, height;
+    float r2_max;      // centre-disk threshold on |o|^2
+    f3 cam, fwd;
+    float2 uv;
+    uint32_t beta_q;
+    bool ao_on;
+};
+
+__device__ __forceinline__ CamConst cam_const(const hg_hair_params& p, float2 uv, float beta) {
+    CamConst k;
+    k.width = f2i(p.screen[0]);
+    k.height = f2i(p.screen[1]);
+    k.r2_max = sqrt_bound(fmaxf(p.appearance[3], 0.05f) * 0.5f);
+    k.cam = mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2]);
+    k.fwd = mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]);
+    k.uv = uv;
+    k.beta_q = f2u(clampf(beta, 0.0f, 1.0f) * 255.0f + 0.5f);
+    k.ao_on = p.flags[2] != 0u;
+    return k;
+}
+
+// Segment j with off[j] <= s < off[j+1].
+__device__ __forceinline__ int32_t find_segment(const StrandSmem& sm, int32_t nseg, int32_t s) {
+    int32_t lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int32_t mid = (lo + hi + 1) >> 1;
+        if (sm.u.off[mid] <= s) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// The cheap half of write_pixel (raster.wgsl:77-116) for DDA step i of segment
+// j: true when the sample's depth can still lower one of the words of its centre
+// pixel or diagonal side pixels.  Words are read from L2; buffers only decrease
+// during the pass, so a stale read only makes the test conservative.
+__device__ __forceinline__ bool sample_can_write(const RasterArgs& a, const CamConst& k, const StrandSmem& sm,
+                                                 int32_t j, int32_t i, float t, int32_t px, int32_t py, int32_t qx,
+                                                 int32_t qy) {
+    const bool side = i > 0 && qx != px && qy != py;
+    const bool on0 = on_screen(px, py, k.width, k.height);
+    const bool on1 = side && on_screen(qx, py, k.width, k.height);
+    const bool on2 = side && on_screen(px, qy, k.width, k.height);
+    if (!(on0 || on1 || on2)) return false;
+    const uint32_t w = (uint32_t)k.width;
+    const unsigned long long c0 = on0 ? __ldcg(&a.cons[(uint32_t)py * w + (uint32_t)px]) : 0ull;
+    const unsigned long long m0 = on0 ? __ldcg(&a.center[(uint32_t)py * w + (uint32_t)px]) : 0ull;
+    const unsigned long long c1 = on1 ? __ldcg(&a.cons[(uint32_t)py * w + (uint32_t)qx]) : 0ull;
+    const unsigned long long c2 = on2 ? __ldcg(&a.cons[(uint32_t)qy * w + (uint32_t)px]) : 0ull;
+    const float4 p0 = sm.cp[j], p1 = sm.cp[j + 1];
+    const float dist = dot3(sub3(mix3(xyz(p0), xyz(p1), t), k.cam), k.fwd);
+    if (dist <= a.p.screen[2]) return false;
+    const uint32_t depth = quantize_depth(dist, a.p.screen[2], a.p.screen[3]);
+    const unsigned long long lower = (unsigned long long)depth << 40;  // smallest payload with this depth
+    return (on0 && (lower < c0 || depth <= (uint32_t)(m0 >> 40))) || (on1 && lower < c1) || (on2 && lower < c2);
+}
+
+// The full write_pixel (raster.wgsl:77-116) for queued sample s: payload once,
+// then the centre pixel's conservative/centre/beta words and the diagonal side
+// pixels' conservative words.  An atomicMin whose value cannot lower the word
+// read just before is skipped; the final buffers are unchanged by that.
+__device__ __forceinline__ void sample_write(const RasterArgs& a, const CamConst& k, const StrandSmem& sm,
+                                             int32_t nseg, int32_t s) {
+    const hg_hair_params& p = a.p;
+    const int32_t j = find_segment(sm, nseg, s);
+    const int32_t i = s - sm.u.off[j];
+    const float4 A = sm.cs[j], B = sm.cs[j + 1];
+    const float fn = __int2float_rn(__float_as_int(A.w));
+    const float t = __fdiv_rn(__int2float_rn(i), fn);
+    const int32_t px = f2i(floorf(mixf(A.x, B.x, t))), py = f2i(floorf(mixf(A.y, B.y, t)));
+    bool side = false;
+    int32_t qx = px, qy = py;
+    if (i > 0) {
+        // the DDA's previous step, floor(mix(a, b, (i-1)/n)) (raster.wgsl:214-219)
+        const float tp = __fdiv_rn(__int2float_rn(i - 1), fn);
+        qx = f2i(floorf(mixf(A.x, B.x, tp)));
+        qy = f2i(floorf(mixf(A.y, B.y, tp)));
+        side = qx != px && qy != py;
+    }
+    const bool on0 = on_screen(px, py, k.width, k.height);
+    const bool on1 = side && on_screen(qx, py, k.width, k.height);
+    const bool on2 = side && on_screen(px, qy, k.width, k.height);
+    const uint32_t w = (uint32_t)k.width;
+    const uint32_t pix0 = (uint32_t)py * w + (uint32_t)px;
+    const uint32_t pix1 = (uint32_t)py * w + (uint32_t)qx;
+    const uint32_t pix2 = (uint32_t)qy * w + (uint32_t)px;
+    const unsigned long long c0 = on0 ? __ldcg(&a.cons[pix0]) : 0ull;
+    const unsigned long long m0 = on0 ? __ldcg(&a.center[pix0]) : 0ull;
+    const unsigned long long c1 = on1 ? __ldcg(&a.cons[pix1]) : 0ull;
+    const unsigned long long c2 = on2 ? __ldcg(&a.cons[pix2]) : 0ull;
+
+    const float4 p0 = sm.cp[j], p1 = sm.cp[j + 1];
+    const f3 world = mix3(xyz(p0), xyz(p1), t);
+    const float dist = dot3(sub3(world, k.cam), k.fwd);
+    if (dist <= p.screen[2]) return;
+    const uint32_t depth = quantize_depth(dist, p.screen[2], p.screen[3]);
+    const unsigned long long lower = (unsigned long long)depth << 40;
+    bool w0 = on0 && lower < c0;
+    bool wm = on0 && depth <= (uint32_t)(m0 >> 40);
+    bool w1 = on1 && lower < c1;
+    bool w2 = on2 && lower < c2;
+    if (wm) {
+        // centre-disk test (raster.wgsl:206-212): length(o) <= d/2 is
+        // sqrt_rn(|o|^2) <= d/2, i.e. |o|^2 <= r2_max
+        const float cx = __int2float_rn(px) + 0.5f, cy = __int2float_rn(py) + 0.5f;
+        const float gx = B.x - A.x, gy = B.y - A.y;
+        const float denom = fmaxf(gx * gx + gy * gy, 1e-6f);
+        const float closest = clampf(__fdiv_rn((cx - A.x) * gx + (cy - A.y) * gy, denom), 0.0f, 1.0f);
+        const float ox = cx - (A.x + gx * closest), oy = cy - (A.y + gy * closest);
+        wm = ox * ox + oy * oy <= k.r2_max;
+    }
+    if (!(w0 || wm || w1 || w2)) return;
+    if (a.scene) {
+        const float4 clip = mat_mul(p.clip_from_world, world.x, world.y, world.z, 1.0f);
+        const float clip_depth = __fdiv_rn(clip.z, fmaxf(clip.w, 1e-5f));
+        const bool rev = p.pass_mode[2] == 1u;
+        auto hidden = [&](uint32_t pix) {
+            const float scene = __ldg(&a.scene[pix]);
+            return rev ? clip_depth < scene : clip_depth > scene;
+        };
+        if ((w0 || wm) && hidden(pix0)) w0 = wm = false;
+        if (w1 && hidden(pix1)) w1 = false;
+        if (w2 && hidden(pix2)) w2 = false;
+        if (!(w0 || wm || w1 || w2)) return;
+    }
+    const float4 t0 = sm.ct[j], t1 = sm.ct[j + 1];
+    const f3 tangent = safe_normalize(mix3(xyz(t0), xyz(t1), t));
+    const uint32_t oct = oct_encode(tangent);
+    const uint32_t ao_q = k.ao_on ? f2u(clampf(mixf(A.z, B.z, t), 0.0f, 1.0f) * 63.0f + 0.5f) : 63u;
+    const unsigned long long payload =
+        pack_gb(depth, oct & 0xffu, oct >> 8u, quant63(mixf(k.uv.x, k.uv.x, t)), quant63(mixf(k.uv.y, k.uv.y, t)),
+                quant63(mixf(t0.w, t1.w, t)), ao_q);
+    if (w0 && payload < c0) atomicMin(&a.cons[pix0], payload);
+    if (wm) {
+        if (payload < m0) atomicMin(&a.center[pix0], payload);
+        atomicMin(&a.beta[pix0], (depth << 8u) | k.beta_q);
+    }
+    if (w1 && payload < c1) atomicMin(&a.cons[pix1], payload);
+    if (w2 && payload < c2) atomicMin(&a.cons[pix2], payload);
 }
 
 // Camera raster of one generated strand.  The DDA of every segment
@@ -435,29 +591,20 @@ __device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& s
     __syncwarp();
 
     const int32_t total = carry;
-    const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
-    const float half_diameter = fmaxf(p.appearance[3], 0.05f) * 0.5f;
-    const f3 cam = mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2]);
-    const f3 fwd = mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]);
-    const uint32_t beta_q = f2u(clampf(beta, 0.0f, 1.0f) * 255.0f + 0.5f);
-    const bool ao_on = p.flags[2] != 0u;
+    const CamConst k = cam_const(p, uv, beta);
+    // Pass 1: every sample computes its pixel(s) and depth and is queued only
+    // when some word can still take it.  Pass 2 runs the full payload 32 wide
+    // over the queue, so the expensive part of write_pixel never idles lanes.
+    int32_t qn = 0;
     int32_t carry_px = 0, carry_py = 0;
     for (int32_t base = 0; base < total; base += 32) {
         const int32_t s = min(base + (int32_t)lane, total - 1);
         const bool active = base + (int32_t)lane < total;
-        // segment j with off[j] <= s < off[j+1]
-        int32_t lo = 0, hi = nseg - 1;
-        while (lo < hi) {
-            int32_t mid = (lo + hi + 1) >> 1;
-            if (sm.u.off[mid] <= s) lo = mid; else hi = mid - 1;
-        }
-        const int32_t j = lo;
+        const int32_t j = find_segment(sm, nseg, s);
         const int32_t i = s - sm.u.off[j];
         const float4 A = sm.cs[j], B = sm.cs[j + 1];
-        const int32_t n = __float_as_int(A.w);
-        const float t = __fdiv_rn(__int2float_rn(i), __int2float_rn(n));
-        const float sx = mixf(A.x, B.x, t), sy = mixf(A.y, B.y, t);
-        const int32_t px = f2i(floorf(sx)), py = f2i(floorf(sy));
+        const float t = __fdiv_rn(__int2float_rn(i), __int2float_rn(__float_as_int(A.w)));
+        const int32_t px = f2i(floorf(mixf(A.x, B.x, t))), py = f2i(floorf(mixf(A.y, B.y, t)));
         int32_t qx = __shfl_up_sync(0xffffffffu, px, 1), qy = __shfl_up_sync(0xffffffffu, py, 1);
         if (lane == 0) {
             qx = carry_px;
@@ -465,76 +612,25 @@ __device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& s
         }
         carry_px = __shfl_sync(0xffffffffu, px, 31);
         carry_py = __shfl_sync(0xffffffffu, py, 31);
-        if (!active) continue;
-        const bool side = i > 0 && qx != px && qy != py;
-        const bool on0 = on_screen(px, py, width, height);
-        const bool on1 = side && on_screen(qx, py, width, height);
-        const bool on2 = side && on_screen(px, qy, width, height);
-        if (!(on0 || on1 || on2)) continue;
-        const uint32_t pix0 = (uint32_t)py * (uint32_t)width + (uint32_t)px;
-        const uint32_t pix1 = (uint32_t)py * (uint32_t)width + (uint32_t)qx;
-        const uint32_t pix2 = (uint32_t)qy * (uint32_t)width + (uint32_t)px;
-        // Current words, read from L2 before the payload is known.  Buffers only
-        // decrease during the pass, so a stale read is an upper bound: an atomicMin
-        // is skipped only when it cannot change the word.
-        const unsigned long long cur_c0 = on0 ? __ldcg(&a.cons[pix0]) : 0ull;
-        const unsigned long long cur_m0 = on0 ? __ldcg(&a.center[pix0]) : 0ull;
-        const unsigned long long cur_c1 = on1 ? __ldcg(&a.cons[pix1]) : 0ull;
-        const unsigned long long cur_c2 = on2 ? __ldcg(&a.cons[pix2]) : 0ull;
-
-        const float cx = __int2float_rn(px) + 0.5f, cy = __int2float_rn(py) + 0.5f;
-        const float gx = B.x - A.x, gy = B.y - A.y;
-        const float denom = fmaxf(gx * gx + gy * gy, 1e-6f);
-        const float closest = clampf(__fdiv_rn((cx - A.x) * gx + (cy - A.y) * gy, denom), 0.0f, 1.0f);
-        const float ox = cx - (A.x + gx * closest), oy = cy - (A.y + gy * closest);
-        const bool center_hit = __fsqrt_rn(ox * ox + oy * oy) <= half_diameter;
-
-        // write_pixel (raster.wgsl:83-115): depth first; the rest of the payload
-        // only when some word can still take it.
-        const float4 c0 = sm.cp[j], c1 = sm.cp[j + 1];
-        const f3 world = mix3(xyz(c0), xyz(c1), t);
-        const float dist = dot3(sub3(world, cam), fwd);
-        if (dist <= p.screen[2]) continue;
-        const uint32_t depth = quantize_depth(dist, p.screen[2], p.screen[3]);
-        const unsigned long long lower = (unsigned long long)depth << 40;  // smallest payload with this depth
-        bool w0 = on0 && lower < cur_c0;
-        bool wm = on0 && center_hit && depth <= (uint32_t)(cur_m0 >> 40);
-        bool w1 = on1 && lower < cur_c1;
-        bool w2 = on2 && lower < cur_c2;
-        if (!(w0 || wm || w1 || w2)) continue;
-        if (a.scene) {
-            const float4 clip = mat_mul(p.clip_from_world, world.x, world.y, world.z, 1.0f);
-            const float clip_depth = __fdiv_rn(clip.z, fmaxf(clip.w, 1e-5f));
-            const bool rev = p.pass_mode[2] == 1u;
-            auto hidden = [&](uint32_t pix) {
-                const float scene = __ldg(&a.scene[pix]);
-                return rev ? clip_depth < scene : clip_depth > scene;
-            };
-            if ((w0 || wm) && hidden(pix0)) w0 = wm = false;
-            if (w1 && hidden(pix1)) w1 = false;
-            if (w2 && hidden(pix2)) w2 = false;
-            if (!(w0 || wm || w1 || w2)) continue;
+        const bool survive = active && sample_can_write(a, k, sm, j, i, t, px, py, qx, qy);
+        const unsigned m = __ballot_sync(0xffffffffu, survive);
+        if (survive) sm.q[qn + __popc(m & ((1u << lane) - 1u))] = s;
+        qn += __popc(m);
+        if (qn >= 32) {
+            __syncwarp();
+            sample_write(a, k, sm, nseg, sm.q[lane]);
+            __syncwarp();
+            if ((int32_t)lane < qn - 32) sm.q[lane] = sm.q[lane + 32];
+            qn -= 32;
+            __syncwarp();
         }
-        const float4 t0 = sm.ct[j], t1 = sm.ct[j + 1];
-        const f3 tangent = safe_normalize(mix3(xyz(t0), xyz(t1), t));
-        const uint32_t oct = oct_encode(tangent);
-        const uint32_t ao_q = ao_on ? f2u(clampf(mixf(A.z, B.z, t), 0.0f, 1.0f) * 63.0f + 0.5f) : 63u;
-        const unsigned long long payload = pack_gb(depth, oct & 0xffu, oct >> 8u, quant63(mixf(uv.x, uv.x, t)),
-                                                   quant63(mixf(uv.y, uv.y, t)), quant63(mixf(t0.w, t1.w, t)), ao_q);
-        if (w0 && payload < cur_c0) atomicMin(&a.cons[pix0], payload);
-        if (wm) {
-            if (payload < cur_m0) atomicMin(&a.center[pix0], payload);
-            atomicMin(&a.beta[pix0], (depth << 8u) | beta_q);
-        }
-        if (w1 && payload < cur_c1) atomicMin(&a.cons[pix1], payload);
-        if (w2 && payload < cur_c2) atomicMin(&a.cons[pix2], payload);
     }
+    __syncwarp();
+    if ((int32_t)lane < qn) sample_write(a, k, sm, nseg, sm.q[lane]);
 }
 
 // write_dom_pixel (raster.wgsl:118-148) for the Bresenham pixel (px, py) of
-// the segment p0-p1 (screen a -> a + seg).  The texel's front depth is read
-// before the sample position is computed; mode 1 skips an atomicMin that
-// cannot lower it (the map only decreases during the pass).
+// the segment p0-p1 (screen a -> a + seg).
 template <int MODE>
 __device__ __forceinline__ void dom_write(const RasterArgs& a, int32_t px, int32_t py, int32_t width, int32_t height,
                                           float2 A, float2 seg, float seg_len2, f3 p0, f3 p1) {
@@ -542,7 +638,10 @@ __device__ __forceinline__ void dom_write(const RasterArgs& a, int32_t px, int32
     if (px < 0 || py < 0 || px >= width || py >= height) return;
     const uint32_t dom_w = f2u(p.dom_info[0]);
     const uint32_t pix = (uint32_t)py * dom_w + (uint32_t)px;
-    const uint32_t cur = __ldcg(&a.dom[pix]);
+    // Mode 2 needs the texel's front depth (final after mode 1); mode 1's
+    // atomicMin is fire-and-forget, which beats reading the word first in this
+    // sequential per-lane loop.
+    const uint32_t cur = MODE == 2 ? __ldcg(&a.dom[pix]) : 0u;
     if (MODE == 2 && cur == kDomEmpty) return;
     const float2 ctr = make_float2(__int2float_rn(px) + 0.5f, __int2float_rn(py) + 0.5f);
     const float t = clampf(__fdiv_rn(dot2(sub2(ctr, A), seg), seg_len2), 0.0f, 1.0f);
@@ -552,8 +651,7 @@ __device__ __forceinline__ void dom_write(const RasterArgs& a, int32_t px, int32
                             mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]));
     if (dist <= near_ || dist >= far_) return;
     if (MODE == 1) {
-        const uint32_t q = quantize_depth(dist, near_, far_);
-        if (q < cur) atomicMin(&a.dom[pix], q);
+        atomicMin(&a.dom[pix], quantize_depth(dist, near_, far_));
         return;
     }
     const float z_front = dequantize_depth(cur, near_, far_);

@@ -129,6 +129,18 @@ def test_visibility_and_dom_bit_exact(renderer, name):
     _check_visibility(got, want)
 
 
+@pytest.mark.parametrize("diameter", [0.01, 0.3, 0.7, 1.0, 1.41421356, 2.5])
+def test_center_disk_diameters(renderer, diameter):
+    """The centre-sample acceptance disk (raster.wgsl:201,212) at several
+    diameters, including the 0.05 floor and one whose radius squares inexactly."""
+    sc = configs.config1(scale=0.03)
+    sc.groom.center_diameter = diameter
+    cam, dom = sc.params()
+    got = _visibility(renderer, sc, cam, None)
+    want = _oracle_visibility(sc, cam, None)
+    _check_visibility(got, want, with_dom=False)
+
+
 def test_clear_sentinels(renderer):
     renderer.ensure_targets(37, 19, 7, 5)
     renderer.clear()
