@@ -282,6 +282,11 @@ hg_status hg_groom_upload(hg_ctx* ctx, const hg_gpu_bundle* bundles, uint32_t bu
         alloc(g->refs[s], (size_t)g->ref_capacity * sizeof(hg_strand_ref));
         alloc(g->indirect[s], 16);
         alloc(g->offsets[s], ((size_t)bundle_count + 1) * 4);
+        alloc(g->depth_key[s], (size_t)std::max<uint32_t>(bundle_count, 1u) * 4);
+        alloc(g->sorted[s], (size_t)std::max<uint32_t>(bundle_count, 1u) * 4);
+        alloc(g->sorted_off[s], ((size_t)bundle_count + 1) * 4);
+        alloc(g->draw_order[s], (size_t)g->ref_capacity * 4);
+        alloc(g->order_meta[s], 8);
     }
     if (e == cudaSuccess && bundle_count) {
         e = cudaMemcpyAsync(g->bundles, bundles, (size_t)bundle_count * sizeof(hg_gpu_bundle), cudaMemcpyHostToDevice,
@@ -295,6 +300,7 @@ hg_status hg_groom_upload(hg_ctx* ctx, const hg_gpu_bundle* bundles, uint32_t bu
     for (int s = 0; s < 2 && e == cudaSuccess; ++s) {
         e = cudaMemsetAsync(g->indirect[s], 0, 16, ctx->stream);
         if (e == cudaSuccess) e = cudaMemsetAsync(g->lod[s], 0, (size_t)std::max<uint32_t>(bundle_count, 1u) * 16, ctx->stream);
+        if (e == cudaSuccess) e = cudaMemsetAsync(g->order_meta[s], 0, 8, ctx->stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) {
@@ -317,6 +323,11 @@ hg_status hg_groom_destroy(hg_ctx* ctx, hg_groom* g) {
         free_dev(g->refs[s]);
         free_dev(g->indirect[s]);
         free_dev(g->offsets[s]);
+        free_dev(g->depth_key[s]);
+        free_dev(g->sorted[s]);
+        free_dev(g->sorted_off[s]);
+        free_dev(g->draw_order[s]);
+        free_dev(g->order_meta[s]);
     }
     delete g;
     return HG_OK;

@@ -23,6 +23,12 @@ struct hg_groom {
     hg_strand_ref* refs[2] = {nullptr, nullptr};
     uint32_t* indirect[2] = {nullptr, nullptr};  // (total, 1, 1, 0)
     uint32_t* offsets[2] = {nullptr, nullptr};   // exclusive scan of n_lod, bundle_count + 1
+    // Front-to-back draw order of the camera pass (scheduling only).
+    uint32_t* depth_key[2] = {nullptr, nullptr};   // per bundle: nearest-depth bucket
+    uint32_t* sorted[2] = {nullptr, nullptr};      // live bundles in depth order
+    uint32_t* sorted_off[2] = {nullptr, nullptr};  // scan of n_lod in that order, bundle_count + 1
+    uint32_t* draw_order[2] = {nullptr, nullptr};  // permutation of refs, ref_capacity
+    uint32_t* order_meta[2] = {nullptr, nullptr};  // (live bundles, order valid)
 };
 
 struct hg_ctx {

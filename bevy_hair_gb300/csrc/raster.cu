@@ -75,14 +75,19 @@ __device__ __forceinline__ uint32_t control_points_for_lod(float l) {
     return snapped < 127u ? snapped : 127u;
 }
 
+constexpr uint32_t kDepthBuckets = 1024;
+
 // lod.wgsl:6-59, one warp per bundle (two of the 64 cage corners per lane).
+// Also writes the bundle's nearest view distance as one of kDepthBuckets
+// buckets between near and far, for the front-to-back draw order.
 __global__ void lod_kernel(const hg_hair_params p, const hg_gpu_bundle* __restrict__ bundles,
-                           const float4* __restrict__ layers, hg_lod_record* __restrict__ out, uint32_t count) {
+                           const float4* __restrict__ layers, hg_lod_record* __restrict__ out,
+                           uint32_t* __restrict__ depth_key, uint32_t count) {
     uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     uint32_t lane = threadIdx.x & 31u;
     if (b >= count) return;
     hg_gpu_bundle bundle = bundles[b];
-    float mnx = 1e20f, mny = 1e20f, mxx = -1e20f, mxy = -1e20f;
+    float mnx = 1e20f, mny = 1e20f, mxx = -1e20f, mxy = -1e20f, mnd = 3.0e38f;
     bool front = false;
     for (uint32_t c = lane; c < 64u; c += 32u) {
         float4 pa = __ldg(&layers[2u * (bundle.layer_offset + c)]);
@@ -91,6 +96,7 @@ __global__ void lod_kernel(const hg_hair_params p, const hg_gpu_bundle* __restri
         float dist = dot3(sub3(world, mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2])),
                           mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]));
         if (clip.w > 0.0f && dist > 0.0f) front = true;
+        mnd = fminf(mnd, dist);
         Projected pr = project_world(p, world);
         mnx = fminf(mnx, pr.screen.x);
         mny = fminf(mny, pr.screen.y);
@@ -103,9 +109,12 @@ __global__ void lod_kernel(const hg_hair_params p, const hg_gpu_bundle* __restri
         mny = fminf(mny, __shfl_xor_sync(0xffffffffu, mny, o));
         mxx = fmaxf(mxx, __shfl_xor_sync(0xffffffffu, mxx, o));
         mxy = fmaxf(mxy, __shfl_xor_sync(0xffffffffu, mxy, o));
+        mnd = fminf(mnd, __shfl_xor_sync(0xffffffffu, mnd, o));
     }
     bool any_front = __any_sync(0xffffffffu, front);
     if (lane != 0) return;
+    const float rel = (mnd - p.screen[2]) / fmaxf(p.screen[3] - p.screen[2], 1e-3f);
+    depth_key[b] = min(f2u(clampf(rel, 0.0f, 1.0f) * (float)kDepthBuckets), kDepthBuckets - 1u);
     bool culled = !any_front || mxx < 0.0f || mxy < 0.0f || mnx > p.screen[0] || mny > p.screen[1];
     uint32_t n_lod = 0u, cps = kLayerCount;
     if (!culled) {
@@ -136,12 +145,47 @@ __global__ void lod_kernel(const hg_hair_params p, const hg_gpu_bundle* __restri
 // clamped to the refs capacity.
 constexpr int kScanThreads = 1024;
 
+// Block-wide exclusive scan of one value per thread; returns the thread's
+// exclusive prefix and, through *total, the block's sum.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += y;
+    }
+    if (lane == 31) warp_sums[warp] = incl;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = warp_sums[lane];
+        uint32_t wi = w;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, wi, o);
+            if (lane >= (uint32_t)o) wi += y;
+        }
+        warp_sums[lane] = wi - w;
+        if (lane == 31) warp_sums[32] = wi;
+    }
+    __syncthreads();
+    const uint32_t r = warp_sums[warp] + incl - v;
+    *total = warp_sums[32];
+    __syncthreads();
+    return r;
+}
+
 __global__ void __launch_bounds__(kScanThreads) scan_offsets_kernel(const hg_lod_record* __restrict__ lod,
                                                                     uint32_t count, uint32_t capacity,
                                                                     uint32_t* __restrict__ offsets,
-                                                                    uint32_t* __restrict__ indirect) {
-    __shared__ uint32_t warp_sums[32];
+                                                                    uint32_t* __restrict__ indirect,
+                                                                    const uint32_t* __restrict__ depth_key,
+                                                                    uint32_t* __restrict__ sorted,
+                                                                    uint32_t* __restrict__ sorted_off,
+                                                                    uint32_t* __restrict__ order_meta) {
+    __shared__ uint32_t warp_sums[33];
     __shared__ uint32_t carry;
+    __shared__ uint32_t bucket[kDepthBuckets];
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -181,6 +225,39 @@ __global__ void __launch_bounds__(kScanThreads) scan_offsets_kernel(const hg_lod
         indirect[2] = 1u;
         indirect[3] = 0u;
     }
+    if (!sorted) return;
+    // Draw order: live bundles (n_lod > 0) counting-sorted by depth bucket,
+    // then their n_lod scanned in that order.  The raster visits strands in
+    // this order (near bundles first) so most later samples fail the depth
+    // test before any payload work; results do not depend on the order.
+    const uint32_t full = carry;
+    for (uint32_t k = threadIdx.x; k < kDepthBuckets; k += kScanThreads) bucket[k] = 0u;
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < count; b += kScanThreads)
+        if (lod[b].n_lod) atomicAdd(&bucket[depth_key[b]], 1u);
+    __syncthreads();
+    uint32_t live = 0;
+    const uint32_t start = block_exclusive_scan(threadIdx.x < kDepthBuckets ? bucket[threadIdx.x] : 0u, warp_sums,
+                                                &live);
+    if (threadIdx.x < kDepthBuckets) bucket[threadIdx.x] = start;
+    __syncthreads();
+    for (uint32_t b = threadIdx.x; b < count; b += kScanThreads)
+        if (lod[b].n_lod) sorted[atomicAdd(&bucket[depth_key[b]], 1u)] = b;
+    __syncthreads();
+    uint32_t run = 0;
+    for (uint32_t base = 0; base < live; base += kScanThreads) {
+        const uint32_t k = base + threadIdx.x;
+        const uint32_t v = k < live ? lod[sorted[k]].n_lod : 0u;
+        uint32_t sum = 0;
+        const uint32_t ex = block_exclusive_scan(v, warp_sums, &sum);
+        if (k < live) sorted_off[k] = run + ex;
+        run += sum;
+    }
+    if (threadIdx.x == 0) {
+        sorted_off[live] = run;
+        order_meta[0] = live;
+        order_meta[1] = full <= capacity ? 1u : 0u;  // every ref exists, so the order is a permutation
+    }
 }
 
 // Step 2: one warp per bundle writes its StrandRefs (bundle-major order, as
@@ -200,13 +277,37 @@ __global__ void scan_expand_kernel(const hg_lod_record* __restrict__ lod, const 
     }
 }
 
+// Step 2 with a draw order: one warp per live bundle in depth order writes
+// its StrandRefs at their reference positions and the matching draw-order
+// entries (indices into refs).
+__global__ void scan_expand_sorted_kernel(const hg_lod_record* __restrict__ lod, const uint32_t* __restrict__ offsets,
+                                          const uint32_t* __restrict__ sorted, const uint32_t* __restrict__ sorted_off,
+                                          const uint32_t* __restrict__ order_meta, uint32_t capacity,
+                                          hg_strand_ref* __restrict__ refs, uint32_t* __restrict__ draw_order) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t live = order_meta[0];
+    const bool valid = order_meta[1] != 0u;
+    for (uint32_t k = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; k < live; k += warps) {
+        const uint32_t b = sorted[k];
+        const hg_lod_record rec = lod[b];
+        const uint32_t off = offsets[b], dpos = sorted_off[k];
+        for (uint32_t s = lane; s < rec.n_lod; s += 32u) {
+            const uint32_t i = off + s;
+            if (i >= capacity) break;
+            reinterpret_cast<uint4*>(refs)[i] = make_uint4(b, s, rec.n_lod, rec.control_points);
+            if (valid) draw_order[dpos + s] = i;
+        }
+    }
+}
+
 // ------------------------------------------------------------------ raster
 
 constexpr int kRasterWarps = 4;
 constexpr int kRasterThreads = kRasterWarps * 32;
-constexpr int kRasterMinBlocks = 7;  // 28 warps per SM: registers <= 73, shared memory 7 x 27.7 KB
+constexpr int kRasterMinBlocks = 7;  // 28 warps per SM: registers <= 73, shared memory 7 x 26.8 KB
 
-// Per-warp shared memory, 6.9 KB.  The layer samples are needed only while
+// Per-warp shared memory, 6.7 KB.  The layer samples are needed only while
 // control points are generated, so they share storage with the sample offsets.
 struct alignas(16) StrandSmem {
     float4 cp[128];  // control point: model position, then world position + in_front flag
@@ -219,7 +320,6 @@ struct alignas(16) StrandSmem {
         } gen;
         int32_t off[132];  // camera: exclusive sample offset per segment
     } u;
-    int32_t q[64];  // camera: queued sample indices (at most 63 between flushes)
 };
 
 struct RasterArgs {
@@ -229,6 +329,8 @@ struct RasterArgs {
     const float4* style;
     const hg_strand_ref* refs;
     const uint32_t* indirect;
+    const uint32_t* draw_order;  // permutation of refs to visit, or nullptr
+    const uint32_t* order_meta;  // (live bundles, order valid)
     unsigned long long* center;
     unsigned long long* cons;
     uint32_t* beta;
@@ -408,147 +510,6 @@ __device__ __forceinline__ bool on_screen(int32_t x, int32_t y, int32_t w, int32
     return x >= 0 && y >= 0 && x < w && y < h;
 }
 
-struct CamConst {
-    int32_t width, height;
-    float r2_max;      // centre-disk threshold on |o|^2
-    f3 cam, fwd;
-    float2 uv;
-    uint32_t beta_q;
-    bool ao_on;
-};
-
-__device__ __forceinline__ CamConst cam_const(const hg_hair_params& p, float2 uv, float beta) {
-    CamConst k;
-    k.width = f2i(p.screen[0]);
-    k.height = f2i(p.screen[1]);
-    k.r2_max = sqrt_bound(fmaxf(p.appearance[3], 0.05f) * 0.5f);
-    k.cam = mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2]);
-    k.fwd = mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]);
-    k.uv = uv;
-    k.beta_q = f2u(clampf(beta, 0.0f, 1.0f) * 255.0f + 0.5f);
-    k.ao_on = p.flags[2] != 0u;
-    return k;
-}
-
-// Segment j with off[j] <= s < off[j+1].
-__device__ __forceinline__ int32_t find_segment(const StrandSmem& sm, int32_t nseg, int32_t s) {
-    int32_t lo = 0, hi = nseg - 1;
-    while (lo < hi) {
-        const int32_t mid = (lo + hi + 1) >> 1;
-        if (sm.u.off[mid] <= s) lo = mid; else hi = mid - 1;
-    }
-    return lo;
-}
-
-// The cheap half of write_pixel (raster.wgsl:77-116) for DDA step i of segment
-// j: true when the sample's depth can still lower one of the words of its centre
-// pixel or diagonal side pixels.  Words are read from L2; buffers only decrease
-// during the pass, so a stale read only makes the test conservative.
-__device__ __forceinline__ bool sample_can_write(const RasterArgs& a, const CamConst& k, const StrandSmem& sm,
-                                                 int32_t j, int32_t i, float t, int32_t px, int32_t py, int32_t qx,
-                                                 int32_t qy) {
-    const bool side = i > 0 && qx != px && qy != py;
-    const bool on0 = on_screen(px, py, k.width, k.height);
-    const bool on1 = side && on_screen(qx, py, k.width, k.height);
-    const bool on2 = side && on_screen(px, qy, k.width, k.height);
-    if (!(on0 || on1 || on2)) return false;
-    const uint32_t w = (uint32_t)k.width;
-    const unsigned long long c0 = on0 ? __ldcg(&a.cons[(uint32_t)py * w + (uint32_t)px]) : 0ull;
-    const unsigned long long m0 = on0 ? __ldcg(&a.center[(uint32_t)py * w + (uint32_t)px]) : 0ull;
-    const unsigned long long c1 = on1 ? __ldcg(&a.cons[(uint32_t)py * w + (uint32_t)qx]) : 0ull;
-    const unsigned long long c2 = on2 ? __ldcg(&a.cons[(uint32_t)qy * w + (uint32_t)px]) : 0ull;
-    const float4 p0 = sm.cp[j], p1 = sm.cp[j + 1];
-    const float dist = dot3(sub3(mix3(xyz(p0), xyz(p1), t), k.cam), k.fwd);
-    if (dist <= a.p.screen[2]) return false;
-    const uint32_t depth = quantize_depth(dist, a.p.screen[2], a.p.screen[3]);
-    const unsigned long long lower = (unsigned long long)depth << 40;  // smallest payload with this depth
-    return (on0 && (lower < c0 || depth <= (uint32_t)(m0 >> 40))) || (on1 && lower < c1) || (on2 && lower < c2);
-}
-
-// The full write_pixel (raster.wgsl:77-116) for queued sample s: payload once,
-// then the centre pixel's conservative/centre/beta words and the diagonal side
-// pixels' conservative words.  An atomicMin whose value cannot lower the word
-// read just before is skipped; the final buffers are unchanged by that.
-__device__ __forceinline__ void sample_write(const RasterArgs& a, const CamConst& k, const StrandSmem& sm,
-                                             int32_t nseg, int32_t s) {
-    const hg_hair_params& p = a.p;
-    const int32_t j = find_segment(sm, nseg, s);
-    const int32_t i = s - sm.u.off[j];
-    const float4 A = sm.cs[j], B = sm.cs[j + 1];
-    const float fn = __int2float_rn(__float_as_int(A.w));
-    const float t = __fdiv_rn(__int2float_rn(i), fn);
-    const int32_t px = f2i(floorf(mixf(A.x, B.x, t))), py = f2i(floorf(mixf(A.y, B.y, t)));
-    bool side = false;
-    int32_t qx = px, qy = py;
-    if (i > 0) {
-        // the DDA's previous step, floor(mix(a, b, (i-1)/n)) (raster.wgsl:214-219)
-        const float tp = __fdiv_rn(__int2float_rn(i - 1), fn);
-        qx = f2i(floorf(mixf(A.x, B.x, tp)));
-        qy = f2i(floorf(mixf(A.y, B.y, tp)));
-        side = qx != px && qy != py;
-    }
-    const bool on0 = on_screen(px, py, k.width, k.height);
-    const bool on1 = side && on_screen(qx, py, k.width, k.height);
-    const bool on2 = side && on_screen(px, qy, k.width, k.height);
-    const uint32_t w = (uint32_t)k.width;
-    const uint32_t pix0 = (uint32_t)py * w + (uint32_t)px;
-    const uint32_t pix1 = (uint32_t)py * w + (uint32_t)qx;
-    const uint32_t pix2 = (uint32_t)qy * w + (uint32_t)px;
-    const unsigned long long c0 = on0 ? __ldcg(&a.cons[pix0]) : 0ull;
-    const unsigned long long m0 = on0 ? __ldcg(&a.center[pix0]) : 0ull;
-    const unsigned long long c1 = on1 ? __ldcg(&a.cons[pix1]) : 0ull;
-    const unsigned long long c2 = on2 ? __ldcg(&a.cons[pix2]) : 0ull;
-
-    const float4 p0 = sm.cp[j], p1 = sm.cp[j + 1];
-    const f3 world = mix3(xyz(p0), xyz(p1), t);
-    const float dist = dot3(sub3(world, k.cam), k.fwd);
-    if (dist <= p.screen[2]) return;
-    const uint32_t depth = quantize_depth(dist, p.screen[2], p.screen[3]);
-    const unsigned long long lower = (unsigned long long)depth << 40;
-    bool w0 = on0 && lower < c0;
-    bool wm = on0 && depth <= (uint32_t)(m0 >> 40);
-    bool w1 = on1 && lower < c1;
-    bool w2 = on2 && lower < c2;
-    if (wm) {
-        // centre-disk test (raster.wgsl:206-212): length(o) <= d/2 is
-        // sqrt_rn(|o|^2) <= d/2, i.e. |o|^2 <= r2_max
-        const float cx = __int2float_rn(px) + 0.5f, cy = __int2float_rn(py) + 0.5f;
-        const float gx = B.x - A.x, gy = B.y - A.y;
-        const float denom = fmaxf(gx * gx + gy * gy, 1e-6f);
-        const float closest = clampf(__fdiv_rn((cx - A.x) * gx + (cy - A.y) * gy, denom), 0.0f, 1.0f);
-        const float ox = cx - (A.x + gx * closest), oy = cy - (A.y + gy * closest);
-        wm = ox * ox + oy * oy <= k.r2_max;
-    }
-    if (!(w0 || wm || w1 || w2)) return;
-    if (a.scene) {
-        const float4 clip = mat_mul(p.clip_from_world, world.x, world.y, world.z, 1.0f);
-        const float clip_depth = __fdiv_rn(clip.z, fmaxf(clip.w, 1e-5f));
-        const bool rev = p.pass_mode[2] == 1u;
-        auto hidden = [&](uint32_t pix) {
-            const float scene = __ldg(&a.scene[pix]);
-            return rev ? clip_depth < scene : clip_depth > scene;
-        };
-        if ((w0 || wm) && hidden(pix0)) w0 = wm = false;
-        if (w1 && hidden(pix1)) w1 = false;
-        if (w2 && hidden(pix2)) w2 = false;
-        if (!(w0 || wm || w1 || w2)) return;
-    }
-    const float4 t0 = sm.ct[j], t1 = sm.ct[j + 1];
-    const f3 tangent = safe_normalize(mix3(xyz(t0), xyz(t1), t));
-    const uint32_t oct = oct_encode(tangent);
-    const uint32_t ao_q = k.ao_on ? f2u(clampf(mixf(A.z, B.z, t), 0.0f, 1.0f) * 63.0f + 0.5f) : 63u;
-    const unsigned long long payload =
-        pack_gb(depth, oct & 0xffu, oct >> 8u, quant63(mixf(k.uv.x, k.uv.x, t)), quant63(mixf(k.uv.y, k.uv.y, t)),
-                quant63(mixf(t0.w, t1.w, t)), ao_q);
-    if (w0 && payload < c0) atomicMin(&a.cons[pix0], payload);
-    if (wm) {
-        if (payload < m0) atomicMin(&a.center[pix0], payload);
-        atomicMin(&a.beta[pix0], (depth << 8u) | k.beta_q);
-    }
-    if (w1 && payload < c1) atomicMin(&a.cons[pix1], payload);
-    if (w2 && payload < c2) atomicMin(&a.cons[pix2], payload);
-}
-
 // Camera raster of one generated strand.  The DDA of every segment
 // (raster.wgsl:192-223) is flattened into one list of samples so the 32 lanes
 // share the work evenly.  Consecutive samples sit on consecutive lanes, so the
@@ -591,20 +552,29 @@ __device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& s
     __syncwarp();
 
     const int32_t total = carry;
-    const CamConst k = cam_const(p, uv, beta);
-    // Pass 1: every sample computes its pixel(s) and depth and is queued only
-    // when some word can still take it.  Pass 2 runs the full payload 32 wide
-    // over the queue, so the expensive part of write_pixel never idles lanes.
-    int32_t qn = 0;
+    const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
+    const float r2_max = sqrt_bound(fmaxf(p.appearance[3], 0.05f) * 0.5f);
+    const f3 cam = mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2]);
+    const f3 fwd = mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]);
+    const uint32_t beta_q = f2u(clampf(beta, 0.0f, 1.0f) * 255.0f + 0.5f);
+    const bool ao_on = p.flags[2] != 0u;
     int32_t carry_px = 0, carry_py = 0;
     for (int32_t base = 0; base < total; base += 32) {
         const int32_t s = min(base + (int32_t)lane, total - 1);
         const bool active = base + (int32_t)lane < total;
-        const int32_t j = find_segment(sm, nseg, s);
+        // segment j with off[j] <= s < off[j+1]
+        int32_t lo = 0, hi = nseg - 1;
+        while (lo < hi) {
+            int32_t mid = (lo + hi + 1) >> 1;
+            if (sm.u.off[mid] <= s) lo = mid; else hi = mid - 1;
+        }
+        const int32_t j = lo;
         const int32_t i = s - sm.u.off[j];
         const float4 A = sm.cs[j], B = sm.cs[j + 1];
-        const float t = __fdiv_rn(__int2float_rn(i), __int2float_rn(__float_as_int(A.w)));
-        const int32_t px = f2i(floorf(mixf(A.x, B.x, t))), py = f2i(floorf(mixf(A.y, B.y, t)));
+        const int32_t n = __float_as_int(A.w);
+        const float t = __fdiv_rn(__int2float_rn(i), __int2float_rn(n));
+        const float sx = mixf(A.x, B.x, t), sy = mixf(A.y, B.y, t);
+        const int32_t px = f2i(floorf(sx)), py = f2i(floorf(sy));
         int32_t qx = __shfl_up_sync(0xffffffffu, px, 1), qy = __shfl_up_sync(0xffffffffu, py, 1);
         if (lane == 0) {
             qx = carry_px;
@@ -612,21 +582,73 @@ __device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& s
         }
         carry_px = __shfl_sync(0xffffffffu, px, 31);
         carry_py = __shfl_sync(0xffffffffu, py, 31);
-        const bool survive = active && sample_can_write(a, k, sm, j, i, t, px, py, qx, qy);
-        const unsigned m = __ballot_sync(0xffffffffu, survive);
-        if (survive) sm.q[qn + __popc(m & ((1u << lane) - 1u))] = s;
-        qn += __popc(m);
-        if (qn >= 32) {
-            __syncwarp();
-            sample_write(a, k, sm, nseg, sm.q[lane]);
-            __syncwarp();
-            if ((int32_t)lane < qn - 32) sm.q[lane] = sm.q[lane + 32];
-            qn -= 32;
-            __syncwarp();
+        if (!active) continue;
+        const bool side = i > 0 && qx != px && qy != py;
+        const bool on0 = on_screen(px, py, width, height);
+        const bool on1 = side && on_screen(qx, py, width, height);
+        const bool on2 = side && on_screen(px, qy, width, height);
+        if (!(on0 || on1 || on2)) continue;
+        const uint32_t pix0 = (uint32_t)py * (uint32_t)width + (uint32_t)px;
+        const uint32_t pix1 = (uint32_t)py * (uint32_t)width + (uint32_t)qx;
+        const uint32_t pix2 = (uint32_t)qy * (uint32_t)width + (uint32_t)px;
+        // Current words, read from L2 before the payload is known.  Buffers only
+        // decrease during the pass, so a stale read is an upper bound: an atomicMin
+        // is skipped only when it cannot change the word.
+        const unsigned long long cur_c0 = on0 ? __ldcg(&a.cons[pix0]) : 0ull;
+        const unsigned long long cur_m0 = on0 ? __ldcg(&a.center[pix0]) : 0ull;
+        const unsigned long long cur_c1 = on1 ? __ldcg(&a.cons[pix1]) : 0ull;
+        const unsigned long long cur_c2 = on2 ? __ldcg(&a.cons[pix2]) : 0ull;
+
+        // write_pixel (raster.wgsl:83-115): depth first; the rest of the payload
+        // only when some word can still take it.
+        const float4 c0 = sm.cp[j], c1 = sm.cp[j + 1];
+        const f3 world = mix3(xyz(c0), xyz(c1), t);
+        const float dist = dot3(sub3(world, cam), fwd);
+        if (dist <= p.screen[2]) continue;
+        const uint32_t depth = quantize_depth(dist, p.screen[2], p.screen[3]);
+        const unsigned long long lower = (unsigned long long)depth << 40;  // smallest payload with this depth
+        bool w0 = on0 && lower < cur_c0;
+        bool wm = on0 && depth <= (uint32_t)(cur_m0 >> 40);
+        bool w1 = on1 && lower < cur_c1;
+        bool w2 = on2 && lower < cur_c2;
+        if (wm) {
+            // centre-disk test (raster.wgsl:206-212); length(o) <= r is
+            // sqrt_rn(|o|^2) <= r, i.e. |o|^2 <= r2_max
+            const float cx = __int2float_rn(px) + 0.5f, cy = __int2float_rn(py) + 0.5f;
+            const float gx = B.x - A.x, gy = B.y - A.y;
+            const float denom = fmaxf(gx * gx + gy * gy, 1e-6f);
+            const float closest = clampf(__fdiv_rn((cx - A.x) * gx + (cy - A.y) * gy, denom), 0.0f, 1.0f);
+            const float ox = cx - (A.x + gx * closest), oy = cy - (A.y + gy * closest);
+            wm = ox * ox + oy * oy <= r2_max;
         }
+        if (!(w0 || wm || w1 || w2)) continue;
+        if (a.scene) {
+            const float4 clip = mat_mul(p.clip_from_world, world.x, world.y, world.z, 1.0f);
+            const float clip_depth = __fdiv_rn(clip.z, fmaxf(clip.w, 1e-5f));
+            const bool rev = p.pass_mode[2] == 1u;
+            auto hidden = [&](uint32_t pix) {
+                const float scene = __ldg(&a.scene[pix]);
+                return rev ? clip_depth < scene : clip_depth > scene;
+            };
+            if ((w0 || wm) && hidden(pix0)) w0 = wm = false;
+            if (w1 && hidden(pix1)) w1 = false;
+            if (w2 && hidden(pix2)) w2 = false;
+            if (!(w0 || wm || w1 || w2)) continue;
+        }
+        const float4 t0 = sm.ct[j], t1 = sm.ct[j + 1];
+        const f3 tangent = safe_normalize(mix3(xyz(t0), xyz(t1), t));
+        const uint32_t oct = oct_encode(tangent);
+        const uint32_t ao_q = ao_on ? f2u(clampf(mixf(A.z, B.z, t), 0.0f, 1.0f) * 63.0f + 0.5f) : 63u;
+        const unsigned long long payload = pack_gb(depth, oct & 0xffu, oct >> 8u, quant63(mixf(uv.x, uv.x, t)),
+                                                   quant63(mixf(uv.y, uv.y, t)), quant63(mixf(t0.w, t1.w, t)), ao_q);
+        if (w0 && payload < cur_c0) atomicMin(&a.cons[pix0], payload);
+        if (wm) {
+            if (payload < cur_m0) atomicMin(&a.center[pix0], payload);
+            atomicMin(&a.beta[pix0], (depth << 8u) | beta_q);
+        }
+        if (w1 && payload < cur_c1) atomicMin(&a.cons[pix1], payload);
+        if (w2 && payload < cur_c2) atomicMin(&a.cons[pix2], payload);
     }
-    __syncwarp();
-    if ((int32_t)lane < qn) sample_write(a, k, sm, nseg, sm.q[lane]);
 }
 
 // write_dom_pixel (raster.wgsl:118-148) for the Bresenham pixel (px, py) of
@@ -706,9 +728,10 @@ __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) raster_kerne
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     StrandSmem& sm = smem[warp];
     const uint32_t total = a.indirect[0];
+    const uint32_t* order = a.draw_order && a.order_meta[1] ? a.draw_order : nullptr;
     const uint32_t nwarps = gridDim.x * kRasterWarps;
     for (uint32_t r = blockIdx.x * kRasterWarps + warp; r < total; r += nwarps) {
-        const hg_strand_ref ref = a.refs[r];
+        const hg_strand_ref ref = a.refs[order ? order[r] : r];
         if (ref.bundle >= a.bundle_count) {
             if (lane == 0) atomicOr(a.err, kErrBadRef);
             continue;
@@ -760,20 +783,31 @@ cudaError_t launch_lod(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int sl
     if (count == 0) return cudaSuccess;
     int threads = 256;
     int blocks = (int)((count * 32u + threads - 1) / threads);
-    lod_kernel<<<blocks, threads, 0, ctx->stream>>>(p, g->bundles, g->layers, g->lod[slot], count);
+    lod_kernel<<<blocks, threads, 0, ctx->stream>>>(p, g->bundles, g->layers, g->lod[slot], g->depth_key[slot],
+                                                    count);
     return cudaGetLastError();
 }
 
 cudaError_t launch_scan(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot) {
     uint32_t count = std::min(p.pass_mode[1], g->bundle_count);
-    scan_offsets_kernel<<<1, kScanThreads, 0, ctx->stream>>>(g->lod[slot], count, g->ref_capacity, g->offsets[slot],
-                                                            g->indirect[slot]);
+    // The camera pass draws near bundles first; the DOM passes gain nothing from it.
+    const bool order = p.pass_mode[0] == 0u;
+    scan_offsets_kernel<<<1, kScanThreads, 0, ctx->stream>>>(
+        g->lod[slot], count, g->ref_capacity, g->offsets[slot], g->indirect[slot], g->depth_key[slot],
+        order ? g->sorted[slot] : nullptr, g->sorted_off[slot], g->order_meta[slot]);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || count == 0) return e;
     int threads = 256;
     int blocks = (int)std::min<uint32_t>((count * 32u + threads - 1) / threads, (uint32_t)ctx->sm_count * 8u);
-    scan_expand_kernel<<<blocks, threads, 0, ctx->stream>>>(g->lod[slot], g->offsets[slot], count, g->ref_capacity,
-                                                            g->refs[slot]);
+    if (order) {
+        scan_expand_sorted_kernel<<<blocks, threads, 0, ctx->stream>>>(g->lod[slot], g->offsets[slot], g->sorted[slot],
+                                                                       g->sorted_off[slot], g->order_meta[slot],
+                                                                       g->ref_capacity, g->refs[slot],
+                                                                       g->draw_order[slot]);
+    } else {
+        scan_expand_kernel<<<blocks, threads, 0, ctx->stream>>>(g->lod[slot], g->offsets[slot], count,
+                                                                g->ref_capacity, g->refs[slot]);
+    }
     return cudaGetLastError();
 }
 
@@ -786,6 +820,8 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
     a.style = g->style;
     a.refs = g->refs[slot];
     a.indirect = g->indirect[slot];
+    a.draw_order = p.pass_mode[0] == 0u ? g->draw_order[slot] : nullptr;
+    a.order_meta = g->order_meta[slot];
     a.center = ctx->center;
     a.cons = ctx->cons;
     a.beta = ctx->beta;
