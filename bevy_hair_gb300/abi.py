@@ -18,6 +18,7 @@ LAYER_COUNT = 16
 STYLE_TEXELS = 1024
 DOM_LAYERS = 16
 MAX_LIGHTS = 256
+SCAN_NOALLOC_MAX_BUNDLES = 65536
 
 # --------------------------------------------------------------------- dtypes
 
@@ -127,6 +128,7 @@ _SIGNATURES = {
     "hg_composite": (_I32, [_VP, _VP, _U32]),
     "hg_clear_color": (_I32, [_VP, _F32]),
     "hg_groom_frame": (_I32, [_VP, _VP, C.POINTER(FrameDesc)]),
+    "hg_scan_noalloc": (_I32, [_VP, _U32, _U32, _VP, _VP, _VP]),
 }
 
 _BAKE_SIGNATURES = {

@@ -7,6 +7,8 @@
 // raster.wgsl (src/render/shaders/).
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "hg_device.cuh"
 #include "hg_internal.h"
 
@@ -845,3 +847,77 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
 }
 
 }  // namespace hg
+
+// ------------------------------------------------------------------ allocation-free scan
+//
+// hg_scan_noalloc: the scan pass for hosts that cannot allocate device memory
+// while they record a frame -- for example an engine whose device memory is
+// owned entirely by its own allocator or arena (a render graph that hands out
+// every buffer up front), or a real-time host with a fixed memory budget
+// that forbids allocation inside the frame loop.  The caller passes the
+// LodRecords (input) and the StrandRef and indirect buffers (outputs) as
+// device pointers; the only working memory the scan needs beyond them, the
+// per-bundle offsets, lives in the file-scope array below instead of a
+// cudaMalloc.
+
+namespace hg {
+namespace {
+
+// Largest bundle count the allocation-free scan accepts: 65,536 bundles,
+// i.e. 256 KB of offsets held on every device that loads this library.
+constexpr uint32_t kNoAllocMaxBundles = 65536;
+static __device__ __align__(256) uint32_t g_noalloc_offsets[kNoAllocMaxBundles + 1];
+
+// Device address of g_noalloc_offsets per device ordinal, looked up once.
+// The host-side name g_noalloc_offsets is not a device address, so kernels
+// are only ever given the address from cudaGetSymbolAddress.
+constexpr int kNoAllocMaxDevices = 64;
+uint32_t* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+std::mutex g_noalloc_mutex;
+
+cudaError_t noalloc_scratch(uint32_t** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+        uint32_t* ptr = nullptr;
+        e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_offsets);
+        if (e != cudaSuccess) return e;
+        g_noalloc_ptr[dev] = ptr;
+    }
+    *out = g_noalloc_ptr[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace hg
+
+// See include/hairgb.h.  The first call on a device (the device current on
+// the calling thread) looks up the scratch array's device address; make that
+// first call before any stream capture on that device.  Every call shares the
+// one array, so calls that overlap on the GPU (different streams, no ordering
+// between them) race on it; the offsets are fully rewritten by each call, so
+// nothing needs clearing between calls.
+extern "C" hg_status hg_scan_noalloc(const hg_lod_record* lod, uint32_t bundle_count, uint32_t capacity,
+                                     hg_strand_ref* refs, uint32_t* indirect, void* stream) {
+    if (!indirect || (bundle_count && (!lod || !refs)) || capacity == 0) return HG_INVALID_ARG;
+    if (bundle_count > hg::kNoAllocMaxBundles) return HG_CAPACITY_EXCEEDED;
+    uint32_t* offsets = nullptr;
+    if (hg::noalloc_scratch(&offsets) != cudaSuccess) return HG_CUDA_ERROR;
+    cudaStream_t st = (cudaStream_t)stream;
+    hg::scan_offsets_kernel<<<1, hg::kScanThreads, 0, st>>>(lod, bundle_count, capacity, offsets, indirect, nullptr,
+                                                            nullptr, nullptr, nullptr);
+    if (cudaGetLastError() != cudaSuccess) return HG_CUDA_ERROR;
+    if (bundle_count == 0) return HG_OK;
+    int sms = 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return HG_CUDA_ERROR;
+    const int threads = 256;
+    const int blocks = (int)std::min<uint32_t>((bundle_count * 32u + threads - 1) / threads, (uint32_t)sms * 8u);
+    hg::scan_expand_kernel<<<blocks, threads, 0, st>>>(lod, offsets, bundle_count, capacity, refs);
+    return cudaGetLastError() == cudaSuccess ? HG_OK : HG_CUDA_ERROR;
+}

@@ -263,6 +263,40 @@ hg_status hg_clear_color(hg_ctx* ctx, float depth_clear);
  * raster mode 2; shade; filter when camera->flags[1]; composite. */
 hg_status hg_groom_frame(hg_ctx* ctx, hg_groom* groom, const hg_frame_desc* desc);
 
+/* ---------------------------------------------------------------- allocation-free scan */
+
+/* Largest bundle_count hg_scan_noalloc accepts. */
+#define HG_SCAN_NOALLOC_MAX_BUNDLES 65536u
+
+/* The scan pass without any device allocation, for hosts that cannot call
+ * cudaMalloc while they record a frame: an engine whose device memory all comes
+ * from its own allocator or arena (every buffer handed out up front by its
+ * render graph), or a real-time host whose fixed memory budget forbids
+ * allocating inside the frame loop.  This entry point has no counterpart in
+ * the reference; it computes the same StrandRefs and indirect words as hg_scan
+ * (without hg_scan's front-to-back draw order, which needs more working
+ * memory) and needs no context.
+ *
+ * lod:      device hg_lod_record[bundle_count] (input)
+ * refs:     device hg_strand_ref[capacity] (output; entries past the total
+ *           stay untouched)
+ * indirect: device u32[4] (output: total, 1, 1, 0)
+ * stream:   cudaStream_t to launch on (NULL: the legacy default stream)
+ * Work goes on `stream` on the device current on the calling thread.
+ *
+ * The per-bundle offsets live in a fixed device array of
+ * HG_SCAN_NOALLOC_MAX_BUNDLES + 1 words (256 KB) that every device holds while
+ * the library is loaded; larger bundle counts return HG_CAPACITY_EXCEEDED.
+ * The first call on a device looks up that array's device address, so make
+ * the first call on each device before any stream capture on it.  All calls
+ * share the one array: calls that can overlap on the GPU (unordered streams)
+ * race and must be serialised by the caller.  Each call rewrites the offsets
+ * it reads, so nothing has to be cleared between calls.  Returns
+ * HG_INVALID_ARG for null pointers or capacity 0 and HG_CUDA_ERROR when a
+ * launch fails. */
+hg_status hg_scan_noalloc(const hg_lod_record* lod, uint32_t bundle_count, uint32_t capacity,
+                          hg_strand_ref* refs, uint32_t* indirect, void* stream);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif
