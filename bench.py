@@ -105,6 +105,14 @@ class Dist:
             self.td.destroy_process_group()
 
 
+def aggregate(dist: "Dist", local_ms: float, local_segments: float) -> tuple[float, float, float]:
+    """Whole-job throughput of N replicas: segments summed over ranks divided by
+    the slowest rank's time.  Returns (Gseg/s, max ms, total segments)."""
+    total_ms = dist.max(local_ms)
+    total_segs = dist.sum(local_segments)
+    return total_segs / (total_ms * 1e-3) / 1e9, total_ms, total_segs
+
+
 class Clocks:
     """nvidia-smi samples during the timed region."""
 
@@ -243,10 +251,8 @@ def run_ours(args, rank, world, local):
     dist.barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     local_ms = float(np.sum(step_ms))
-    total_ms = dist.max(local_ms)
+    value, total_ms, total_segs = aggregate(dist, local_ms, float(seg_c) * args.steps)
     ms_per_step = total_ms / args.steps
-    total_segs = dist.sum(float(seg_c) * args.steps)
-    value = total_segs / (total_ms * 1e-3) / 1e9
 
     # per-pass breakdown on this rank: events between the pass calls
     passes = ["clear", "lod_camera", "scan_camera", "raster_camera", "clear_dom", "lod_dom", "scan_dom",
@@ -304,8 +310,7 @@ def run_ours(args, rank, world, local):
         t_s = time.perf_counter()
         e2e_step()
         e2e_total += time.perf_counter() - t_s
-    e2e_ms = dist.max(e2e_total * 1e3)
-    e2e_value = total_segs / (e2e_ms * 1e-3) / 1e9
+    e2e_value, e2e_ms, _ = aggregate(dist, e2e_total * 1e3, float(seg_c) * args.steps)
     launches = 15 * args.steps
 
     cpu = None
