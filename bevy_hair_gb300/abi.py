@@ -123,6 +123,7 @@ _SIGNATURES = {
     "hg_lod": (_I32, [_VP, _VP, _VP, _I32]),
     "hg_scan": (_I32, [_VP, _VP, _VP, _I32]),
     "hg_raster": (_I32, [_VP, _VP, _VP, _I32, _VP]),
+    "hg_generate": (_I32, [_VP, _VP, _VP]),
     "hg_shade": (_I32, [_VP, _VP, C.POINTER(ShadeDesc)]),
     "hg_filter": (_I32, [_VP, _VP]),
     "hg_composite": (_I32, [_VP, _VP, _U32]),

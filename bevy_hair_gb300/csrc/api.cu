@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "../../include/hairgb.h"
 #include "hg_internal.h"
@@ -288,6 +289,18 @@ hg_status hg_groom_upload(hg_ctx* ctx, const hg_gpu_bundle* bundles, uint32_t bu
         alloc(g->draw_order[s], (size_t)g->ref_capacity * 4);
         alloc(g->order_meta[s], 8);
     }
+    // Per-strand bundle index and per-bundle first strand, for the strand cache.
+    std::vector<uint32_t> base(bundle_count + 1u, 0u), owner(g->strand_total);
+    for (uint32_t b = 0; b < bundle_count; ++b) {
+        base[b + 1] = base[b] + bundles[b].strand_count;
+        for (uint32_t s2 = base[b]; s2 < base[b + 1]; ++s2) owner[s2] = b;
+    }
+    alloc(g->strand_base, base.size() * 4);
+    alloc(g->strand_bundle, (size_t)g->strand_total * 4);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(g->strand_base, base.data(), base.size() * 4, cudaMemcpyHostToDevice,
+                                              ctx->stream);
+    if (e == cudaSuccess && g->strand_total)
+        e = cudaMemcpyAsync(g->strand_bundle, owner.data(), owner.size() * 4, cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess && bundle_count) {
         e = cudaMemcpyAsync(g->bundles, bundles, (size_t)bundle_count * sizeof(hg_gpu_bundle), cudaMemcpyHostToDevice,
                             ctx->stream);
@@ -318,6 +331,9 @@ hg_status hg_groom_destroy(hg_ctx* ctx, hg_groom* g) {
     free_dev(g->bundles);
     free_dev(g->layers);
     free_dev(g->style);
+    free_dev(g->strand_base);
+    free_dev(g->strand_bundle);
+    free_dev(g->cache);
     for (int s = 0; s < 2; ++s) {
         free_dev(g->lod[s]);
         free_dev(g->refs[s]);
@@ -387,6 +403,20 @@ hg_status hg_lod(hg_ctx* ctx, hg_groom* g, const hg_hair_params* p, hg_view_slot
 hg_status hg_scan(hg_ctx* ctx, hg_groom* g, const hg_hair_params* p, hg_view_slot slot) {
     if (!ctx || !g || !p || (slot != HG_SLOT_CAMERA && slot != HG_SLOT_DOM)) return HG_INVALID_ARG;
     HG_CUDA(ctx, hg::launch_scan(ctx, g, *p, slot));
+    return HG_OK;
+}
+
+hg_status hg_generate(hg_ctx* ctx, hg_groom* g, const hg_hair_params* p) {
+    if (!ctx || !g || !p) return HG_INVALID_ARG;
+    if (!g->cache && g->strand_total) {
+        cudaSetDevice(ctx->device);
+        size_t bytes = (size_t)g->strand_total * 2u * hg::kStrandCacheCps * sizeof(float4);
+        HG_CUDA(ctx, cudaMalloc((void**)&g->cache, bytes));
+    }
+    g->cache_valid = false;
+    HG_CUDA(ctx, hg::launch_generate(ctx, g, *p));
+    std::memcpy(g->cache_model, p->world_from_model, sizeof(g->cache_model));
+    g->cache_valid = true;
     return HG_OK;
 }
 
@@ -464,6 +494,10 @@ hg_status hg_groom_frame(hg_ctx* ctx, hg_groom* g, const hg_frame_desc* d) {
     if ((s = hg_clear(ctx)) != HG_OK) return s;
     if ((s = hg_lod(ctx, g, &cam, HG_SLOT_CAMERA)) != HG_OK) return s;
     if ((s = hg_scan(ctx, g, &cam, HG_SLOT_CAMERA)) != HG_OK) return s;
+    // With the deep opacity map on, every strand is drawn at full detail at
+    // least once, so each is generated once into the strand cache and the
+    // camera and DOM rasters read it.
+    if (dom && (s = hg_generate(ctx, g, &cam)) != HG_OK) return s;
     if ((s = hg_raster(ctx, g, &cam, HG_SLOT_CAMERA, d->scene_depth)) != HG_OK) return s;
     if (dom) {
         hg_hair_params layers_params = *d->dom;

@@ -29,6 +29,12 @@ struct hg_groom {
     uint32_t* sorted_off[2] = {nullptr, nullptr};  // scan of n_lod in that order, bundle_count + 1
     uint32_t* draw_order[2] = {nullptr, nullptr};  // permutation of refs, ref_capacity
     uint32_t* order_meta[2] = {nullptr, nullptr};  // (live bundles, order valid)
+    // Strand cache (hg_generate): world-space control points of every strand.
+    uint32_t* strand_bundle = nullptr;  // bundle of each strand, strand_total
+    uint32_t* strand_base = nullptr;    // first strand of each bundle, bundle_count + 1
+    float4* cache = nullptr;            // strand_total * 2 * 65 float4, allocated on first use
+    bool cache_valid = false;
+    float cache_model[16] = {};         // world_from_model the cache was generated with
 };
 
 struct hg_ctx {
@@ -66,6 +72,8 @@ cudaError_t launch_clear_dom(hg_ctx* ctx);
 cudaError_t launch_lod(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot);
 cudaError_t launch_scan(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot);
 cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot, const float* scene);
+cudaError_t launch_generate(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p);
+constexpr uint32_t kStrandCacheCps = 65;
 
 // shade.cu
 cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights, uint32_t ortho, float exposure,

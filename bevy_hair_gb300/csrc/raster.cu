@@ -7,6 +7,7 @@
 // raster.wgsl (src/render/shaders/).
 #include <cuda_runtime.h>
 
+#include <cstring>
 #include <mutex>
 
 #include "hg_device.cuh"
@@ -333,6 +334,8 @@ struct RasterArgs {
     const uint32_t* indirect;
     const uint32_t* draw_order;  // permutation of refs to visit, or nullptr
     const uint32_t* order_meta;  // (live bundles, order valid)
+    const float4* cache;         // strand cache (kCacheCps positions then tangents per strand), or nullptr
+    const uint32_t* strand_base; // first strand of each bundle in the cache
     unsigned long long* center;
     unsigned long long* cons;
     uint32_t* beta;
@@ -403,18 +406,20 @@ __device__ __forceinline__ f3 shfl_idx3(f3 v, int src) {
             __shfl_sync(0xffffffffu, v.z, src)};
 }
 
-// Strand generation (raster.wgsl:231-317) for one warp.  Leaves world-space
-// control points (+ in_front), screen positions and, for the camera pass,
-// world tangents, w and ao in shared memory.  The DOM passes need positions
-// only, so they skip the tangents.
-template <int MODE>
-__device__ __forceinline__ uint32_t generate_strand(const RasterArgs& a, StrandSmem& sm, const hg_strand_ref& ref,
-                                                    const hg_gpu_bundle& bundle, float2 uv, uint32_t lane) {
-    const hg_hair_params& p = a.p;
-    // Layer samples on lanes 0..15; neighbours come over shuffles.
+// Control points cached per frame: control_points_for_lod(1.0), the count of
+// every deep-opacity strand and of camera strands at full detail.
+constexpr uint32_t kCacheCps = 65;
+
+// Model-space control points of one strand (raster.wgsl:231-284): layer
+// samples on lanes 0..15 (neighbours over shuffles) and their finite-difference
+// tangents into lp/lt, then eval_cp for control point j on lane j % 32, slot
+// j / 32.
+__device__ __forceinline__ void model_cps(const float4* __restrict__ layers, const float4* __restrict__ style,
+                                          float4* lp, float4* lt, const hg_gpu_bundle& bundle, float2 uv,
+                                          uint32_t ncp, uint32_t lane, f3 mp[4], float wk[4], float aok[4]) {
     float4 loaded = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (lane < kLayerCount) {
-        const float4* c = a.layers + 2u * (bundle.layer_offset + lane * 4u);
+        const float4* c = layers + 2u * (bundle.layer_offset + lane * 4u);
         loaded = bilinear4(__ldg(c), __ldg(c + 2), __ldg(c + 4), __ldg(c + 6), uv);
     }
     float4 prev_l = shfl_up4(loaded, 1);
@@ -424,16 +429,11 @@ __device__ __forceinline__ uint32_t generate_strand(const RasterArgs& a, StrandS
         f3 prev = lane == 0u ? curr : xyz(prev_l);
         f3 next = lane + 1u >= kLayerCount ? curr : xyz(next_l);
         f3 t = calc_tangent(lane, kLayerCount, prev, curr, next);
-        sm.u.gen.lp[lane] = loaded;
-        sm.u.gen.lt[lane] = make_float4(t.x, t.y, t.z, 0.0f);
+        lp[lane] = loaded;
+        lt[lane] = make_float4(t.x, t.y, t.z, 0.0f);
     }
     __syncwarp();
-
-    const uint32_t ncp = min(max(ref.control_points, 2u), 127u);
     const float den = __uint2float_rn(max(ncp - 1u, 1u));
-    // eval_cp (raster.wgsl:62-75): control point j lives on lane j % 32, slot j / 32.
-    f3 mp[4];
-    float wk[4], aok[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const uint32_t idx = lane + 32u * k;
@@ -445,51 +445,100 @@ __device__ __forceinline__ uint32_t generate_strand(const RasterArgs& a, StrandS
             uint32_t i0 = min(f2u(floorf(layers_f)), kLayerCount - 1u);
             uint32_t i1 = min(i0 + 1u, kLayerCount - 1u);
             float t = layers_f - __uint2float_rn(i0);
-            float4 la = sm.u.gen.lp[i0], lb = sm.u.gen.lp[i1];
-            f3 base = hermite(xyz(la), xyz(lb), xyz(sm.u.gen.lt[i0]), xyz(sm.u.gen.lt[i1]), t);
-            f3 res = sample_style(a.style, bundle.style_offset, uv, w);
+            float4 la = lp[i0], lb = lp[i1];
+            f3 base = hermite(xyz(la), xyz(lb), xyz(lt[i0]), xyz(lt[i1]), t);
+            f3 res = sample_style(style, bundle.style_offset, uv, w);
             mp[k] = add3(base, res);
             wk[k] = w;
             aok[k] = mixf(la.w, lb.w, t);
         }
     }
+}
 
-    // Control-point tangents (raster.wgsl:286-317): neighbours j-1 and j+1 are
-    // the next lane down/up of the same slot, or lane 31 / lane 0 of the
-    // adjacent slot.  Then world space and projection, stored once.
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-        const uint32_t idx = lane + 32u * k;
-        f3 prev = mp[k], next = mp[k];
-        if (MODE == 0) {
-            prev = shfl_up3(mp[k]);
-            next = shfl_down3(mp[k]);
-            if (k > 0) {
-                f3 w31 = shfl_idx3(mp[k > 0 ? k - 1 : 0], 31);
-                if (lane == 0) prev = w31;
-            }
-            if (k < 3) {
-                f3 w0 = shfl_idx3(mp[k < 3 ? k + 1 : 3], 0);
-                if (lane == 31) next = w0;
-            }
-        }
-        if (idx < ncp) {
-            const f3 curr = mp[k];
-            const f3 wp = to_world(p, curr);
-            const Projected pr = project_world(p, wp);
-            sm.cp[idx] = make_float4(wp.x, wp.y, wp.z, pr.in_front ? 1.0f : 0.0f);
-            if (MODE == 0) {
-                f3 pp = idx > 0u ? prev : curr;
-                f3 nn = idx + 1u < ncp ? next : curr;
-                f3 tm = safe_normalize(calc_tangent(idx, ncp, pp, curr, nn));
-                f3 wt = dir_world(p, tm);
-                sm.ct[idx] = make_float4(wt.x, wt.y, wt.z, wk[k]);
-                sm.cs[idx] = make_float4(pr.screen.x, pr.screen.y, aok[k], 0.0f);
-            } else {
-                sm.cs[idx] = make_float4(pr.screen.x, pr.screen.y, 0.0f, 0.0f);
-            }
-        }
+// Neighbours j-1 and j+1 of the control point in slot k of this lane: the next
+// lane down/up of the same slot, or lane 31 / lane 0 of the adjacent slot.
+// Every lane of the warp must call this (shuffles).
+template <int K>
+__device__ __forceinline__ void cp_neighbours(const f3 mp[4], uint32_t lane, f3& prev, f3& next) {
+    prev = shfl_up3(mp[K]);
+    next = shfl_down3(mp[K]);
+    if (K > 0) {
+        f3 w31 = shfl_idx3(mp[K > 0 ? K - 1 : 0], 31);
+        if (lane == 0) prev = w31;
     }
+    if (K < 3) {
+        f3 w0 = shfl_idx3(mp[K < 3 ? K + 1 : 3], 0);
+        if (lane == 31) next = w0;
+    }
+}
+
+// World tangent of control point idx (raster.wgsl:286-317, then dir_world).
+__device__ __forceinline__ f3 cp_world_tangent(const hg_hair_params& p, uint32_t idx, uint32_t ncp, f3 prev, f3 curr,
+                                               f3 next) {
+    const f3 pp = idx > 0u ? prev : curr;
+    const f3 nn = idx + 1u < ncp ? next : curr;
+    return dir_world(p, safe_normalize(calc_tangent(idx, ncp, pp, curr, nn)));
+}
+
+// Projection and shared-memory layout of one control point.
+template <int MODE>
+__device__ __forceinline__ void store_cp(const hg_hair_params& p, StrandSmem& sm, uint32_t idx, f3 wp, f3 wt, float w,
+                                         float ao) {
+    const Projected pr = project_world(p, wp);
+    sm.cp[idx] = make_float4(wp.x, wp.y, wp.z, pr.in_front ? 1.0f : 0.0f);
+    if (MODE == 0) {
+        sm.ct[idx] = make_float4(wt.x, wt.y, wt.z, w);
+        sm.cs[idx] = make_float4(pr.screen.x, pr.screen.y, ao, 0.0f);
+    } else {
+        sm.cs[idx] = make_float4(pr.screen.x, pr.screen.y, 0.0f, 0.0f);
+    }
+}
+
+template <int K, int MODE>
+__device__ __forceinline__ void generate_slot(const hg_hair_params& p, StrandSmem& sm, const f3 mp[4],
+                                              const float wk[4], const float aok[4], uint32_t ncp, uint32_t lane) {
+    const uint32_t idx = lane + 32u * K;
+    f3 prev = mp[K], next = mp[K];
+    if (MODE == 0) cp_neighbours<K>(mp, lane, prev, next);
+    if (idx < ncp) {
+        const f3 wp = to_world(p, mp[K]);
+        const f3 wt = MODE == 0 ? cp_world_tangent(p, idx, ncp, prev, mp[K], next) : mk3(0.0f, 0.0f, 0.0f);
+        store_cp<MODE>(p, sm, idx, wp, wt, wk[K], aok[K]);
+    }
+}
+
+// Strand generation (raster.wgsl:231-317) for one warp.  Leaves world-space
+// control points (+ in_front), screen positions and, for the camera pass,
+// world tangents, w and ao in shared memory.  Strands at kCacheCps control
+// points come from the frame's strand cache when one is given; the DOM passes
+// need positions only.
+template <int MODE>
+__device__ __forceinline__ uint32_t generate_strand(const RasterArgs& a, StrandSmem& sm, const hg_strand_ref& ref,
+                                                    const hg_gpu_bundle& bundle, float2 uv, uint32_t lane) {
+    const hg_hair_params& p = a.p;
+    const uint32_t ncp = min(max(ref.control_points, 2u), 127u);
+    if (a.cache && ncp == kCacheCps) {
+        const float4* pos = a.cache + (size_t)(a.strand_base[ref.bundle] + ref.strand) * (2u * kCacheCps);
+        const float4* tan = pos + kCacheCps;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            const uint32_t idx = lane + 32u * k;
+            if (idx < kCacheCps) {
+                const float4 wp = __ldg(pos + idx);
+                const float4 wt = MODE == 0 ? __ldg(tan + idx) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                store_cp<MODE>(p, sm, idx, xyz(wp), xyz(wt), wt.w, wp.w);
+            }
+        }
+        __syncwarp();
+        return ncp;
+    }
+    f3 mp[4];
+    float wk[4], aok[4];
+    model_cps(a.layers, a.style, sm.u.gen.lp, sm.u.gen.lt, bundle, uv, ncp, lane, mp, wk, aok);
+    generate_slot<0, MODE>(p, sm, mp, wk, aok, ncp, lane);
+    generate_slot<1, MODE>(p, sm, mp, wk, aok, ncp, lane);
+    generate_slot<2, MODE>(p, sm, mp, wk, aok, ncp, lane);
+    generate_slot<3, MODE>(p, sm, mp, wk, aok, ncp, lane);
     __syncwarp();
     return ncp;
 }
@@ -723,6 +772,54 @@ __device__ __forceinline__ void raster_dom(const RasterArgs& a, StrandSmem& sm, 
     }
 }
 
+// Strand cache: every strand of the groom at kCacheCps control points, world
+// space, warp per strand.  Per strand kCacheCps float4 (position, ao) then
+// kCacheCps float4 (world tangent, w); the raster passes read these instead
+// of regenerating the strand (raster.wgsl:231-317 is the same computation).
+struct GenArgs {
+    hg_hair_params p;
+    const hg_gpu_bundle* bundles;
+    const float4* layers;
+    const float4* style;
+    const uint32_t* strand_bundle;  // bundle of each strand
+    const uint32_t* strand_base;    // first strand of each bundle
+    float4* cache;
+    uint32_t strands;
+};
+
+__global__ void __launch_bounds__(kRasterThreads) generate_kernel(const GenArgs a) {
+    __shared__ float4 lp[kRasterWarps][16];
+    __shared__ float4 lt[kRasterWarps][16];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t nwarps = gridDim.x * kRasterWarps;
+    for (uint32_t g = blockIdx.x * kRasterWarps + warp; g < a.strands; g += nwarps) {
+        const uint32_t b = a.strand_bundle[g];
+        const uint32_t s = g - a.strand_base[b];
+        const hg_gpu_bundle bundle = a.bundles[b];
+        const float2 uv = pcg_uv(s ^ (b * 0x85ebca6bu));
+        f3 mp[4];
+        float wk[4], aok[4];
+        model_cps(a.layers, a.style, lp[warp], lt[warp], bundle, uv, kCacheCps, lane, mp, wk, aok);
+        float4* pos = a.cache + (size_t)g * (2u * kCacheCps);
+        float4* tan = pos + kCacheCps;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            f3 prev, next;
+            if (k == 0) cp_neighbours<0>(mp, lane, prev, next);
+            if (k == 1) cp_neighbours<1>(mp, lane, prev, next);
+            if (k == 2) cp_neighbours<2>(mp, lane, prev, next);
+            const uint32_t idx = lane + 32u * k;
+            if (idx < kCacheCps) {
+                const f3 wp = to_world(a.p, mp[k]);
+                const f3 wt = cp_world_tangent(a.p, idx, kCacheCps, prev, mp[k], next);
+                pos[idx] = make_float4(wp.x, wp.y, wp.z, aok[k]);
+                tan[idx] = make_float4(wt.x, wt.y, wt.z, wk[k]);
+            }
+        }
+        __syncwarp();
+    }
+}
+
 // raster.wgsl:225-337: one warp per strand ref, persistent over the refs.
 template <int MODE>
 __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) raster_kernel(const RasterArgs a) {
@@ -813,6 +910,22 @@ cudaError_t launch_scan(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int s
     return cudaGetLastError();
 }
 
+cudaError_t launch_generate(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p) {
+    if (g->strand_total == 0) return cudaSuccess;
+    GenArgs a;
+    a.p = p;
+    a.bundles = g->bundles;
+    a.layers = g->layers;
+    a.style = g->style;
+    a.strand_bundle = g->strand_bundle;
+    a.strand_base = g->strand_base;
+    a.cache = g->cache;
+    a.strands = g->strand_total;
+    int blocks = blocks_for(ctx, (const void*)generate_kernel, kRasterThreads, g->strand_total, kRasterWarps);
+    generate_kernel<<<blocks, kRasterThreads, 0, ctx->stream>>>(a);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot, const float* scene) {
     if (g->bundle_count == 0) return cudaSuccess;
     RasterArgs a;
@@ -824,6 +937,10 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
     a.indirect = g->indirect[slot];
     a.draw_order = p.pass_mode[0] == 0u ? g->draw_order[slot] : nullptr;
     a.order_meta = g->order_meta[slot];
+    const bool cached = g->cache && g->cache_valid &&
+                        std::memcmp(g->cache_model, p.world_from_model, sizeof(g->cache_model)) == 0;
+    a.cache = cached ? g->cache : nullptr;
+    a.strand_base = g->strand_base;
     a.center = ctx->center;
     a.cons = ctx->cons;
     a.beta = ctx->beta;

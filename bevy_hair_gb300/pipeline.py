@@ -162,6 +162,9 @@ class HairRenderer:
     def scan(self, groom: GpuGroom, params: np.ndarray, slot: int) -> None:
         _check(self.lib, self.ctx, self.lib.hg_scan(self.ctx, groom.handle, params.ctypes.data, slot))
 
+    def generate(self, groom: GpuGroom, params: np.ndarray) -> None:
+        _check(self.lib, self.ctx, self.lib.hg_generate(self.ctx, groom.handle, params.ctypes.data))
+
     def raster(self, groom: GpuGroom, params: np.ndarray, slot: int, scene_depth_ptr: int | None = None) -> None:
         _check(self.lib, self.ctx,
                self.lib.hg_raster(self.ctx, groom.handle, params.ctypes.data, slot, scene_depth_ptr))

@@ -247,6 +247,15 @@ hg_status hg_scan(hg_ctx* ctx, hg_groom* groom, const hg_hair_params* params, hg
  * scene_depth: device float[W*H] scene depth (raster.wgsl:93-100) or NULL. */
 hg_status hg_raster(hg_ctx* ctx, hg_groom* groom, const hg_hair_params* params,
                     hg_view_slot slot, const float* scene_depth);
+/* Strand cache: generates every strand of the groom at the full 65 control
+ * points (control_points_for_lod(1.0)) in world space with
+ * params->world_from_model -- the strand generation of raster.wgsl:231-317,
+ * run once.  Later hg_raster calls whose params carry the same
+ * world_from_model read refs drawn at 65 control points from the cache
+ * instead of regenerating them; results are identical either way.  The
+ * reference regenerates strands in every raster dispatch, so this pass has no
+ * counterpart there.  The cache (2 KiB per strand) is allocated on first use. */
+hg_status hg_generate(hg_ctx* ctx, hg_groom* groom, const hg_hair_params* params);
 /* shade.wesl:523-593 (Karis model) over every pixel. */
 hg_status hg_shade(hg_ctx* ctx, const hg_hair_params* params, const hg_shade_desc* desc);
 /* filter.wgsl:20-135. */
@@ -260,7 +269,8 @@ hg_status hg_clear_color(hg_ctx* ctx, float depth_clear);
 
 /* The whole per-groom sequence of hair_pass: clear, lod, scan, raster; when
  * camera->flags[3] (deep_opacity): clear_dom, lod, scan, raster mode 1,
- * raster mode 2; shade; filter when camera->flags[1]; composite. */
+ * raster mode 2; shade; filter when camera->flags[1]; composite.  With the
+ * deep opacity map on it also runs hg_generate once before the rasters. */
 hg_status hg_groom_frame(hg_ctx* ctx, hg_groom* groom, const hg_frame_desc* desc);
 
 /* ---------------------------------------------------------------- allocation-free scan */

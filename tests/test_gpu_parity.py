@@ -129,6 +129,41 @@ def test_visibility_and_dom_bit_exact(renderer, name):
     _check_visibility(got, want)
 
 
+@pytest.mark.parametrize("name", ["config2", "config3_far"])
+def test_strand_cache_gives_the_same_visibility(renderer, name):
+    """hg_generate then the rasters: refs at 65 control points read the strand
+    cache, the others generate in the raster; the buffers must not change."""
+    if name == "config2":
+        sc = configs.config2(scale=0.02)
+    else:  # LOD levels: only part of the camera refs are at 65 control points
+        sc = configs.config3(scale=0.01)
+        sc.view = configs._camera(sc.view.width, sc.view.height, 3000.0)
+        sc.groom.lam = 1.0
+    cam, dom = sc.params()
+    renderer.ensure_targets(sc.view.width, sc.view.height, *sc.dom_size)
+    g = renderer.upload(sc.mesh)
+    renderer.generate(g, cam)
+    renderer.clear()
+    renderer.lod(g, cam, abi.SLOT_CAMERA)
+    renderer.scan(g, cam, abi.SLOT_CAMERA)
+    renderer.raster(g, cam, abi.SLOT_CAMERA)
+    renderer.clear_dom()
+    renderer.lod(g, dom, abi.SLOT_DOM)
+    renderer.scan(g, dom, abi.SLOT_DOM)
+    renderer.raster(g, dom, abi.SLOT_DOM)
+    renderer.raster(g, host.dom_layers_params(dom), abi.SLOT_DOM)
+    assert renderer.synchronize() == 0
+    want = _oracle_visibility(sc, cam, dom)
+    _assert_equal("center", renderer.read(abi.BUF_CENTER), want["center"])
+    _assert_equal("conservative", renderer.read(abi.BUF_CONSERVATIVE), want["cons"])
+    _assert_equal("beta", renderer.read(abi.BUF_BETA), want["beta"])
+    _assert_equal("dom", renderer.read(abi.BUF_DOM), want["dom"])
+    cps = want["lod"]["control_points"][want["lod"]["n_lod"] > 0]
+    if name != "config2":
+        assert (cps == 65).any() and (cps != 65).any()
+    g.close()
+
+
 @pytest.mark.parametrize("diameter", [0.01, 0.3, 0.7, 1.0, 1.41421356, 2.5])
 def test_center_disk_diameters(renderer, diameter):
     """The centre-sample acceptance disk (raster.wgsl:201,212) at several
