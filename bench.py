@@ -178,10 +178,11 @@ def pass_bytes(sc, seg_refs: dict) -> dict:
     groom_in = b * (16 + 2048 + 16384)
     return {
         "clear": 20 * px,
-        "raster_camera": 20 * px + groom_in + 16 * seg_refs["camera_refs"],
+        "generate": groom_in + 2 * 65 * 16 * seg_refs["strands"],
+        "raster_camera": 20 * px + 2 * 65 * 16 * seg_refs["camera_refs"],
         "clear_dom": 68 * tex,
-        "raster_dom_depth": 4 * tex + groom_in + 16 * seg_refs["dom_refs"],
-        "raster_dom_layers": 68 * tex + groom_in + 16 * seg_refs["dom_refs"],
+        "raster_dom_depth": 4 * tex + 65 * 16 * seg_refs["dom_refs"],
+        "raster_dom_layers": 68 * tex + 65 * 16 * seg_refs["dom_refs"],
         "shade": 12 * px + 20 * px + 4 * 68 * seg_refs["hair_pixels"],
         "filter": 32 * px + 20 * px,
         "composite": 20 * px + 40 * px,
@@ -255,7 +256,7 @@ def run_ours(args, rank, world, local):
     ms_per_step = total_ms / args.steps
 
     # per-pass breakdown on this rank: events between the pass calls
-    passes = ["clear", "lod_camera", "scan_camera", "raster_camera", "clear_dom", "lod_dom", "scan_dom",
+    passes = ["clear", "lod_camera", "scan_camera", "clear_dom", "lod_dom", "scan_dom", "generate", "raster_camera",
               "raster_dom_depth", "raster_dom_layers", "shade", "filter", "clear_color", "composite"]
     reps = max(3, min(args.steps, 10))
     acc = {p: 0.0 for p in passes}
@@ -265,9 +266,9 @@ def run_ours(args, rank, world, local):
         flush.fill_(3)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(len(passes) + 1)]
         ev[0].record(stream)
-        calls = [lambda: r.clear(), lambda: r.lod(g, cam, 0), lambda: r.scan(g, cam, 0),
-                 lambda: r.raster(g, cam, 0), lambda: r.clear_dom(), lambda: r.lod(g, dom, 1),
-                 lambda: r.scan(g, dom, 1), lambda: r.raster(g, dom, 1), lambda: r.raster(g, layers, 1),
+        calls = [lambda: r.clear(), lambda: r.lod(g, cam, 0), lambda: r.scan(g, cam, 0), lambda: r.clear_dom(),
+                 lambda: r.lod(g, dom, 1), lambda: r.scan(g, dom, 1), lambda: r.generate(g, cam),
+                 lambda: r.raster(g, cam, 0), lambda: r.raster(g, dom, 1), lambda: r.raster(g, layers, 1),
                  lambda: r.shade(cam, lights), lambda: r.filter(cam), lambda: r.clear_color(0.0),
                  lambda: r.composite(cam, True)]
         for k, call in enumerate(calls):
@@ -277,7 +278,8 @@ def run_ours(args, rank, world, local):
         for k, p in enumerate(passes):
             acc[p] += ev[k].elapsed_time(ev[k + 1]) / reps
     per_pass = {p: round(v, 4) for p, v in acc.items()}
-    nbytes = pass_bytes(sc, {"camera_refs": ref_c, "dom_refs": ref_d, "hair_pixels": hair_px})
+    nbytes = pass_bytes(sc, {"camera_refs": ref_c, "dom_refs": ref_d, "hair_pixels": hair_px,
+                             "strands": sc.mesh.strand_count()})
     dominant = max((p for p in nbytes), key=lambda p: acc[p])
     peak, peak_kind = peaks()
     achieved = nbytes[dominant] / (acc[dominant] * 1e-3) / 1e9
@@ -311,7 +313,7 @@ def run_ours(args, rank, world, local):
         e2e_step()
         e2e_total += time.perf_counter() - t_s
     e2e_value, e2e_ms, _ = aggregate(dist, e2e_total * 1e3, float(seg_c) * args.steps)
-    launches = 15 * args.steps
+    launches = 16 * args.steps
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

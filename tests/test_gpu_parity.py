@@ -137,7 +137,7 @@ def test_strand_cache_gives_the_same_visibility(renderer, name):
         sc = configs.config2(scale=0.02)
     else:  # LOD levels: only part of the camera refs are at 65 control points
         sc = configs.config3(scale=0.01)
-        sc.view = configs._camera(sc.view.width, sc.view.height, 3000.0)
+        sc.view = configs._camera(sc.view.width, sc.view.height, 1200.0)
         sc.groom.lam = 1.0
     cam, dom = sc.params()
     renderer.ensure_targets(sc.view.width, sc.view.height, *sc.dom_size)
