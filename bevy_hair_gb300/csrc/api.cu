@@ -139,6 +139,9 @@ hg_status hg_create(int device, void* stream, hg_ctx** out) {
             ctx->own_stream = e == cudaSuccess;
         }
     }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+    for (cudaEvent_t* ev : {&ctx->ev_fork, &ctx->ev_gen, &ctx->ev_join})
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->err, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->err, 0, sizeof(uint32_t), ctx->stream);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->lights, sizeof(hg_light) * HG_MAX_LIGHTS);
@@ -163,6 +166,12 @@ hg_status hg_destroy(hg_ctx* ctx) {
     if (ctx->lights_host) cudaFreeHost(ctx->lights_host);
     for (int i = 0; i < hg_ctx::kLightSlots; ++i)
         if (ctx->light_events[i]) cudaEventDestroy(ctx->light_events[i]);
+    if (ctx->side) {
+        cudaStreamSynchronize(ctx->side);
+        cudaStreamDestroy(ctx->side);
+    }
+    for (cudaEvent_t ev : {ctx->ev_fork, ctx->ev_gen, ctx->ev_join})
+        if (ev) cudaEventDestroy(ev);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return HG_OK;
@@ -490,31 +499,56 @@ hg_status hg_groom_frame(hg_ctx* ctx, hg_groom* g, const hg_frame_desc* d) {
     const bool dom = cam.flags[3] != 0u;
     if (dom && (!d->dom || d->dom->pass_mode[0] != 1u))
         return fail(ctx, HG_INVALID_ARG, "deep opacity needs DOM params with pass_mode.x == 1");
+    // The camera and deep-opacity halves of the frame are independent until
+    // shading, so the DOM half (and the colour-target clear) runs on the
+    // context's side stream, forked from and joined back into the main stream
+    // with events: work before and after the frame stays ordered on the main
+    // stream.
+    const cudaStream_t main_stream = ctx->stream;
+    struct Restore {
+        hg_ctx* c;
+        cudaStream_t st;
+        ~Restore() { c->stream = st; }
+    } restore{ctx, main_stream};
+    auto on = [&](cudaStream_t st) { ctx->stream = st; };
+    HG_CUDA(ctx, cudaEventRecord(ctx->ev_fork, main_stream));
+    HG_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
     hg_status s;
+    // main: camera setup, then (with the DOM on) the strand cache: every strand
+    // is drawn at full detail at least once, so each is generated once and the
+    // camera and DOM rasters read it.
+    on(main_stream);
     if ((s = hg_clear(ctx)) != HG_OK) return s;
     if ((s = hg_lod(ctx, g, &cam, HG_SLOT_CAMERA)) != HG_OK) return s;
     if ((s = hg_scan(ctx, g, &cam, HG_SLOT_CAMERA)) != HG_OK) return s;
-    // With the deep opacity map on, every strand is drawn at full detail at
-    // least once, so each is generated once into the strand cache and the
-    // camera and DOM rasters read it.
-    if (dom && (s = hg_generate(ctx, g, &cam)) != HG_OK) return s;
-    if ((s = hg_raster(ctx, g, &cam, HG_SLOT_CAMERA, d->scene_depth)) != HG_OK) return s;
+    if (dom) {
+        if ((s = hg_generate(ctx, g, &cam)) != HG_OK) return s;
+        HG_CUDA(ctx, cudaEventRecord(ctx->ev_gen, main_stream));
+    }
+    // side: DOM setup, the two DOM rasters after the cache, colour clear
+    on(ctx->side);
     if (dom) {
         hg_hair_params layers_params = *d->dom;
         layers_params.pass_mode[0] = 2u;
         if ((s = hg_clear_dom(ctx)) != HG_OK) return s;
         if ((s = hg_lod(ctx, g, d->dom, HG_SLOT_DOM)) != HG_OK) return s;
         if ((s = hg_scan(ctx, g, d->dom, HG_SLOT_DOM)) != HG_OK) return s;
+        HG_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_gen, 0));
         if ((s = hg_raster(ctx, g, d->dom, HG_SLOT_DOM, nullptr)) != HG_OK) return s;
         if ((s = hg_raster(ctx, g, &layers_params, HG_SLOT_DOM, nullptr)) != HG_OK) return s;
     }
+    if (d->composite && d->clear_color &&
+        (s = hg_clear_color(ctx, cam.pass_mode[2] == 1u ? 0.0f : 1.0f)) != HG_OK)
+        return s;
+    HG_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
+    // main: camera raster, join, shade, filter, composite
+    on(main_stream);
+    if ((s = hg_raster(ctx, g, &cam, HG_SLOT_CAMERA, d->scene_depth)) != HG_OK) return s;
+    HG_CUDA(ctx, cudaStreamWaitEvent(main_stream, ctx->ev_join, 0));
     if ((s = hg_shade(ctx, &cam, &d->shade)) != HG_OK) return s;
     const bool filter = cam.flags[1] != 0u;
     if (filter && (s = hg_filter(ctx, &cam)) != HG_OK) return s;
-    if (d->composite) {
-        if (d->clear_color && (s = hg_clear_color(ctx, cam.pass_mode[2] == 1u ? 0.0f : 1.0f)) != HG_OK) return s;
-        if ((s = hg_composite(ctx, &cam, filter ? 1u : 0u)) != HG_OK) return s;
-    }
+    if (d->composite && (s = hg_composite(ctx, &cam, filter ? 1u : 0u)) != HG_OK) return s;
     return HG_OK;
 }
 

@@ -34,6 +34,19 @@ __device__ __forceinline__ float2 screen_tangent(const hg_hair_params& p, f3 wor
     return make_float2(__fdiv_rn(d.x, l), __fdiv_rn(d.y, l));
 }
 
+// The largest x with sqrt_rn(x) <= r (sqrt_rn is monotone), found from r*r by
+// stepping one ulp at a time (a few steps at most; bounded by 8 each way).
+__device__ __forceinline__ float sqrt_bound(float r) {
+    float x = r * r;
+    for (int k = 0; k < 8 && __fsqrt_rn(x) > r; ++k) x = nextafterf(x, 0.0f);
+    for (int k = 0; k < 8; ++k) {
+        const float up = nextafterf(x, __int_as_float(0x7f800000));
+        if (!(__fsqrt_rn(up) <= r)) break;
+        x = up;
+    }
+    return x;
+}
+
 // One 32x8 tile per CTA.  The 42x18 neighbourhood is staged in shared memory
 // once: per texel the centre word's normalised depth f32(depth)/16777214 (the
 // exact value filter.wgsl:94 computes per tap; -1 marks an empty centre with a
@@ -95,7 +108,8 @@ __global__ void __launch_bounds__(kTileX* kTileY) filter_kernel(const FilterArgs
     const float k_par = 1.4426950408889634f / (sigma_par * sigma_par);
     const float k_perp = 1.4426950408889634f / (sigma_perp * sigma_perp);
     const float k_col = 1.4426950408889634f / (0.9f * 0.9f);
-    const float depth_reject = 1.45e-3f, closer_eps = 5e-4f, strip = 0.5f;
+    const float depth_reject = 1.45e-3f, closer_eps = 5e-4f;
+    const float strip2 = sqrt_bound(0.5f);  // the strip half-width of filter.wgsl:63
     const float p_norm = __fdiv_rn(__uint2float_rn(depth_q), 16777214.0f);
     const bool promote = !center_hit;
     const bool use_color = !promote && cc.w > 0.0f;
@@ -112,9 +126,10 @@ __global__ void __launch_bounds__(kTileX* kTileY) filter_kernel(const FilterArgs
             const float fdx = (float)dx, fdy = (float)dy;
             const float d_par = fdx * ts.x + fdy * ts.y;
             const float ex = fdx - ts.x * d_par, ey = fdy - ts.y * d_par;
-            const float d_perp = __fsqrt_rn(ex * ex + ey * ey);
+            // d_perp = sqrt_rn(e2); d_perp <= 0.5 exactly when e2 <= strip2
+            const float e2 = ex * ex + ey * ey;
             const float nrm = s_norm[ly + dy][lx + dx];
-            if (d_perp <= strip) {
+            if (e2 <= strip2) {
                 if (nrm >= 0.0f) {
                     h_center += 1.0f;
                 } else if (nrm == -1.0f) {
@@ -124,7 +139,7 @@ __global__ void __launch_bounds__(kTileX* kTileY) filter_kernel(const FilterArgs
             if (nrm < 0.0f) continue;
             if (fabsf(nrm - p_norm) > depth_reject) continue;
             const float4 qcol = s_col[ly + dy][lx + dx];
-            float e = d_par * d_par * k_par + d_perp * d_perp * k_perp;
+            float e = d_par * d_par * k_par + e2 * k_perp;
             if (use_color) {
                 const float cx = cc.x - qcol.x, cy = cc.y - qcol.y, cz = cc.z - qcol.z;
                 e += (cx * cx + cy * cy + cz * cz) * k_col;

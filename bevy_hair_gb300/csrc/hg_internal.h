@@ -60,6 +60,9 @@ struct hg_ctx {
     hg_light* lights_host = nullptr;  // kLightSlots * HG_MAX_LIGHTS
     cudaEvent_t light_events[kLightSlots] = {};
     int light_slot = 0;
+    // Side stream and events for the frame's independent DOM half.
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_gen = nullptr, ev_join = nullptr;
     int sm_count = 0;
     std::string last_error;
 };

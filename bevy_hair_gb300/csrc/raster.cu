@@ -952,7 +952,10 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
     const void* fn = mode == 0 ? (const void*)raster_kernel<0>
                      : mode == 1 ? (const void*)raster_kernel<1>
                                  : (const void*)raster_kernel<2>;
-    int blocks = blocks_for(ctx, fn, kRasterThreads, g->ref_capacity, kRasterWarps);
+    // One warp per ref slot, no persistence: raster launches on different
+    // streams then share the SMs through the block scheduler.
+    (void)fn;
+    int blocks = (int)std::max<size_t>((g->ref_capacity + kRasterWarps - 1) / kRasterWarps, 1);
     if (mode == 0) {
         raster_kernel<0><<<blocks, kRasterThreads, 0, ctx->stream>>>(a);
     } else if (mode == 1) {
