@@ -51,7 +51,7 @@ def parse_args():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--config", type=int, default=2)
     ap.add_argument("--scale", type=float, default=1.0)
-    ap.add_argument("--cpu-scale", type=float, default=0.1,
+    ap.add_argument("--cpu-scale", type=float, default=1.0,
                     help="scale of the CPU sample (strand count and pixel count)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
@@ -158,6 +158,27 @@ class Clocks:
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows)}
+
+
+def atomic_peak() -> dict | None:
+    """Measured L2 reduction throughput on this GPU (libhairprobe.so): 64-bit
+    min with the warp-coherent pattern of the DDA, and 32-bit add at random."""
+    import ctypes as C
+
+    from bevy_hair_gb300 import abi
+
+    path = abi.LIB_DIR / "libhairprobe.so"
+    if not path.exists():
+        return None
+    lib = C.CDLL(str(path))
+    lib.hg_probe_atomics.restype = C.c_int
+    lib.hg_probe_atomics.argtypes = [C.c_int, C.c_int, C.c_uint32, C.POINTER(C.c_double)]
+    out = {}
+    for name, op, pattern in [("u64_min_coherent", 0, 1), ("u64_min_random", 0, 0), ("u32_add_random", 2, 0)]:
+        v = C.c_double()
+        if lib.hg_probe_atomics(op, pattern, 1 << 21, C.byref(v)) == 0:
+            out[name] = v.value
+    return out or None
 
 
 def peaks() -> tuple[float, str]:
@@ -283,10 +304,17 @@ def run_ours(args, rank, world, local):
     dominant = max((p for p in nbytes), key=lambda p: acc[p])
     peak, peak_kind = peaks()
     achieved = nbytes[dominant] / (acc[dominant] * 1e-3) / 1e9
+    traffic, traffic_src = None, None
+    try:  # DRAM bytes per launch from the committed ncu capture of this workload
+        tj = json.loads((ROOT / "profiles" / "traffic.json").read_text())
+        traffic, traffic_src = tj["per_launch"][dominant]["dram_bytes"], tj["profile"]
+    except (OSError, KeyError, ValueError):
+        pass
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 2), "peak": peak,
                 "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "traffic": None, "bytes_per_launch": nbytes[dominant],
-                "note": "raster passes are bound by L2 atomics, not HBM: see per_pass and DESIGN.md"}
+                "traffic": traffic, "traffic_source": traffic_src, "bytes_per_launch": nbytes[dominant],
+                "note": "the raster passes are bound by instruction issue and L2 reductions, not HBM "
+                        "(see roofline.atomics)"}
 
     # end to end through the C ABI: host uniforms, frame, colour + depth back to pinned memory
     color_pin = torch.empty(sc.view.width * sc.view.height * 4, dtype=torch.float32, pin_memory=True)
@@ -318,6 +346,22 @@ def run_ours(args, rank, world, local):
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(args, sample=True)
+    # Second ceiling of the raster roofline: the reference algorithm's atomics
+    # (the oracle's count for this frame) at the measured L2 reduction rate.
+    apeak = atomic_peak()
+    if cpu and apeak and "counts_camera" in cpu:
+        c = cpu.pop("counts_camera")
+        ops = c["cons_min"] + c["center_min"] + c["beta_min"]
+        rate = apeak.get("u64_min_coherent")
+        t_bound_ms = ops / rate * 1e3 if rate else None
+        roofline["atomics"] = {
+            "kernel": "raster_camera", "algorithmic_ops": int(ops), "peak_ops_per_s": rate,
+            "peak_source": "measured (libhairprobe: u64 atomicMin, warp-coherent, 16 MB L2-resident buffer)",
+            "t_bound_ms": round(t_bound_ms, 4) if t_bound_ms else None,
+            "frac": round(t_bound_ms / acc["raster_camera"], 4) if t_bound_ms else None,
+            "probe": {k: round(v / 1e9, 2) for k, v in apeak.items()}, "probe_unit": "G ops/s"}
+    elif cpu:
+        cpu.pop("counts_camera", None)
     g.close()
     r.close()
     dist.close()
@@ -369,6 +413,7 @@ def cpu_baseline(args, sample: bool) -> dict:
     dt = time.perf_counter() - t
     segs = int(out["counts_camera"]["segments"])
     return {"value": round(segs / dt / 1e9, 6), "unit": "Gseg/s", "cores": threads, "kind": "port",
+            "counts_camera": out["counts_camera"],
             "sample": (f"one whole frame of config{args.config} at scale {scale}: {sc.mesh.strand_count()} "
                        f"strands, {sc.view.width}x{sc.view.height}, DOM {sc.dom_size[0]}^2, "
                        f"{segs} camera segments, {dt:.2f} s"),

@@ -91,6 +91,17 @@ def build_cuda(verbose_ptxas: bool = False, force: bool = False) -> Path:
     return lib
 
 
+def build_probe(force: bool = False) -> Path:
+    """The benchmark's measurement probes (L2 atomic throughput)."""
+    BUILD_DIR.mkdir(exist_ok=True)
+    LIB_DIR.mkdir(exist_ok=True)
+    src = CSRC / "probe.cu"
+    lib = LIB_DIR / "libhairprobe.so"
+    if force or _stale(lib, [src]):
+        _run([nvcc(), *NVCC_COMMON, "-shared", "-o", str(lib), str(src), "-lcudart"])
+    return lib
+
+
 def build_bake(force: bool = False) -> Path:
     """Compile the host baker."""
     LIB_DIR.mkdir(exist_ok=True)
@@ -104,8 +115,8 @@ def build_bake(force: bool = False) -> Path:
 
 
 def build_all(force: bool = False) -> None:
-    with cf.ThreadPoolExecutor(max_workers=2) as ex:
-        futs = [ex.submit(build_cuda, False, force), ex.submit(build_bake, force)]
+    with cf.ThreadPoolExecutor(max_workers=3) as ex:
+        futs = [ex.submit(build_cuda, False, force), ex.submit(build_bake, force), ex.submit(build_probe, force)]
         for f in futs:
             f.result()
 
