@@ -52,6 +52,10 @@ LIGHT = np.dtype([
 ])
 assert LIGHT.itemsize == 112
 
+SHADOW_LIGHT = np.dtype([("light_clip_from_world", "<f4", 16), ("light_eye", "<f4", 4), ("light_forward", "<f4", 4),
+                         ("depth", "<f4", 4)])
+assert SHADOW_LIGHT.itemsize == 112
+
 LIGHT_POINT, LIGHT_SPOT, LIGHT_DIRECTIONAL, LIGHT_RECT = 0, 1, 2, 3
 LIGHT_CASTS_SHADOWS = 1
 
@@ -130,6 +134,8 @@ _SIGNATURES = {
     "hg_clear_color": (_I32, [_VP, _F32]),
     "hg_groom_frame": (_I32, [_VP, _VP, C.POINTER(FrameDesc)]),
     "hg_scan_noalloc": (_I32, [_VP, _U32, _U32, _VP, _VP, _VP]),
+    "hg_shadow_light_from": (_I32, [_VP, _VP]),
+    "hg_hair_visibility": (_I32, [_VP, _VP, _VP, _U32, _VP]),
 }
 
 _BAKE_SIGNATURES = {

@@ -491,6 +491,34 @@ hg_status hg_clear_color(hg_ctx* ctx, float depth_clear) {
     return HG_OK;
 }
 
+hg_status hg_shadow_light_from(const hg_hair_params* dom, hg_shadow_light* out) {
+    if (!dom || !out) return HG_INVALID_ARG;
+    if (dom->pass_mode[0] != 1u && dom->pass_mode[0] != 2u) return HG_INVALID_ARG;
+    // src/render/pass.rs:574-579: the light clip matrix, eye (w 1), forward
+    // (w 0), and (near, far, DOM_SIGMA, 1); DOM_SIGMA travels in filter_params.w.
+    std::memcpy(out->light_clip_from_world, dom->light_clip_from_world, sizeof(out->light_clip_from_world));
+    for (int i = 0; i < 3; ++i) {
+        out->light_eye[i] = dom->light_eye[i];
+        out->light_forward[i] = dom->light_forward[i];
+    }
+    out->light_eye[3] = 1.0f;
+    out->light_forward[3] = 0.0f;
+    out->depth[0] = dom->dom_info[2];
+    out->depth[1] = dom->dom_info[3];
+    out->depth[2] = dom->filter_params[3];
+    out->depth[3] = 1.0f;
+    return HG_OK;
+}
+
+hg_status hg_hair_visibility(hg_ctx* ctx, const hg_shadow_light* light, const float* points, uint32_t n,
+                             float* visibility) {
+    if (!ctx || !light || (n && (!points || !visibility))) return HG_INVALID_ARG;
+    hg_status s = check_targets(ctx, true);
+    if (s != HG_OK) return s;
+    HG_CUDA(ctx, hg::launch_visibility(ctx, *light, points, n, visibility));
+    return HG_OK;
+}
+
 // hair_pass per-groom body (src/render/pass.rs:375-643).
 hg_status hg_groom_frame(hg_ctx* ctx, hg_groom* g, const hg_frame_desc* d) {
     if (!ctx || !g || !d || !d->camera) return HG_INVALID_ARG;

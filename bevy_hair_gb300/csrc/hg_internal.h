@@ -87,4 +87,7 @@ cudaError_t launch_filter(hg_ctx* ctx, const hg_hair_params& p);
 cudaError_t launch_composite(hg_ctx* ctx, const hg_hair_params& p, uint32_t source_filtered);
 cudaError_t launch_clear_color(hg_ctx* ctx, float depth_clear);
 
+// receiver.cu
+cudaError_t launch_visibility(hg_ctx* ctx, const hg_shadow_light& L, const float* points, uint32_t n, float* out);
+
 }  // namespace hg

@@ -273,6 +273,30 @@ hg_status hg_clear_color(hg_ctx* ctx, float depth_clear);
  * deep opacity map on it also runs hg_generate once before the rasters. */
 hg_status hg_groom_frame(hg_ctx* ctx, hg_groom* groom, const hg_frame_desc* desc);
 
+/* ---------------------------------------------------------------- deep-opacity receivers */
+
+/* ShadowLight (src/render/pass.rs:32-40), 112 bytes: the light view published
+ * with the deep opacity map for other surfaces. depth = (near, far,
+ * extinction per strand fragment, 1 once a map exists). */
+typedef struct hg_shadow_light {
+    float light_clip_from_world[16];
+    float light_eye[4];
+    float light_forward[4];
+    float depth[4];
+} hg_shadow_light;
+
+/* The ShadowLight the reference publishes after the DOM passes
+ * (src/render/pass.rs:574-579), from the DOM params (pass_mode.x == 1). */
+hg_status hg_shadow_light_from(const hg_hair_params* dom_params, hg_shadow_light* out);
+
+/* hair_visibility (src/render/shaders/hair_shadow.wesl:30-75) for n world
+ * points against the context's deep opacity map: the fraction of the key
+ * light that reaches each point through the groom.  points: device float4[n]
+ * (xyz used); visibility: device float[n].  The map's size is the context's
+ * DOM size (the reference fixes 512x512). */
+hg_status hg_hair_visibility(hg_ctx* ctx, const hg_shadow_light* light, const float* points, uint32_t n,
+                             float* visibility);
+
 /* ---------------------------------------------------------------- allocation-free scan */
 
 /* Largest bundle_count hg_scan_noalloc accepts. */
@@ -318,6 +342,7 @@ static_assert(sizeof(hg_gpu_layer) == 32, "GpuLayer is 32 bytes");
 static_assert(sizeof(hg_lod_record) == 16, "LodRecord is 16 bytes");
 static_assert(sizeof(hg_strand_ref) == 16, "StrandRef is 16 bytes");
 static_assert(sizeof(hg_light) == 112, "hg_light is 112 bytes");
+static_assert(sizeof(hg_shadow_light) == 112, "ShadowLight is 112 bytes");
 #else
 _Static_assert(sizeof(hg_hair_params) == 432, "HairParams is 432 bytes (pipeline.rs:12)");
 _Static_assert(sizeof(hg_gpu_bundle) == 16, "GpuBundle is 16 bytes");
@@ -325,6 +350,7 @@ _Static_assert(sizeof(hg_gpu_layer) == 32, "GpuLayer is 32 bytes");
 _Static_assert(sizeof(hg_lod_record) == 16, "LodRecord is 16 bytes");
 _Static_assert(sizeof(hg_strand_ref) == 16, "StrandRef is 16 bytes");
 _Static_assert(sizeof(hg_light) == 112, "hg_light is 112 bytes");
+_Static_assert(sizeof(hg_shadow_light) == 112, "ShadowLight is 112 bytes");
 #endif
 
 #endif /* HAIRGB_H */

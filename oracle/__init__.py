@@ -56,6 +56,7 @@ _SIGS = {
     "oracle_shade": (None, [_VP, _VP, _VP, _VP, _VP, _U32, _U32, _F, _VP, _VP]),
     "oracle_filter": (None, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "oracle_composite": (None, [_VP, _VP, _VP, _VP, _VP]),
+    "oracle_hair_visibility": (None, [_VP, _VP, _U32, _U32, _VP, _U32, _VP]),
 }
 
 
@@ -195,4 +196,13 @@ def frame(mesh, camera, dom_params, lights, exposure=1.0, ortho=False, scene_dep
     depth = np.full(w * h, 0.0 if int(camera["pass_mode"][2]) == 1 else 1.0, dtype=np.float32)
     composite(camera, src, srcd, color, depth)
     out.update(color=color, depth=depth)
+    return out
+
+
+def hair_visibility(light: np.ndarray, dom: np.ndarray, dom_w: int, dom_h: int, points: np.ndarray) -> np.ndarray:
+    """hair_shadow.wesl:52-75 for float4 points against a deep opacity map."""
+    pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 4)
+    out = np.empty(len(pts), dtype=np.float32)
+    lib().oracle_hair_visibility(_p(np.ascontiguousarray(light)), _p(np.ascontiguousarray(dom)), dom_w, dom_h,
+                                 _p(pts), len(pts), _p(out))
     return out

@@ -1213,3 +1213,48 @@ void oracle_composite(const hg_hair_params* p, const float* color_src, const flo
         }
     }
 }
+
+/* ------------------------------------------------------------------ receivers */
+
+/* hair_shadow.wesl:30-50; light = ShadowLight (16 + 4 + 4 + 4 floats). */
+static float receiver_texel(const float* light, const uint32_t* dom, uint32_t dom_w, uint32_t dom_h, int32_t x,
+                            int32_t y, float dist) {
+    if (x < 0 || y < 0 || x >= (int32_t)dom_w || y >= (int32_t)dom_h) return 1.0f;
+    uint32_t pix = (uint32_t)y * dom_w + (uint32_t)x;
+    uint32_t front_q = dom[pix];
+    if (front_q == DOM_EMPTY) return 1.0f;
+    float near_ = light[24], far_ = light[25];
+    float z_front = mixf(near_, far_, (float)front_q / 16777214.0f);
+    float thickness = fmaxf(far_ - near_, 1e-3f) / (float)DOM_LAYERS;
+    float t = fmaxf(dist - z_front, 0.0f) / thickness;
+    const uint32_t* base = dom + (size_t)dom_w * dom_h + (size_t)pix * DOM_LAYERS;
+    float hits = 0.0f;
+    for (uint32_t slice = 0; slice < DOM_LAYERS; ++slice)
+        hits += (float)base[slice] * clampf(t - (float)slice, 0.0f, 1.0f);
+    return expf(-hits * light[26]);
+}
+
+/* hair_shadow.wesl:52-75 for n points (float4, xyz used). */
+void oracle_hair_visibility(const float* light, const uint32_t* dom, uint32_t dom_w, uint32_t dom_h,
+                            const float* points, uint32_t n, float* out) {
+    for (uint32_t i = 0; i < n; ++i) {
+        v3 world = ld3(points + 4 * (size_t)i);
+        out[i] = 1.0f;
+        if (light[27] == 0.0f) continue;
+        v4 clip = mat_mul(light, V4(world.x, world.y, world.z, 1.0f));
+        if (clip.w <= 0.0f) continue;
+        float nx = clip.x / clip.w, ny = clip.y / clip.w;
+        float ux = nx * 0.5f + 0.5f, uy = 1.0f - (ny * 0.5f + 0.5f);
+        if (ux < 0.0f || uy < 0.0f || ux > 1.0f || uy > 1.0f) continue;
+        float dist = dot3(sub3(world, ld3(light + 16)), ld3(light + 20));
+        float fx = ux * (float)dom_w - 0.5f, fy = uy * (float)dom_h - 0.5f;
+        float flx = floorf(fx), fly = floorf(fy);
+        int32_t x0 = f2i(flx), y0 = f2i(fly);
+        float tx = fx - flx, ty = fy - fly;
+        float v00 = receiver_texel(light, dom, dom_w, dom_h, x0, y0, dist);
+        float v10 = receiver_texel(light, dom, dom_w, dom_h, x0 + 1, y0, dist);
+        float v01 = receiver_texel(light, dom, dom_w, dom_h, x0, y0 + 1, dist);
+        float v11 = receiver_texel(light, dom, dom_w, dom_h, x0 + 1, y0 + 1, dist);
+        out[i] = mixf(mixf(v00, v10, tx), mixf(v01, v11, tx), ty);
+    }
+}

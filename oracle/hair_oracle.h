@@ -85,6 +85,9 @@ void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_
                   float* shaded, float* shaded_depth);
 void oracle_filter(const hg_hair_params* p, const uint64_t* center, const uint64_t* cons,
                    const float* shaded, const float* shaded_depth, float* filtered, float* filtered_depth);
+/* hair_shadow.wesl:52-75: light is a ShadowLight (28 floats). */
+void oracle_hair_visibility(const float* light, const uint32_t* dom, uint32_t dom_w, uint32_t dom_h,
+                            const float* points, uint32_t n, float* out);
 void oracle_composite(const hg_hair_params* p, const float* color_src, const float* depth_src,
                       float* color_dst, float* depth_dst);
 

@@ -381,3 +381,35 @@ def test_invalid_arguments_are_rejected(renderer):
         renderer.ensure_targets(0, 10, 0, 0)
     assert renderer.synchronize() == 0
     g.close()
+
+
+def test_hair_visibility_for_receivers(renderer):
+    """The deep-opacity lookup other surfaces use (hair_shadow.wesl:30-75) on
+    the frame's map, against the oracle, for points through the groom."""
+    import ctypes as C
+
+    import torch
+
+    sc = configs.config1(scale=0.05)
+    cam, dom = sc.params()
+    renderer.ensure_targets(sc.view.width, sc.view.height, *sc.dom_size)
+    g = renderer.upload(sc.mesh)
+    renderer.render_groom(g, cam, dom, sc.light_array())
+    light = np.zeros((), dtype=abi.SHADOW_LIGHT)
+    assert renderer.lib.hg_shadow_light_from(dom.ctypes.data, light.ctypes.data) == abi.HG_OK
+    rng = np.random.default_rng(3)
+    lo, hi = sc.mesh.bounds_min - 20, sc.mesh.bounds_max + 20
+    pts = np.concatenate([rng.uniform(lo, hi, size=(4000, 3)), np.ones((4000, 1))], axis=1).astype(np.float32)
+    d_pts = torch.from_numpy(pts).cuda()
+    d_out = torch.empty(len(pts), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    st = renderer.lib.hg_hair_visibility(renderer.ctx, light.ctypes.data, C.c_void_p(d_pts.data_ptr()), len(pts),
+                                         C.c_void_p(d_out.data_ptr()))
+    assert st == abi.HG_OK
+    renderer.synchronize()
+    got = d_out.cpu().numpy()
+    dmap = renderer.read(abi.BUF_DOM)
+    want = oracle.hair_visibility(light.view(np.float32), dmap, *sc.dom_size, pts)
+    np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-6)
+    assert (want < 0.99).sum() > 100 and (want == 1.0).sum() > 100  # shadowed and unshadowed points
+    g.close()

@@ -56,3 +56,18 @@ def test_groom_params_layout():
     assert cam["pass_mode"][2] == 1  # reverse-Z perspective
     lp = host.dom_layers_params(dom)
     assert lp["pass_mode"][0] == 2 and dom["pass_mode"][0] == 1
+
+
+def test_shadow_light_published_from_the_dom_params():
+    """hg_shadow_light_from: the ShadowLight of src/render/pass.rs:574-579."""
+    from bevy_hair_gb300 import abi
+
+    sc = configs.config1(scale=0.01)
+    cam, dom = sc.params()
+    light = np.zeros((), dtype=abi.SHADOW_LIGHT)
+    assert abi.load().hg_shadow_light_from(dom.ctypes.data, light.ctypes.data) == abi.HG_OK
+    assert np.array_equal(light["light_clip_from_world"], dom["light_clip_from_world"])
+    assert light["light_eye"][3] == 1.0 and light["light_forward"][3] == 0.0
+    assert np.array_equal(light["light_eye"][:3], dom["light_eye"][:3])
+    assert light["depth"].tolist() == pytest.approx([dom["dom_info"][2], dom["dom_info"][3], 0.05, 1.0])
+    assert abi.load().hg_shadow_light_from(cam.ctypes.data, light.ctypes.data) == abi.HG_INVALID_ARG
