@@ -19,6 +19,10 @@ STYLE_TEXELS = 1024
 DOM_LAYERS = 16
 MAX_LIGHTS = 256
 SCAN_NOALLOC_MAX_BUNDLES = 65536
+MLP_PARAMS = 14608
+MLP_INPUTS = 10
+MLP_OUTPUTS = 12
+SHADE_KARIS, SHADE_SURROGATE = 0, 1
 
 # --------------------------------------------------------------------- dtypes
 
@@ -136,6 +140,16 @@ _SIGNATURES = {
     "hg_scan_noalloc": (_I32, [_VP, _U32, _U32, _VP, _VP, _VP]),
     "hg_shadow_light_from": (_I32, [_VP, _VP]),
     "hg_hair_visibility": (_I32, [_VP, _VP, _VP, _U32, _VP]),
+    "hg_mlp_create": (_I32, [_VP, C.POINTER(_VP)]),
+    "hg_mlp_destroy": (None, [_VP]),
+    "hg_mlp_set_params": (_I32, [_VP, _VP, _U32]),
+    "hg_mlp_get_params": (_I32, [_VP, _VP, _U32]),
+    "hg_mlp_samples": (_I32, [_VP, C.c_uint64, C.c_uint64, _U32, _F32, _VP, _VP, _VP]),
+    "hg_mlp_infer": (_I32, [_VP, _VP, _U32, _VP, _VP]),
+    "hg_mlp_gradients": (_I32, [_VP, _VP, _VP, _U32, _VP, C.POINTER(_F32)]),
+    "hg_mlp_train_step": (_I32, [_VP, _VP, _VP, _U32, _F32, _VP]),
+    "hg_mlp_bind": (_I32, [_VP, _VP]),
+    "hg_karis_lobes": (_I32, [_VP, _VP, _U32, _F32, _VP]),
 }
 
 _BAKE_SIGNATURES = {

@@ -441,7 +441,9 @@ hg_status hg_shade(hg_ctx* ctx, const hg_hair_params* p, const hg_shade_desc* d)
     if (!ctx || !p || !d) return HG_INVALID_ARG;
     if (d->light_count > HG_MAX_LIGHTS) return fail(ctx, HG_CAPACITY_EXCEEDED, "more than HG_MAX_LIGHTS lights");
     if (d->light_count && !d->lights) return fail(ctx, HG_INVALID_ARG, "null light array");
-    if (d->shade_model != 0u) return fail(ctx, HG_INVALID_ARG, "unknown shade model");
+    if (d->shade_model > 1u) return fail(ctx, HG_INVALID_ARG, "unknown shade model");
+    if (d->shade_model == 1u && !ctx->surrogate)
+        return fail(ctx, HG_NOT_READY, "shade model 1 needs a surrogate bound with hg_mlp_bind");
     hg_status s = check_screen(ctx, p);
     if (s != HG_OK) return s;
     if (p->pass_mode[0] != 0u) return fail(ctx, HG_INVALID_ARG, "shade takes the camera params (pass_mode.x == 0)");

@@ -37,6 +37,22 @@ struct hg_groom {
     float cache_model[16] = {};         // world_from_model the cache was generated with
 };
 
+// Learned shading surrogate (surrogate.cu): FP32 master parameters, Adam
+// state, FP16 forward and transposed copies, training scratch.
+struct hg_mlp {
+    hg_ctx* ctx = nullptr;
+    float* params = nullptr;   // HG_MLP_PARAMS
+    float* grad = nullptr;
+    float* adam_m = nullptr;
+    float* adam_v = nullptr;
+    void* w16 = nullptr;       // __half[HG_MLP_PARAMS], parameter layout
+    void* wt16 = nullptr;      // __half[13312], W2^T W3^T W4^T W5^T
+    float* loss = nullptr;     // device scalar
+    void* scratch = nullptr;   // transposed activations and gradients, (16 + 4*64 + 4*64 + 16) x ld halves
+    uint32_t ld_capacity = 0;
+    uint64_t step = 0;
+};
+
 struct hg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -64,6 +80,7 @@ struct hg_ctx {
     cudaStream_t side = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_gen = nullptr, ev_join = nullptr;
     int sm_count = 0;
+    hg_mlp* surrogate = nullptr;   // bound by hg_mlp_bind, used by shade_model 1
     std::string last_error;
 };
 
@@ -81,6 +98,10 @@ constexpr uint32_t kStrandCacheCps = 65;
 // shade.cu
 cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights, uint32_t ortho, float exposure,
                          uint32_t model);
+cudaError_t launch_karis_lobes(hg_ctx* ctx, const float* inputs, uint32_t n, float tilt, float* lobes);
+
+// surrogate.cu
+cudaError_t launch_mlp_infer(hg_mlp* m, const float* inputs, uint32_t n, float* lobes, float* net);
 
 // filter.cu
 cudaError_t launch_filter(hg_ctx* ctx, const hg_hair_params& p);

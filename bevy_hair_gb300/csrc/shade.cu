@@ -4,8 +4,11 @@
 // file compiles with FMA contraction on.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "hg_device.cuh"
 #include "hg_internal.h"
+#include "hg_mlp.cuh"
 
 namespace hg {
 namespace {
@@ -149,42 +152,58 @@ __device__ Dual dual_scatter(float cos_theta_d, f3 sigma_a, const Shape& shape) 
     return d;
 }
 
-// hair_bsdf (shade.wesl:193-244)
-__device__ f3 hair_bsdf(f3 tangent, f3 view, f3 light, f3 sigma_a, const Shape& shape, const Dual& ds, float depth) {
+// Angles of one light at a fibre (shade.wesl:196-206).
+struct Geometry {
+    float sin_i, sin_o, theta_h, cos_theta_d, cos_phi;
+};
+
+__device__ __forceinline__ Geometry light_geometry(f3 tangent, f3 view, f3 light) {
     f3 t = safe_normalize(tangent);
     f3 v = safe_normalize(view);
     f3 l = safe_normalize(light);
-    float sin_i = clampf(dot3(t, l), -1.0f, 1.0f);
-    float sin_o = clampf(dot3(t, v), -1.0f, 1.0f);
-    float theta_i = asinf(sin_i);
-    float theta_o = asinf(sin_o);
-    float theta_h = theta_i + theta_o;
-    float cos_theta_d = fmaxf(cosf(0.5f * fabsf(theta_i - theta_o)), 1e-3f);
-    f3 t_i = sub3(l, mul3s(t, sin_i));
-    f3 t_o = sub3(v, mul3s(t, sin_o));
+    Geometry g;
+    g.sin_i = clampf(dot3(t, l), -1.0f, 1.0f);
+    g.sin_o = clampf(dot3(t, v), -1.0f, 1.0f);
+    float theta_i = asinf(g.sin_i);
+    float theta_o = asinf(g.sin_o);
+    g.theta_h = theta_i + theta_o;
+    g.cos_theta_d = fmaxf(cosf(0.5f * fabsf(theta_i - theta_o)), 1e-3f);
+    f3 t_i = sub3(l, mul3s(t, g.sin_i));
+    f3 t_o = sub3(v, mul3s(t, g.sin_o));
     float proj = sqrtf(fmaxf(dot3(t_i, t_i) * dot3(t_o, t_o), 1e-8f));
-    float cos_phi = clampf(dot3(t_i, t_o) / proj, -1.0f, 1.0f);
-    Lobes n = azimuthal(cos_theta_d, cos_phi, sigma_a);
+    g.cos_phi = clampf(dot3(t_i, t_o) / proj, -1.0f, 1.0f);
+    return g;
+}
+
+// Forward-scattered spread through `depth` of hair in front of the fibre
+// (shade.wesl:228-242).
+__device__ f3 spread_term(const Shape& shape, const Dual& ds, float theta_h, float depth, float direct) {
     f3 x = spl(theta_h);
+    f3 sigma_f2 = mul3s(ds.beta_f2, depth);
+    f3 transmit = {powf(ds.a_f.x, depth), powf(ds.a_f.y, depth), powf(ds.a_f.z, depth)};
+    f3 beta2 = vmul(shape.beta, shape.beta);
+    f3 g0 = gaussian3(vsqrt(add3(spl(beta2.x), sigma_f2)), sub3(x, spl(shape.alpha.x)));
+    f3 g1 = gaussian3(vsqrt(add3(spl(beta2.y), sigma_f2)), sub3(x, spl(shape.alpha.y)));
+    f3 g2 = gaussian3(vsqrt(add3(spl(beta2.z), sigma_f2)), sub3(x, spl(shape.alpha.z)));
+    f3 spread = add3(add3(vmul(g0, ds.fwd.r), vmul(g1, ds.fwd.tt)), vmul(g2, ds.fwd.trt));
+    f3 gb = gaussian3(vsqrt(add3(ds.sigma_b2, sigma_f2)), sub3(x, ds.delta_b));
+    f3 back_spread = mul3s(vmul(ds.a_back, gb), 2.0f / kPi);
+    f3 inner = add3(mul3s(spread, 1.0f / kPi), mul3s(back_spread, kPi * kDensityBack));
+    return vmul(mul3s(transmit, (1.0f - direct) * kDensityFront), inner);
+}
+
+// hair_bsdf (shade.wesl:193-244)
+__device__ f3 hair_bsdf(f3 tangent, f3 view, f3 light, f3 sigma_a, const Shape& shape, const Dual& ds, float depth) {
+    const Geometry gm = light_geometry(tangent, view, light);
+    Lobes n = azimuthal(gm.cos_theta_d, gm.cos_phi, sigma_a);
+    f3 x = spl(gm.theta_h);
     f3 m = gaussian3(shape.beta, sub3(x, shape.alpha));
     f3 single = add3(add3(mul3s(n.r, m.x), mul3s(n.tt, m.y)), mul3s(n.trt, m.z));
     f3 g = gaussian3(vsqrt(ds.sigma_b2), sub3(x, ds.delta_b));
     f3 back = mul3s(vmul(ds.a_back, g), 2.0f / kPi);
     float direct = expf(-depth);
     f3 color = mul3s(add3(single, mul3s(back, kDensityBack)), direct);
-    if (depth > 1e-3f) {
-        f3 sigma_f2 = mul3s(ds.beta_f2, depth);
-        f3 transmit = {powf(ds.a_f.x, depth), powf(ds.a_f.y, depth), powf(ds.a_f.z, depth)};
-        f3 beta2 = vmul(shape.beta, shape.beta);
-        f3 g0 = gaussian3(vsqrt(add3(spl(beta2.x), sigma_f2)), sub3(x, spl(shape.alpha.x)));
-        f3 g1 = gaussian3(vsqrt(add3(spl(beta2.y), sigma_f2)), sub3(x, spl(shape.alpha.y)));
-        f3 g2 = gaussian3(vsqrt(add3(spl(beta2.z), sigma_f2)), sub3(x, spl(shape.alpha.z)));
-        f3 spread = add3(add3(vmul(g0, ds.fwd.r), vmul(g1, ds.fwd.tt)), vmul(g2, ds.fwd.trt));
-        f3 gb = gaussian3(vsqrt(add3(ds.sigma_b2, sigma_f2)), sub3(x, ds.delta_b));
-        f3 back_spread = mul3s(vmul(ds.a_back, gb), 2.0f / kPi);
-        f3 inner = add3(mul3s(spread, 1.0f / kPi), mul3s(back_spread, kPi * kDensityBack));
-        color = add3(color, vmul(mul3s(transmit, (1.0f - direct) * kDensityFront), inner));
-    }
+    if (depth > 1e-3f) color = add3(color, spread_term(shape, ds, gm.theta_h, depth, direct));
     return color;
 }
 
@@ -345,11 +364,171 @@ __global__ void __launch_bounds__(256, 3) shade_kernel(const ShadeArgs a) {
     a.shaded_depth[pix] = view_dist;
 }
 
+// The learned-surrogate variant of fs: the network gives R, TT, TRT and the
+// local back-scattering per pixel and light (hg_mlp.cuh); the DOM-shadowed
+// light's forward spread keeps the dual-scattering statistics of
+// dual_scatter.  A warp shades 32 pixels of one row and evaluates the
+// network for all of them per light, so every lane takes part in each
+// evaluation; pixels without hair run it on placeholder inputs.  Azimuthal
+// roughness beta_n, which the Karis fit does not have, is the fibre
+// roughness clamped to the trained range [0.2, 0.8].
+constexpr int kSurrogateWarps = 8;
+constexpr size_t kSurrogateSmem = sizeof(mlp::FwdWeights) + kSurrogateWarps * sizeof(mlp::WarpIo);
+
+__global__ void __launch_bounds__(kSurrogateWarps * 32, 1)
+    shade_surrogate_kernel(const ShadeArgs a, const __half* __restrict__ w16, const float* __restrict__ mparams) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    mlp::FwdWeights& w = *reinterpret_cast<mlp::FwdWeights*>(smem);
+    mlp::WarpIo& io = reinterpret_cast<mlp::WarpIo*>(smem + sizeof(mlp::FwdWeights))[threadIdx.x >> 5];
+    mlp::load_fwd(w, w16, mparams, threadIdx.x, blockDim.x);
+    __syncthreads();
+    const hg_hair_params& p = a.p;
+    const uint32_t width = f2u(p.screen[0]), height = f2u(p.screen[1]);
+    const uint32_t tiles_x = (width + 31u) >> 5, tiles = tiles_x * ((height + 7u) >> 3);
+    const uint32_t lane = threadIdx.x & 31u, row = threadIdx.x >> 5;
+    for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+        const uint32_t x = (tile % tiles_x) * 32u + lane, y = (tile / tiles_x) * 8u + row;
+        const bool inside = x < width && y < height;
+        const uint32_t pix = y * width + x;
+        unsigned long long word = 0ull;
+        bool active = false;
+        if (inside) {
+            word = __ldg(&a.center[pix]);
+            active = !is_empty(word);
+            if (!active) {
+                a.shaded[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                a.shaded_depth[pix] = 0.0f;
+            }
+        }
+        if (!__any_sync(0xffffffffu, active)) continue;
+        const uint32_t low = (uint32_t)word, high = (uint32_t)(word >> 32);
+        const float view_dist = dequantize_depth(high >> 8u, p.screen[2], p.screen[3]);
+        const f3 world = reconstruct_world(p, (int32_t)x, (int32_t)y, view_dist);
+        const f3 tangent = oct_decode(high & 0xffu, low >> 24u);
+        const float uvw_z = (float)((low >> 6u) & 0x3fu) / 63.0f;
+        const float beta = inside ? (float)(__ldg(&a.beta[pix]) & 0xffu) / 255.0f : 0.0f;
+        const float roughness = fmaxf(p.appearance[0] * (0.65f + 0.7f * uvw_z), 0.04f);
+        const float ascale = 0.65f + 0.35f * uvw_z;
+        const f3 albedo = {p.albedo[0] * ascale, p.albedo[1] * ascale, p.albedo[2] * ascale};
+        f3 view;
+        if (a.ortho) {
+            view = safe_normalize(mk3(p.clip_from_world[2], p.clip_from_world[6], p.clip_from_world[10]));
+        } else {
+            view = safe_normalize(sub3(ld3(p.camera_pos), world));
+        }
+        const Shape shape = lobe_shape(roughness, p.appearance[1]);
+        const f3 sigma_a = absorption_from_color(albedo, roughness);
+        const float beta_n = clampf(roughness, 0.2f, 0.8f);
+        f3 color = spl(0.0f);
+        bool dom_left = true;
+        for (uint32_t i = 0; i < a.n_lights; ++i) {
+            const hg_light& L = a.lights[i];
+            const uint32_t kind = L.kind;
+            f3 incident = spl(0.0f);
+            float weight = 0.0f, depth = 0.0f;
+            if (kind == HG_LIGHT_POINT || kind == HG_LIGHT_SPOT) {
+                f3 to_l = sub3(ld3(L.position), world);
+                float dist2 = dot3(to_l, to_l);
+                incident = safe_normalize(to_l);
+                float inv_r2 = 1.0f / fmaxf(L.range * L.range, 1e-8f);
+                weight = range_window(dist2, inv_r2) / fmaxf(dist2, 1e-4f);
+                if (kind == HG_LIGHT_SPOT) {
+                    float cd = dot3(mul3s(ld3(L.direction), -1.0f), incident);
+                    float sm = clampf(cd * L.spot[0] + L.spot[1], 0.0f, 1.0f);
+                    weight *= sm * sm;
+                }
+            } else if (kind == HG_LIGHT_DIRECTIONAL) {
+                incident = ld3(L.direction);
+                weight = 1.0f;
+                if (dom_left && (L.flags & HG_LIGHT_CASTS_SHADOWS)) {
+                    if (active) depth = -logf(fmaxf(dom_visibility(p, a.dom, world, beta), 1e-6f));
+                    dom_left = false;
+                }
+            } else if (kind == HG_LIGHT_RECT) {
+                f3 to_c = sub3(ld3(L.position), world);
+                float dist2 = fmaxf(dot3(to_c, to_c), 1e-4f);
+                incident = mul3s(to_c, rsqrtf(dist2));
+                f3 normal = safe_normalize(cross3(ld3(L.up), ld3(L.right)));
+                float facing = fmaxf(dot3(normal, incident), 0.0f);
+                float solid = L.spot[0] * L.spot[1] * facing / dist2;
+                float range2 = fmaxf(L.range * L.range, 1e-4f);
+                weight = solid * range_window(dist2, 1.0f / range2);
+            }
+            const bool use = active && weight > 0.0f;
+            if (!__any_sync(0xffffffffu, use)) continue;
+            const Geometry gm = light_geometry(tangent, view, incident);
+            float raw[10] = {gm.sin_i, gm.sin_o, gm.cos_phi, sqrtf(fmaxf(1.0f - gm.cos_phi * gm.cos_phi, 0.0f)),
+                             sigma_a.x, sigma_a.y, sigma_a.z, shape.beta.x, beta_n, kIor};
+            if (!use) {
+                raw[0] = raw[1] = raw[3] = 0.0f;
+                raw[2] = 1.0f;
+                raw[4] = raw[5] = raw[6] = 0.4f;
+                raw[7] = mlp::kBetaMMid;
+                raw[8] = mlp::kBetaNMid;
+            }
+            float xn[10], yv[12];
+            mlp::normalise(raw, xn);
+            mlp::forward(w, io, xn, yv);
+            if (use) {
+                f3 single = {mlp::decode(yv[0]) + mlp::decode(yv[3]) + mlp::decode(yv[6]),
+                             mlp::decode(yv[1]) + mlp::decode(yv[4]) + mlp::decode(yv[7]),
+                             mlp::decode(yv[2]) + mlp::decode(yv[5]) + mlp::decode(yv[8])};
+                f3 back = {mlp::decode(yv[9]), mlp::decode(yv[10]), mlp::decode(yv[11])};
+                const float direct = expf(-depth);
+                f3 c = mul3s(add3(single, mul3s(back, kDensityBack)), direct);
+                if (depth > 1e-3f) {
+                    const float tv = dot3(tangent, view);
+                    const Dual ds = dual_scatter(sqrtf(fmaxf(1.0f - tv * tv, 1e-6f)), sigma_a, shape);
+                    c = add3(c, spread_term(shape, ds, gm.theta_h, depth, direct));
+                }
+                color = add3(color, mul3s(vmul(c, ld3(L.color)), weight));
+            }
+        }
+        if (active) {
+            color = mul3s(color, a.exposure);
+            a.shaded[pix] = make_float4(color.x, color.y, color.z, 1.0f);
+            a.shaded_depth[pix] = view_dist;
+        }
+    }
+}
+
+// The 12 lobes R, TT, TRT, B of the Karis fit for surrogate-style inputs
+// (sin_i, sin_o, cos_phi, sin_phi, sigma_a rgb, beta_m, beta_n, eta), as
+// hair_bsdf and dual_scatter evaluate them; beta_n and eta do not enter the
+// fit (its IOR is fixed at 1.55).
+__global__ void karis_lobes_kernel(const float* __restrict__ in, uint32_t n, float tilt, float* __restrict__ out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* x = in + (size_t)i * 10;
+    const float sin_i = clampf(x[0], -1.0f, 1.0f), sin_o = clampf(x[1], -1.0f, 1.0f);
+    const float cos_phi = clampf(x[2], -1.0f, 1.0f);
+    const f3 sigma_a = {x[4], x[5], x[6]};
+    const float bm = x[7];
+    const Shape shape = {{tilt, -0.5f * tilt, -1.5f * tilt}, {bm, 0.5f * bm, 2.0f * bm}};
+    const float theta_i = asinf(sin_i), theta_o = asinf(sin_o), theta_h = theta_i + theta_o;
+    const float cos_theta_d = fmaxf(cosf(0.5f * fabsf(theta_i - theta_o)), 1e-3f);
+    const Lobes l = azimuthal(cos_theta_d, cos_phi, sigma_a);
+    const f3 m = gaussian3(shape.beta, sub3(spl(theta_h), shape.alpha));
+    const Dual ds = dual_scatter(sqrtf(fmaxf(1.0f - sin_o * sin_o, 1e-6f)), sigma_a, shape);
+    const f3 g = gaussian3(vsqrt(ds.sigma_b2), sub3(spl(theta_h), ds.delta_b));
+    const f3 b = mul3s(vmul(ds.a_back, g), 2.0f / kPi);
+    const f3 v[4] = {mul3s(l.r, m.x), mul3s(l.tt, m.y), mul3s(l.trt, m.z), b};
+    float* o = out + (size_t)i * 12;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        o[3 * k] = v[k].x;
+        o[3 * k + 1] = v[k].y;
+        o[3 * k + 2] = v[k].z;
+    }
+}
+
+std::mutex g_surrogate_attr_mutex;
+int g_surrogate_per_sm[64] = {};  // resident blocks per SM, 0 until the attribute is set
+
 }  // namespace
 
 cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights, uint32_t ortho, float exposure,
                          uint32_t model) {
-    (void)model;
     ShadeArgs a;
     a.p = p;
     a.center = ctx->center;
@@ -361,9 +540,37 @@ cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights
     a.n_lights = n_lights;
     a.ortho = ortho;
     a.exposure = exposure;
+    if (model == 1u) {
+        int per_sm = 0;
+        {
+            std::lock_guard<std::mutex> lock(g_surrogate_attr_mutex);
+            if (ctx->device < 0 || ctx->device >= 64) return cudaErrorInvalidDevice;
+            if (g_surrogate_per_sm[ctx->device] == 0) {
+                cudaError_t e = cudaFuncSetAttribute(shade_surrogate_kernel,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSurrogateSmem);
+                if (e == cudaSuccess)
+                    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, shade_surrogate_kernel,
+                                                                      kSurrogateWarps * 32, kSurrogateSmem);
+                if (e != cudaSuccess) return e;
+                g_surrogate_per_sm[ctx->device] = per_sm > 0 ? per_sm : 1;
+            }
+            per_sm = g_surrogate_per_sm[ctx->device];
+        }
+        const uint32_t tiles = ((ctx->width + 31u) / 32u) * ((ctx->height + 7u) / 8u);
+        uint32_t blocks = (uint32_t)ctx->sm_count * (uint32_t)per_sm;
+        if (blocks > tiles) blocks = tiles;
+        shade_surrogate_kernel<<<blocks, kSurrogateWarps * 32, kSurrogateSmem, ctx->stream>>>(
+            a, reinterpret_cast<const __half*>(ctx->surrogate->w16), ctx->surrogate->params);
+        return cudaGetLastError();
+    }
     dim3 block(32, 8);
     dim3 grid((ctx->width + 31) / 32, (ctx->height + 7) / 8);
     shade_kernel<<<grid, block, 0, ctx->stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_karis_lobes(hg_ctx* ctx, const float* inputs, uint32_t n, float tilt, float* lobes) {
+    karis_lobes_kernel<<<(n + 255u) / 256u, 256, 0, ctx->stream>>>(inputs, n, tilt, lobes);
     return cudaGetLastError();
 }
 

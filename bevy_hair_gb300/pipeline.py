@@ -169,9 +169,10 @@ class HairRenderer:
         _check(self.lib, self.ctx,
                self.lib.hg_raster(self.ctx, groom.handle, params.ctypes.data, slot, scene_depth_ptr))
 
-    def shade(self, params: np.ndarray, lights: np.ndarray, exposure: float = 1.0, ortho: bool = False) -> None:
+    def shade(self, params: np.ndarray, lights: np.ndarray, exposure: float = 1.0, ortho: bool = False,
+              model: int = abi.SHADE_KARIS) -> None:
         lights = np.ascontiguousarray(lights, dtype=abi.LIGHT)
-        d = abi.ShadeDesc(abi.ptr(lights) if len(lights) else None, len(lights), int(ortho), exposure, 0)
+        d = abi.ShadeDesc(abi.ptr(lights) if len(lights) else None, len(lights), int(ortho), exposure, int(model))
         _check(self.lib, self.ctx, self.lib.hg_shade(self.ctx, params.ctypes.data, C.byref(d)))
 
     def filter(self, params: np.ndarray) -> None:
@@ -185,21 +186,30 @@ class HairRenderer:
 
     def render_groom(self, groom: GpuGroom, camera: np.ndarray, dom: np.ndarray | None, lights: np.ndarray,
                      exposure: float = 1.0, ortho: bool = False, scene_depth_ptr: int | None = None,
-                     composite: bool = True, clear_color: bool = True) -> None:
+                     composite: bool = True, clear_color: bool = True, model: int = abi.SHADE_KARIS) -> None:
         """hg_groom_frame: clear, lod, scan, raster, [DOM], shade, [filter], composite."""
         lights = np.ascontiguousarray(lights, dtype=abi.LIGHT)
         d = abi.FrameDesc()
         d.camera = camera.ctypes.data
         d.dom = dom.ctypes.data if dom is not None else None
         d.scene_depth = scene_depth_ptr
-        d.shade = abi.ShadeDesc(abi.ptr(lights) if len(lights) else None, len(lights), int(ortho), exposure, 0)
+        d.shade = abi.ShadeDesc(abi.ptr(lights) if len(lights) else None, len(lights), int(ortho), exposure,
+                                int(model))
         d.composite = int(composite)
         d.clear_color = int(clear_color)
         self._frame_keepalive = (lights, camera, dom)
         _check(self.lib, self.ctx, self.lib.hg_groom_frame(self.ctx, groom.handle, C.byref(d)))
 
+    def bind_surrogate(self, surrogate) -> None:
+        """Make `surrogate` (a bevy_hair_gb300.surrogate.Surrogate, or None) the
+        network that shade model 1 evaluates."""
+        handle = surrogate.handle if surrogate is not None else None
+        _check(self.lib, self.ctx, self.lib.hg_mlp_bind(self.ctx, handle))
+
     def close(self) -> None:
         if self.ctx:
+            for s in list(getattr(self, "_surrogates", ())):
+                s.close()
             self.lib.hg_destroy(self.ctx)
             self.ctx = None
 

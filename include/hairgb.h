@@ -331,6 +331,59 @@ hg_status hg_hair_visibility(hg_ctx* ctx, const hg_shadow_light* light, const fl
 hg_status hg_scan_noalloc(const hg_lod_record* lod, uint32_t bundle_count, uint32_t capacity,
                           hg_strand_ref* refs, uint32_t* indirect, void* stream);
 
+/* ---------------------------------------------------------------- learned shading surrogate */
+
+/* A small network that stands in for the Karis-fit lobes of shade.wesl:94-190
+ * (no counterpart in the reference).  Inputs (10): sin theta_i, sin theta_o,
+ * cos phi, sin phi, sigma_a (rgb), beta_m, beta_n, eta.  Outputs (12): the
+ * lobes R, TT, TRT and the local back-scattering B, rgb each.  Architecture
+ * 10 -> 64 -> 64 -> 64 -> 64 -> 12, ReLU, FP16 weights and activations with
+ * FP32 accumulation; the network predicts log1p(lobe / 1e-3).  Parameters
+ * are HG_MLP_PARAMS floats: W1[64][16] b1[64] W2[64][64] b2[64] W3[64][64]
+ * b3[64] W4[64][64] b4[64] W5[16][64] b5[16] (W[out][in]; the padding
+ * columns 10..15 of W1 and rows 12..15 of W5 and b5 stay zero).  A surrogate
+ * works on its context's stream; destroy it before the context. */
+#define HG_MLP_PARAMS 14608u
+#define HG_MLP_INPUTS 10u
+#define HG_MLP_OUTPUTS 12u
+
+typedef struct hg_mlp hg_mlp;
+
+hg_status hg_mlp_create(hg_ctx* ctx, hg_mlp** out);   /* parameters start at zero */
+void hg_mlp_destroy(hg_mlp* mlp);
+/* Host float[count], count == HG_MLP_PARAMS; resets the optimiser state. */
+hg_status hg_mlp_set_params(hg_mlp* mlp, const float* params, uint32_t count);
+hg_status hg_mlp_get_params(hg_mlp* mlp, float* params, uint32_t count);
+/* Training samples with FP64 lobes (Gauss-Legendre integration of the
+ * Marschner/d'Eon azimuthal scattering, Zinke back-scattering) at the
+ * longitudinal tilt `tilt`.  Sample k is a pure function of (seed, first + k).
+ * Device buffers: inputs float[count][10]; targets float[count][12] =
+ * log1p(lobe / 1e-3) (nullable); lobes double[count][12] (nullable). */
+hg_status hg_mlp_samples(hg_ctx* ctx, uint64_t seed, uint64_t first, uint32_t count, float tilt, float* inputs,
+                         float* targets, double* lobes);
+/* Network evaluation.  Device buffers: inputs float[count][10]; lobes
+ * float[count][12] (decoded, nullable); net float[count][12] (raw outputs,
+ * nullable). */
+hg_status hg_mlp_infer(hg_mlp* mlp, const float* inputs, uint32_t count, float* lobes, float* net);
+/* Gradient of the sum over samples and outputs of (net - target)^2 for one
+ * batch (device inputs/targets), into host float[HG_MLP_PARAMS]; the loss sum
+ * into *loss (nullable).  Parameters are unchanged. */
+hg_status hg_mlp_gradients(hg_mlp* mlp, const float* inputs, const float* targets, uint32_t count, float* grad,
+                           float* loss);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the mean squared error
+ * of one batch (device inputs/targets).  loss_sum: nullable device float that
+ * receives the batch's sum of squared errors.  Asynchronous on the stream. */
+hg_status hg_mlp_train_step(hg_mlp* mlp, const float* inputs, const float* targets, uint32_t count, float lr,
+                            float* loss_sum);
+/* The same 12 lobes from the Karis fits of shade.wesl:94-190 in FP32, as
+ * shade model 0 evaluates them, for comparing the two models on one set of
+ * inputs (device float[count][10] -> device float[count][12]; beta_n and eta
+ * do not enter the fit). */
+hg_status hg_karis_lobes(hg_ctx* ctx, const float* inputs, uint32_t count, float tilt, float* lobes);
+/* Bind (or, with NULL, unbind) the surrogate that hg_shade_desc.shade_model 1
+ * uses on this context. */
+hg_status hg_mlp_bind(hg_ctx* ctx, hg_mlp* mlp);
+
 #ifdef __cplusplus
 } /* extern "C" */
 #endif

@@ -53,15 +53,17 @@ _SIGS = {
     "oracle_scan": (None, [_VP, _VP, _VP, _U32, _VP]),
     "oracle_strand_points": (_U32, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "oracle_raster": (None, [_VP, _VP, _VP, _VP, _VP, _U32, _VP, _VP, _VP, _VP, _VP, C.POINTER(Counts)]),
-    "oracle_shade": (None, [_VP, _VP, _VP, _VP, _VP, _U32, _U32, _F, _VP, _VP]),
+    "oracle_shade": (None, [_VP, _VP, _VP, _VP, _VP, _U32, _U32, _F, _VP, _VP, _VP]),
+    "oracle_mlp_forward": (None, [_VP, _VP, _U32, _VP]),
     "oracle_filter": (None, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "oracle_composite": (None, [_VP, _VP, _VP, _VP, _VP]),
     "oracle_hair_visibility": (None, [_VP, _VP, _U32, _U32, _VP, _U32, _VP]),
+    "oracle_lobes_batch": (None, [_I, _VP, _U32, C.c_double, _VP]),
 }
 
 
 def build() -> Path:
-    src = [HERE / "hair_oracle.c", HERE / "hair_oracle.h", HERE.parent / "include" / "hairgb.h"]
+    src = [HERE / "hair_oracle.c", HERE / "marschner.c", HERE / "hair_oracle.h", HERE.parent / "include" / "hairgb.h"]
     if not SO.exists() or any(s.stat().st_mtime > SO.stat().st_mtime for s in src):
         res = subprocess.run(["make", "-C", str(HERE)], capture_output=True, text=True)
         if res.returncode != 0:
@@ -138,15 +140,26 @@ def raster(params, mesh, refs, total, center, cons, beta, dom, scene_depth=None)
     return counts.as_dict()
 
 
-def shade(params, center, beta, dom, lights, exposure=1.0, ortho=False):
+def shade(params, center, beta, dom, lights, exposure=1.0, ortho=False, mlp=None):
+    """Shade model 0 (Karis fit), or model 1 when `mlp` holds the surrogate's parameters."""
     w, h = int(params["screen"][0]), int(params["screen"][1])
     shaded = np.empty(w * h * 4, dtype=np.float32)
     sdepth = np.empty(w * h, dtype=np.float32)
     lights = np.ascontiguousarray(lights, dtype=abi.LIGHT)
     dom_arr = dom if dom is not None else np.zeros(16, dtype=np.uint32)
+    mlp_arr = None if mlp is None else np.ascontiguousarray(mlp, dtype=np.float32)
     lib().oracle_shade(_p(params), _p(center), _p(beta), _p(dom_arr), _p(lights) if len(lights) else None,
-                       len(lights), int(ortho), float(exposure), _p(shaded), _p(sdepth))
+                       len(lights), int(ortho), float(exposure), _p(mlp_arr), _p(shaded), _p(sdepth))
     return shaded, sdepth
+
+
+def mlp_forward(params: np.ndarray, raw: np.ndarray) -> np.ndarray:
+    """The surrogate network on raw inputs (n, 10) -> raw outputs (n, 12), FP16 rounding emulated."""
+    p = np.ascontiguousarray(params, dtype=np.float32)
+    x = np.ascontiguousarray(raw, dtype=np.float32).reshape(-1, 10)
+    out = np.empty((len(x), 12), dtype=np.float32)
+    lib().oracle_mlp_forward(_p(p), _p(x), len(x), _p(out))
+    return out
 
 
 def filter_(params, center, cons, shaded, shaded_depth):
@@ -163,7 +176,7 @@ def composite(params, color_src, depth_src, color_dst, depth_dst) -> None:
                            _p(np.ascontiguousarray(depth_src, dtype=np.float32)), _p(color_dst), _p(depth_dst))
 
 
-def frame(mesh, camera, dom_params, lights, exposure=1.0, ortho=False, scene_depth=None) -> dict:
+def frame(mesh, camera, dom_params, lights, exposure=1.0, ortho=False, scene_depth=None, mlp=None) -> dict:
     """The per-groom sequence of hair_pass (src/render/pass.rs:375-643) on the CPU."""
     w, h = int(camera["screen"][0]), int(camera["screen"][1])
     out: dict = {}
@@ -184,7 +197,7 @@ def frame(mesh, camera, dom_params, lights, exposure=1.0, ortho=False, scene_dep
         layers = dom_params.copy()
         layers["pass_mode"][0] = 2
         out["counts_dom_layers"] = raster(layers, mesh, refs_d, total_d, center, cons, beta, dom)
-    shaded, sdepth = shade(camera, center, beta, dom, lights, exposure, ortho)
+    shaded, sdepth = shade(camera, center, beta, dom, lights, exposure, ortho, mlp)
     out.update(center=center, cons=cons, beta=beta, dom=dom, shaded=shaded, shaded_depth=sdepth)
     if int(camera["flags"][1]):
         filt, fdepth = filter_(camera, center, cons, shaded, sdepth)
@@ -205,4 +218,14 @@ def hair_visibility(light: np.ndarray, dom: np.ndarray, dom_w: int, dom_h: int, 
     out = np.empty(len(pts), dtype=np.float32)
     lib().oracle_hair_visibility(_p(np.ascontiguousarray(light)), _p(np.ascontiguousarray(dom)), dom_w, dom_h,
                                  _p(pts), len(pts), _p(out))
+    return out
+
+
+def lobes(inputs: np.ndarray, model: str = "marschner", tilt: float = 0.08) -> np.ndarray:
+    """FP64 hair lobes for inputs (n, 10): sin_i, sin_o, cos_phi, sin_phi, sigma_a rgb,
+    beta_m, beta_n, eta.  Returns (n, 12): R, TT, TRT, B (rgb each).  model
+    "marschner": exact azimuthal integrals (the judge); "karis": shade.wesl's fits."""
+    x = np.ascontiguousarray(inputs, dtype=np.float64).reshape(-1, 10)
+    out = np.empty((len(x), 12), dtype=np.float64)
+    lib().oracle_lobes_batch(0 if model == "marschner" else 1, _p(x), len(x), float(tilt), _p(out))
     return out

@@ -876,6 +876,22 @@ static dual_t dual_scatter(float cos_theta_d, v3 sigma_a, shape_t shape) {
     return d;
 }
 
+/* shade.wesl:228-242: forward-scattered spread through `depth` of hair. */
+static v3 spread_term(shape_t shape, const dual_t* ds, float theta_h, float depth, float direct) {
+    v3 sigma_f2 = mul3s(ds->beta_f2, depth);
+    v3 transmit = V3(powf(ds->a_f.x, depth), powf(ds->a_f.y, depth), powf(ds->a_f.z, depth));
+    v3 beta2 = mul3(shape.beta, shape.beta);
+    v3 x = spl3(theta_h);
+    v3 g0 = gaussian3(vsqrt(add3(spl3(beta2.x), sigma_f2)), sub3(x, spl3(shape.alpha.x)));
+    v3 g1 = gaussian3(vsqrt(add3(spl3(beta2.y), sigma_f2)), sub3(x, spl3(shape.alpha.y)));
+    v3 g2 = gaussian3(vsqrt(add3(spl3(beta2.z), sigma_f2)), sub3(x, spl3(shape.alpha.z)));
+    v3 spread = add3(add3(mul3(g0, ds->fwd.r), mul3(g1, ds->fwd.tt)), mul3(g2, ds->fwd.trt));
+    v3 gb = gaussian3(vsqrt(add3(ds->sigma_b2, sigma_f2)), sub3(x, ds->delta_b));
+    v3 back_spread = div3s(mul3(mul3s(ds->a_back, 2.0f), gb), PI_F);
+    v3 inner = add3(div3s(spread, PI_F), mul3s(back_spread, PI_F * DENSITY_BACK));
+    return mul3(mul3s(transmit, (1.0f - direct)), mul3s(inner, DENSITY_FRONT));
+}
+
 /* shade.wesl:193-244 */
 static v3 hair_bsdf(v3 tangent, v3 view, v3 light, v3 sigma_a, shape_t shape, const dual_t* ds, float shadow,
                     float depth) {
@@ -900,22 +916,113 @@ static v3 hair_bsdf(v3 tangent, v3 view, v3 light, v3 sigma_a, shape_t shape, co
     v3 back = div3s(mul3(mul3s(ds->a_back, 2.0f), g), PI_F);
     float direct = expf(-depth);
     v3 color = mul3s(add3(single, mul3s(back, DENSITY_BACK)), direct);
-    if (depth > 1e-3f) {
-        v3 sigma_f2 = mul3s(ds->beta_f2, depth);
-        v3 transmit = V3(powf(ds->a_f.x, depth), powf(ds->a_f.y, depth), powf(ds->a_f.z, depth));
-        v3 beta2 = mul3(shape.beta, shape.beta);
-        v3 x = spl3(theta_h);
-        v3 g0 = gaussian3(vsqrt(add3(spl3(beta2.x), sigma_f2)), sub3(x, spl3(shape.alpha.x)));
-        v3 g1 = gaussian3(vsqrt(add3(spl3(beta2.y), sigma_f2)), sub3(x, spl3(shape.alpha.y)));
-        v3 g2 = gaussian3(vsqrt(add3(spl3(beta2.z), sigma_f2)), sub3(x, spl3(shape.alpha.z)));
-        v3 spread = add3(add3(mul3(g0, ds->fwd.r), mul3(g1, ds->fwd.tt)), mul3(g2, ds->fwd.trt));
-        v3 gb = gaussian3(vsqrt(add3(ds->sigma_b2, sigma_f2)), sub3(x, ds->delta_b));
-        v3 back_spread = div3s(mul3(mul3s(ds->a_back, 2.0f), gb), PI_F);
-        v3 inner = add3(div3s(spread, PI_F), mul3s(back_spread, PI_F * DENSITY_BACK));
-        v3 add = mul3(mul3s(transmit, (1.0f - direct)), mul3s(inner, DENSITY_FRONT));
-        color = add3(color, add);
-    }
+    if (depth > 1e-3f) color = add3(color, spread_term(shape, ds, theta_h, depth, direct));
     return mul3s(color, shadow);
+}
+
+/* ------------------------------------------------- learned surrogate
+ * The shade pass's network (hg_mlp.cuh) in FP32 with its FP16 rounding of
+ * weights and activations: 10 -> 64 -> 64 -> 64 -> 64 -> 12, ReLU,
+ * parameters W1[64][16] b1 W2[64][64] b2 W3 b3 W4 b4 W5[16][64] b5.  The
+ * tensor cores sum the products in their own order, so single activations can
+ * land one FP16 step apart; comparisons use a tolerance. */
+
+/* Round to the nearest IEEE binary16 value (ties to even), returned as float. */
+static float round_half(float f) {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    uint32_t sign = u & 0x80000000u, a = u & 0x7fffffffu;
+    if (a >= 0x7f800000u) return f;
+    float af;
+    memcpy(&af, &a, 4);
+    float r;
+    if (af >= 65520.0f) {
+        r = INFINITY;
+    } else if (af < 6.103515625e-05f) {          /* below the smallest normal half: steps of 2^-24 */
+        const float q = 5.9604644775390625e-08f;
+        r = nearbyintf(af / q) * q;
+    } else {
+        uint32_t lsb = (a >> 13) & 1u;
+        a = (a + 0x0fffu + lsb) & ~0x1fffu;
+        memcpy(&r, &a, 4);
+    }
+    uint32_t ru;
+    memcpy(&ru, &r, 4);
+    ru |= sign;
+    memcpy(&r, &ru, 4);
+    return r;
+}
+
+static void mlp_layer(const float* w, const float* b, const float* in, int n_in, int n_out, int relu, float* out) {
+    for (int j = 0; j < n_out; ++j) {
+        float acc = b[j];
+        for (int k = 0; k < n_in; ++k) acc += round_half(w[j * n_in + k]) * in[k];
+        out[j] = relu ? round_half(fmaxf(acc, 0.0f)) : acc;
+    }
+}
+
+void oracle_mlp_forward(const float* params, const float* raw, uint32_t n, float* net) {
+    for (uint32_t s = 0; s < n; ++s) {
+        const float* r = raw + 10 * (size_t)s;
+        float x[16] = {0}, h0[64], h1[64], y[16];
+        x[0] = r[0];
+        x[1] = r[1];
+        x[2] = r[2];
+        x[3] = r[3];
+        for (int c = 0; c < 3; ++c) x[4 + c] = (logf(fmaxf(r[4 + c], 1e-6f)) - (-0.91629073f)) * 0.33380820f;
+        x[7] = (r[7] - 0.165f) * 7.4074074f;
+        x[8] = (r[8] - 0.5f) * 3.3333333f;
+        x[9] = (r[9] - 1.55f) * 10.0f;
+        for (int k = 0; k < 16; ++k) x[k] = round_half(x[k]);
+        const float* p = params;
+        mlp_layer(p, p + 1024, x, 16, 64, 1, h0);
+        p += 1024 + 64;
+        mlp_layer(p, p + 4096, h0, 64, 64, 1, h1);
+        p += 4096 + 64;
+        mlp_layer(p, p + 4096, h1, 64, 64, 1, h0);
+        p += 4096 + 64;
+        mlp_layer(p, p + 4096, h0, 64, 64, 1, h1);
+        p += 4096 + 64;
+        mlp_layer(p, p + 1024, h1, 64, 16, 0, y);
+        for (int c = 0; c < 12; ++c) net[12 * (size_t)s + c] = y[c];
+    }
+}
+
+static inline float mlp_decode(float y) { return 1e-3f * expm1f(fmaxf(y, 0.0f)); }
+
+/* Shade model 1: the network's R, TT, TRT and back-scattering per light; the
+ * shadowed forward spread keeps dual_scatter's statistics.  beta_n is the
+ * fibre roughness clamped to [0.2, 0.8]. */
+static v3 surrogate_bsdf(const float* mlp, v3 tangent, v3 view, v3 light, v3 sigma_a, shape_t shape,
+                         const dual_t* ds, float depth, float roughness) {
+    v3 t = safe_normalize(tangent);
+    v3 v = safe_normalize(view);
+    v3 l = safe_normalize(light);
+    float sin_i = clampf(dot3(t, l), -1.0f, 1.0f);
+    float sin_o = clampf(dot3(t, v), -1.0f, 1.0f);
+    float theta_h = asinf(sin_i) + asinf(sin_o);
+    v3 t_i = sub3(l, mul3s(t, sin_i));
+    v3 t_o = sub3(v, mul3s(t, sin_o));
+    float proj = sqrtf(fmaxf(dot3(t_i, t_i) * dot3(t_o, t_o), 1e-8f));
+    float cos_phi = clampf(dot3(t_i, t_o) / proj, -1.0f, 1.0f);
+    float raw[10] = {sin_i, sin_o, cos_phi, sqrtf(fmaxf(1.0f - cos_phi * cos_phi, 0.0f)), sigma_a.x, sigma_a.y,
+                     sigma_a.z, shape.beta.x, clampf(roughness, 0.2f, 0.8f), IOR};
+    float y[12];
+    oracle_mlp_forward(mlp, raw, 1, y);
+    v3 single = V3(mlp_decode(y[0]) + mlp_decode(y[3]) + mlp_decode(y[6]),
+                   mlp_decode(y[1]) + mlp_decode(y[4]) + mlp_decode(y[7]),
+                   mlp_decode(y[2]) + mlp_decode(y[5]) + mlp_decode(y[8]));
+    v3 back = V3(mlp_decode(y[9]), mlp_decode(y[10]), mlp_decode(y[11]));
+    float direct = expf(-depth);
+    v3 color = mul3s(add3(single, mul3s(back, DENSITY_BACK)), direct);
+    if (depth > 1e-3f) color = add3(color, spread_term(shape, ds, theta_h, depth, direct));
+    return color;
+}
+
+static v3 light_lobe(const float* mlp, v3 tangent, v3 view, v3 incident, v3 sigma_a, shape_t shape, const dual_t* ds,
+                     float depth, float roughness) {
+    if (mlp) return surrogate_bsdf(mlp, tangent, view, incident, sigma_a, shape, ds, depth, roughness);
+    return hair_bsdf(tangent, view, incident, sigma_a, shape, ds, 1.0f, depth);
 }
 
 /* shade.wesl:262-277 */
@@ -981,7 +1088,8 @@ static inline float spot_mask(const hg_light* L, v3 world) {
 
 /* shade.wesl:429-521: point, spot, directional then rect lights. */
 static v3 direct_light(const hg_hair_params* p, const uint32_t* dom, const hg_light* lights, uint32_t n_lights,
-                       v3 world, v3 tangent, v3 view, v3 albedo, float roughness, float tilt, float beta) {
+                       v3 world, v3 tangent, v3 view, v3 albedo, float roughness, float tilt, float beta,
+                       const float* mlp) {
     shape_t shape = lobe_shape(roughness, tilt);
     float tv = dot3(tangent, view);
     float cos_theta_o = sqrtf(fmaxf(1.0f - tv * tv, 1e-6f));
@@ -999,7 +1107,7 @@ static v3 direct_light(const hg_hair_params* p, const uint32_t* dom, const hg_li
                 v3 incident = safe_normalize(light_to_frag);
                 float inv_r2 = 1.0f / fmaxf(L->range * L->range, 1e-8f);
                 float att = distance_attenuation(dist2, inv_r2);
-                v3 lobe = hair_bsdf(tangent, view, incident, sigma_a, shape, &ds, 1.0f, 0.0f);
+                v3 lobe = light_lobe(mlp, tangent, view, incident, sigma_a, shape, &ds, 0.0f, roughness);
                 v3 c = mul3s(mul3(lobe, ld3(L->color)), att);
                 if (kind == HG_LIGHT_SPOT) c = mul3s(c, spot_mask(L, world));
                 color = add3(color, c);
@@ -1011,7 +1119,7 @@ static v3 direct_light(const hg_hair_params* p, const uint32_t* dom, const hg_li
                     depth = -logf(fmaxf(dom_visibility(p, dom, world, beta), 1e-6f));
                     dom_left = 0;
                 }
-                v3 lobe = hair_bsdf(tangent, view, incident, sigma_a, shape, &ds, 1.0f, depth);
+                v3 lobe = light_lobe(mlp, tangent, view, incident, sigma_a, shape, &ds, depth, roughness);
                 color = add3(color, mul3(lobe, ld3(L->color)));
             } else {
                 v3 to_center = sub3(ld3(L->position), world);
@@ -1022,7 +1130,7 @@ static v3 direct_light(const hg_hair_params* p, const uint32_t* dom, const hg_li
                 float solid = L->spot[0] * L->spot[1] * facing / dist2;
                 float range2 = fmaxf(L->range * L->range, 1e-4f);
                 float falloff = range_falloff(dist2, 1.0f / range2);
-                v3 lobe = hair_bsdf(tangent, view, incident, sigma_a, shape, &ds, 1.0f, 0.0f);
+                v3 lobe = light_lobe(mlp, tangent, view, incident, sigma_a, shape, &ds, 0.0f, roughness);
                 color = add3(color, mul3s(mul3s(mul3(lobe, ld3(L->color)), solid), falloff));
             }
         }
@@ -1033,8 +1141,8 @@ static v3 direct_light(const hg_hair_params* p, const uint32_t* dom, const hg_li
 /* shade.wesl:523-593 without the environment probe (probe_radiance is zero
  * in the specialization without ENVIRONMENT_MAP, shade.wesl:384-394). */
 void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_t* beta_buf, const uint32_t* dom,
-                  const hg_light* lights, uint32_t n_lights, uint32_t ortho, float exposure, float* shaded,
-                  float* shaded_depth) {
+                  const hg_light* lights, uint32_t n_lights, uint32_t ortho, float exposure, const float* mlp,
+                  float* shaded, float* shaded_depth) {
     uint32_t width = f2u(p->screen[0]), height = f2u(p->screen[1]);
     int nthreads = oracle_get_threads();
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads)
@@ -1066,7 +1174,7 @@ void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_
         } else {
             view = safe_normalize(sub3(ld3(p->camera_pos), world));
         }
-        v3 color = direct_light(p, dom, lights, n_lights, world, tangent, view, albedo, roughness, tilt, beta);
+        v3 color = direct_light(p, dom, lights, n_lights, world, tangent, view, albedo, roughness, tilt, beta, mlp);
         color = mul3s(color, exposure);
         shaded[4 * pix + 0] = color.x;
         shaded[4 * pix + 1] = color.y;

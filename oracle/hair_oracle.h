@@ -80,14 +80,24 @@ void oracle_raster(const hg_hair_params* p, const hg_gpu_bundle* bundles, const 
                    const float* style, const hg_strand_ref* refs, uint32_t n_refs,
                    uint64_t* center, uint64_t* cons, uint32_t* beta, uint32_t* dom,
                    const float* scene_depth, oracle_counts* counts);
+/* mlp: NULL for shade model 0 (Karis fit); the surrogate's HG_MLP_PARAMS
+ * floats for shade model 1. */
 void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_t* beta, const uint32_t* dom,
-                  const hg_light* lights, uint32_t n_lights, uint32_t ortho, float exposure,
+                  const hg_light* lights, uint32_t n_lights, uint32_t ortho, float exposure, const float* mlp,
                   float* shaded, float* shaded_depth);
+/* The surrogate network on raw inputs (n x 10) -> raw outputs (n x 12). */
+void oracle_mlp_forward(const float* params, const float* raw, uint32_t n, float* net);
 void oracle_filter(const hg_hair_params* p, const uint64_t* center, const uint64_t* cons,
                    const float* shaded, const float* shaded_depth, float* filtered, float* filtered_depth);
 /* hair_shadow.wesl:52-75: light is a ShadowLight (28 floats). */
 void oracle_hair_visibility(const float* light, const uint32_t* dom, uint32_t dom_w, uint32_t dom_h,
                             const float* points, uint32_t n, float* out);
+/* FP64 hair lobes (marschner.c): in[10] = sin_i, sin_o, cos_phi, sin_phi,
+ * sigma_a rgb, beta_m, beta_n, eta -> out[12] = R, TT, TRT, B (rgb each).
+ * oracle_lobes_batch model 0: exact azimuthal integrals; 1: shade.wesl's Karis fits. */
+void oracle_marschner_lobes(const double in[10], double tilt, double out[12]);
+void oracle_karis_lobes(const double in[10], double tilt, double out[12]);
+void oracle_lobes_batch(int model, const double* in, unsigned n, double tilt, double* out);
 void oracle_composite(const hg_hair_params* p, const float* color_src, const float* depth_src,
                       float* color_dst, float* depth_dst);
 

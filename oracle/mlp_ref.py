@@ -1,0 +1,85 @@
+"""FP64 reference of the shading surrogate's network.  TEST INFRASTRUCTURE ONLY.
+
+Forward and backward passes of the 10 -> 4 x 64 -> 12 ReLU network that
+libhairgb.so trains and evaluates on the tensor cores (bevy_hair_gb300/csrc/
+hg_mlp.cuh, surrogate.cu).  With ``half=True`` the weights, the normalised
+inputs and the post-ReLU activations are rounded to FP16 exactly where the
+kernels round them, and everything else is FP64; the gradients are not
+rounded (the kernels round the backward pass's fragments to FP16, so the
+comparison uses a tolerance).  With ``half=False`` the network is smooth FP64
+for finite-difference checks of the analytic gradient.
+
+Loss: sum over samples and the 12 outputs of (y - target)^2.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+LAYERS = ((64, 16), (64, 64), (64, 64), (64, 64), (16, 64))
+N_PARAMS = 14608
+N_OUT = 12
+
+
+def split(params: np.ndarray):
+    out, o = [], 0
+    for rows, cols in LAYERS:
+        w = params[o:o + rows * cols].reshape(rows, cols)
+        o += rows * cols
+        b = params[o:o + rows]
+        o += rows
+        out.append((w, b))
+    assert o == N_PARAMS
+    return out
+
+
+def _h(a: np.ndarray, half: bool) -> np.ndarray:
+    return a.astype(np.float16).astype(np.float64) if half else np.asarray(a, dtype=np.float64)
+
+
+def normalise(raw: np.ndarray) -> np.ndarray:
+    """hg_mlp.cuh normalise(): (n, 10) raw inputs -> (n, 16) network inputs (FP32 like the kernel)."""
+    r = np.asarray(raw, dtype=np.float32).reshape(-1, 10)
+    x = np.zeros((len(r), 16), dtype=np.float32)
+    x[:, 0:4] = r[:, 0:4]
+    x[:, 4:7] = (np.log(np.maximum(r[:, 4:7], np.float32(1e-6))) - np.float32(-0.91629073)) * np.float32(0.33380820)
+    x[:, 7] = (r[:, 7] - np.float32(0.165)) * np.float32(7.4074074)
+    x[:, 8] = (r[:, 8] - np.float32(0.5)) * np.float32(3.3333333)
+    x[:, 9] = (r[:, 9] - np.float32(1.55)) * np.float32(10.0)
+    return x
+
+
+def forward(params: np.ndarray, raw: np.ndarray, half: bool = True):
+    """Network outputs (n, 16; columns 12..15 are padding) and the activations."""
+    # The kernels round the FP32 master weights to FP16; the smooth network keeps FP64.
+    base = np.asarray(params, np.float32) if half else np.asarray(params, np.float64)
+    layers = [(_h(w, half), np.asarray(b, dtype=np.float64)) for w, b in split(base)]
+    x = _h(normalise(raw), half)
+    acts = [x]
+    h = x
+    for k, (w, b) in enumerate(layers):
+        z = h @ w.T + b
+        if k < 4:
+            h = _h(np.maximum(z, 0.0), half)
+            acts.append(h)
+        else:
+            h = z
+    return h, acts, layers
+
+
+def gradients(params: np.ndarray, raw: np.ndarray, targets: np.ndarray, half: bool = True):
+    """(flat gradient float64[N_PARAMS], loss) of sum((y - t)^2) over the 12 outputs."""
+    y, acts, layers = forward(params, raw, half)
+    t = np.asarray(targets, dtype=np.float64).reshape(-1, N_OUT)
+    d = np.zeros_like(y)
+    d[:, :N_OUT] = y[:, :N_OUT] - t
+    loss = float((d * d).sum())
+    dz = 2.0 * d
+    grads = [None] * 5
+    for k in range(4, -1, -1):
+        w, _ = layers[k]
+        grads[k] = (dz.T @ acts[k], dz.sum(axis=0))
+        if k > 0:
+            dh = dz @ w
+            dz = dh * (acts[k] > 0.0)
+    flat = np.concatenate([np.concatenate([gw.ravel(), gb]) for gw, gb in grads])
+    return flat, loss
