@@ -54,6 +54,7 @@ def parse_args():
     ap.add_argument("--cpu-scale", type=float, default=1.0,
                     help="scale of the CPU sample (strand count and pixel count)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-surrogate", action="store_true", help="skip the shade-model-1 measurement")
     return ap.parse_args()
 
 
@@ -189,6 +190,63 @@ def peaks() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
+def tensor_peak() -> tuple[float, str]:
+    """Dense 16-bit tensor-core peak (TFLOP/s): the measured cuBLAS bf16 burst
+    rate; FP16 runs at the same rate."""
+    try:
+        p = json.loads(MEASURED_PEAKS.read_text())
+        return float(p["bf16_tflops"]), "measured (cuBLAS bf16 burst; fp16 has the same dense rate)"
+    except (OSError, KeyError, ValueError):
+        return 1900.0, "fallback"
+
+
+MLP_FLOP_PER_EVAL = 27392  # 2 * (10*64 + 3*64*64 + 64*12)
+
+
+def surrogate_section(r, cam, lights, flush, stream, reps: int, karis_ms: float, hair_px: int) -> dict | None:
+    """Shade model 1 (the learned surrogate) on the same G-buffer: its time
+    beside the Karis shade, its tensor-core throughput, and both models'
+    error against FP64 lobes on 65,536 held-out samples."""
+    import torch
+
+    from bevy_hair_gb300 import abi
+    from bevy_hair_gb300 import surrogate as S
+
+    try:
+        params = S.load_params()
+    except (OSError, ValueError):
+        return None
+    s = S.Surrogate(r, params)
+    r.bind_surrogate(s)
+    times = []
+    for _ in range(reps + 2):
+        flush.fill_(5)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r.shade(cam, lights, model=abi.SHADE_SURROGATE)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+    ms = float(np.mean(times[2:]))
+    ev = S.evaluate(r, s, n=1 << 16)
+    r.bind_surrogate(None)
+    s.close()
+    evals = hair_px * len(lights)
+    tflops = evals * MLP_FLOP_PER_EVAL / (ms * 1e-3) / 1e12
+    peak, src = tensor_peak()
+    return {
+        "shade_ms": round(ms, 4), "karis_shade_ms": round(karis_ms, 4), "ratio_vs_karis": round(ms / karis_ms, 3),
+        "evaluations": int(evals), "flop_per_eval": MLP_FLOP_PER_EVAL,
+        "roofline": {"bound": "tensor", "achieved": round(tflops, 2), "peak": peak, "peak_source": src,
+                     "unit": "TFLOP/s", "frac": round(tflops / peak, 4)},
+        "error": {"judge": "FP64 lobes (64-point Gauss-Legendre in gamma_i, hg_mlp_samples), 65,536 held-out samples",
+                  "metric": "relative L1 of R + TT + TRT + 0.7 B",
+                  "surrogate": round(ev["surrogate_bsdf"], 5), "karis": round(ev["karis_bsdf"], 5),
+                  "per_lobe": {k: round(v, 5) for k, v in ev.items() if k.startswith(("surrogate_", "karis_"))
+                               and not k.endswith("bsdf")}},
+    }
+
+
 # Algorithmic bytes of each pass per launch (what roofline.achieved counts).
 def pass_bytes(sc, seg_refs: dict) -> dict:
     w, h = sc.view.width, sc.view.height
@@ -299,6 +357,8 @@ def run_ours(args, rank, world, local):
         for k, p in enumerate(passes):
             acc[p] += ev[k].elapsed_time(ev[k + 1]) / reps
     per_pass = {p: round(v, 4) for p, v in acc.items()}
+    surr = None if args.no_surrogate else surrogate_section(r, cam, lights, flush, stream, reps, acc["shade"],
+                                                             hair_px)
     nbytes = pass_bytes(sc, {"camera_refs": ref_c, "dom_refs": ref_d, "hair_pixels": hair_px,
                              "strands": sc.mesh.strand_count()})
     dominant = max((p for p in nbytes), key=lambda p: acc[p])
@@ -389,6 +449,7 @@ def run_ours(args, rank, world, local):
                    "parallelism": f"replicas x{world}"},
         "per_pass_ms": per_pass,
         "roofline": roofline,
+        "surrogate": surr,
         "cpu_baseline": cpu,
         "e2e": {"value": round(e2e_value, 4), "unit": "Gseg/s", "ms_per_step": round(e2e_ms / args.steps, 4),
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},

@@ -371,11 +371,48 @@ __global__ void __launch_bounds__(256, 3) shade_kernel(const ShadeArgs a) {
 // network for all of them per light, so every lane takes part in each
 // evaluation; pixels without hair run it on placeholder inputs.  Azimuthal
 // roughness beta_n, which the Karis fit does not have, is the fibre
-// roughness clamped to the trained range [0.2, 0.8].
+// roughness clamped to the trained range [0.2, 0.8].  Per-pixel work (view
+// and tangent, the shadowed light's DOM depth and spread) happens before the
+// light loop, so the loop holds little besides the network's fragments.
 constexpr int kSurrogateWarps = 8;
 constexpr size_t kSurrogateSmem = sizeof(mlp::FwdWeights) + kSurrogateWarps * sizeof(mlp::WarpIo);
 
-__global__ void __launch_bounds__(kSurrogateWarps * 32, 1)
+// Incident direction and weight (scalar factor on the light colour) of a
+// point, spot or rect light; directional lights have weight 1.
+__device__ __forceinline__ float light_weight(const hg_light& L, f3 world, f3& incident) {
+    const uint32_t kind = L.kind;
+    if (kind == HG_LIGHT_POINT || kind == HG_LIGHT_SPOT) {
+        f3 to_l = sub3(ld3(L.position), world);
+        float dist2 = dot3(to_l, to_l);
+        incident = safe_normalize(to_l);
+        float inv_r2 = 1.0f / fmaxf(L.range * L.range, 1e-8f);
+        float w = range_window(dist2, inv_r2) / fmaxf(dist2, 1e-4f);
+        if (kind == HG_LIGHT_SPOT) {
+            float cd = dot3(mul3s(ld3(L.direction), -1.0f), incident);
+            float sm = clampf(cd * L.spot[0] + L.spot[1], 0.0f, 1.0f);
+            w *= sm * sm;
+        }
+        return w;
+    }
+    if (kind == HG_LIGHT_DIRECTIONAL) {
+        incident = ld3(L.direction);
+        return 1.0f;
+    }
+    if (kind == HG_LIGHT_RECT) {
+        f3 to_c = sub3(ld3(L.position), world);
+        float dist2 = fmaxf(dot3(to_c, to_c), 1e-4f);
+        incident = mul3s(to_c, rsqrtf(dist2));
+        f3 normal = safe_normalize(cross3(ld3(L.up), ld3(L.right)));
+        float facing = fmaxf(dot3(normal, incident), 0.0f);
+        float solid = L.spot[0] * L.spot[1] * facing / dist2;
+        float range2 = fmaxf(L.range * L.range, 1e-4f);
+        return solid * range_window(dist2, 1.0f / range2);
+    }
+    incident = spl(0.0f);
+    return 0.0f;
+}
+
+__global__ void __launch_bounds__(kSurrogateWarps * 32, 2)
     shade_surrogate_kernel(const ShadeArgs a, const __half* __restrict__ w16, const float* __restrict__ mparams) {
     extern __shared__ __align__(16) unsigned char smem[];
     mlp::FwdWeights& w = *reinterpret_cast<mlp::FwdWeights*>(smem);
@@ -386,6 +423,14 @@ __global__ void __launch_bounds__(kSurrogateWarps * 32, 1)
     const uint32_t width = f2u(p.screen[0]), height = f2u(p.screen[1]);
     const uint32_t tiles_x = (width + 31u) >> 5, tiles = tiles_x * ((height + 7u) >> 3);
     const uint32_t lane = threadIdx.x & 31u, row = threadIdx.x >> 5;
+    // The light that receives the deep-opacity depth: the first shadow-casting
+    // directional light in the kind-sorted list (shade.wesl:486-503).
+    int dom_light = -1;
+    for (uint32_t i = 0; i < a.n_lights; ++i)
+        if (a.lights[i].kind == HG_LIGHT_DIRECTIONAL && (a.lights[i].flags & HG_LIGHT_CASTS_SHADOWS)) {
+            dom_light = (int)i;
+            break;
+        }
     for (uint32_t tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
         const uint32_t x = (tile % tiles_x) * 32u + lane, y = (tile / tiles_x) * 8u + row;
         const bool inside = x < width && y < height;
@@ -406,7 +451,6 @@ __global__ void __launch_bounds__(kSurrogateWarps * 32, 1)
         const f3 world = reconstruct_world(p, (int32_t)x, (int32_t)y, view_dist);
         const f3 tangent = oct_decode(high & 0xffu, low >> 24u);
         const float uvw_z = (float)((low >> 6u) & 0x3fu) / 63.0f;
-        const float beta = inside ? (float)(__ldg(&a.beta[pix]) & 0xffu) / 255.0f : 0.0f;
         const float roughness = fmaxf(p.appearance[0] * (0.65f + 0.7f * uvw_z), 0.04f);
         const float ascale = 0.65f + 0.35f * uvw_z;
         const f3 albedo = {p.albedo[0] * ascale, p.albedo[1] * ascale, p.albedo[2] * ascale};
@@ -419,45 +463,39 @@ __global__ void __launch_bounds__(kSurrogateWarps * 32, 1)
         const Shape shape = lobe_shape(roughness, p.appearance[1]);
         const f3 sigma_a = absorption_from_color(albedo, roughness);
         const float beta_n = clampf(roughness, 0.2f, 0.8f);
+        const f3 t_n = safe_normalize(tangent), v_n = safe_normalize(view);
+        const float sin_o = clampf(dot3(t_n, v_n), -1.0f, 1.0f);
+        const f3 t_o = sub3(v_n, mul3s(t_n, sin_o));
+        const float to2 = dot3(t_o, t_o);
         f3 color = spl(0.0f);
-        bool dom_left = true;
+        float dom_direct = 1.0f;
+        if (dom_light >= 0 && active) {
+            const hg_light& L = a.lights[dom_light];
+            const float beta = (float)(__ldg(&a.beta[pix]) & 0xffu) / 255.0f;
+            const float depth = -logf(fmaxf(dom_visibility(p, a.dom, world, beta), 1e-6f));
+            dom_direct = expf(-depth);
+            if (depth > 1e-3f) {
+                const float tv = dot3(tangent, view);
+                const Dual ds = dual_scatter(sqrtf(fmaxf(1.0f - tv * tv, 1e-6f)), sigma_a, shape);
+                const Geometry gm = light_geometry(tangent, view, ld3(L.direction));
+                color = vmul(spread_term(shape, ds, gm.theta_h, depth, dom_direct), ld3(L.color));
+            }
+        }
         for (uint32_t i = 0; i < a.n_lights; ++i) {
             const hg_light& L = a.lights[i];
-            const uint32_t kind = L.kind;
-            f3 incident = spl(0.0f);
-            float weight = 0.0f, depth = 0.0f;
-            if (kind == HG_LIGHT_POINT || kind == HG_LIGHT_SPOT) {
-                f3 to_l = sub3(ld3(L.position), world);
-                float dist2 = dot3(to_l, to_l);
-                incident = safe_normalize(to_l);
-                float inv_r2 = 1.0f / fmaxf(L.range * L.range, 1e-8f);
-                weight = range_window(dist2, inv_r2) / fmaxf(dist2, 1e-4f);
-                if (kind == HG_LIGHT_SPOT) {
-                    float cd = dot3(mul3s(ld3(L.direction), -1.0f), incident);
-                    float sm = clampf(cd * L.spot[0] + L.spot[1], 0.0f, 1.0f);
-                    weight *= sm * sm;
-                }
-            } else if (kind == HG_LIGHT_DIRECTIONAL) {
-                incident = ld3(L.direction);
-                weight = 1.0f;
-                if (dom_left && (L.flags & HG_LIGHT_CASTS_SHADOWS)) {
-                    if (active) depth = -logf(fmaxf(dom_visibility(p, a.dom, world, beta), 1e-6f));
-                    dom_left = false;
-                }
-            } else if (kind == HG_LIGHT_RECT) {
-                f3 to_c = sub3(ld3(L.position), world);
-                float dist2 = fmaxf(dot3(to_c, to_c), 1e-4f);
-                incident = mul3s(to_c, rsqrtf(dist2));
-                f3 normal = safe_normalize(cross3(ld3(L.up), ld3(L.right)));
-                float facing = fmaxf(dot3(normal, incident), 0.0f);
-                float solid = L.spot[0] * L.spot[1] * facing / dist2;
-                float range2 = fmaxf(L.range * L.range, 1e-4f);
-                weight = solid * range_window(dist2, 1.0f / range2);
-            }
+            f3 incident;
+            float weight = light_weight(L, world, incident);
+            if ((int)i == dom_light) weight = dom_direct;
             const bool use = active && weight > 0.0f;
             if (!__any_sync(0xffffffffu, use)) continue;
-            const Geometry gm = light_geometry(tangent, view, incident);
-            float raw[10] = {gm.sin_i, gm.sin_o, gm.cos_phi, sqrtf(fmaxf(1.0f - gm.cos_phi * gm.cos_phi, 0.0f)),
+            // sin theta_i and cos phi as light_geometry computes them (the
+            // network needs no angles).
+            const f3 l = safe_normalize(incident);
+            const float sin_i = clampf(dot3(t_n, l), -1.0f, 1.0f);
+            const f3 t_i = sub3(l, mul3s(t_n, sin_i));
+            const float proj = sqrtf(fmaxf(dot3(t_i, t_i) * to2, 1e-8f));
+            const float cos_phi = clampf(dot3(t_i, t_o) / proj, -1.0f, 1.0f);
+            float raw[10] = {sin_i, sin_o, cos_phi, sqrtf(fmaxf(1.0f - cos_phi * cos_phi, 0.0f)),
                              sigma_a.x, sigma_a.y, sigma_a.z, shape.beta.x, beta_n, kIor};
             if (!use) {
                 raw[0] = raw[1] = raw[3] = 0.0f;
@@ -468,20 +506,15 @@ __global__ void __launch_bounds__(kSurrogateWarps * 32, 1)
             }
             float xn[10], yv[12];
             mlp::normalise(raw, xn);
-            mlp::forward(w, io, xn, yv);
+            mlp::forward_fast(w, io, xn, yv);
             if (use) {
-                f3 single = {mlp::decode(yv[0]) + mlp::decode(yv[3]) + mlp::decode(yv[6]),
-                             mlp::decode(yv[1]) + mlp::decode(yv[4]) + mlp::decode(yv[7]),
-                             mlp::decode(yv[2]) + mlp::decode(yv[5]) + mlp::decode(yv[8])};
-                f3 back = {mlp::decode(yv[9]), mlp::decode(yv[10]), mlp::decode(yv[11])};
-                const float direct = expf(-depth);
-                f3 c = mul3s(add3(single, mul3s(back, kDensityBack)), direct);
-                if (depth > 1e-3f) {
-                    const float tv = dot3(tangent, view);
-                    const Dual ds = dual_scatter(sqrtf(fmaxf(1.0f - tv * tv, 1e-6f)), sigma_a, shape);
-                    c = add3(c, spread_term(shape, ds, gm.theta_h, depth, direct));
-                }
-                color = add3(color, mul3s(vmul(c, ld3(L.color)), weight));
+                f3 lobe = {mlp::decode_fast(yv[0]) + mlp::decode_fast(yv[3]) + mlp::decode_fast(yv[6]),
+                           mlp::decode_fast(yv[1]) + mlp::decode_fast(yv[4]) + mlp::decode_fast(yv[7]),
+                           mlp::decode_fast(yv[2]) + mlp::decode_fast(yv[5]) + mlp::decode_fast(yv[8])};
+                lobe = add3(lobe, mul3s(mk3(mlp::decode_fast(yv[9]), mlp::decode_fast(yv[10]),
+                                            mlp::decode_fast(yv[11])),
+                                        kDensityBack));
+                color = add3(color, mul3s(vmul(lobe, ld3(L.color)), weight));
             }
         }
         if (active) {

@@ -252,7 +252,7 @@ __global__ void __launch_bounds__(kWarps * 32) infer_kernel(const InferArgs a) {
         float raw[10], x[10], y[12];
         load_raw(a.inputs, i, valid, raw);
         normalise(raw, x);
-        forward(w, io[warp], x, y);
+        forward_fast(w, io[warp], x, y);
         if (valid) {
 #pragma unroll
             for (int c = 0; c < 12; ++c) {

@@ -174,7 +174,7 @@ def evaluate(renderer: HairRenderer, surrogate: Surrogate, n: int = 1 << 16, see
     return out
 
 
-def train(renderer: HairRenderer, n_samples: int = 16 << 20, batch: int = 32768, epochs: int = 40,
+def train(renderer: HairRenderer, n_samples: int = 16 << 20, batch: int = 16384, epochs: int = 150,
           lr_max: float = 3e-3, lr_min: float = 1e-5, warmup: int = 200, seed: int = SAMPLE_SEED,
           init_seed: int = 0, log=print) -> tuple[np.ndarray, dict]:
     """Generate n_samples FP64 samples on the GPU and fit the network with Adam
@@ -232,8 +232,8 @@ def main(argv=None) -> int:
 
     ap = argparse.ArgumentParser(description="Train the shading surrogate on FP64 samples generated on the GPU.")
     ap.add_argument("--samples", type=int, default=16 << 20)
-    ap.add_argument("--batch", type=int, default=32768)
-    ap.add_argument("--epochs", type=int, default=40)
+    ap.add_argument("--batch", type=int, default=16384)
+    ap.add_argument("--epochs", type=int, default=150)
     ap.add_argument("--lr", type=float, default=3e-3)
     ap.add_argument("--out", type=Path, default=WEIGHTS)
     ap.add_argument("--history", type=Path, default=None)

@@ -409,7 +409,7 @@ def test_hair_visibility_for_receivers(renderer):
     renderer.synchronize()
     got = d_out.cpu().numpy()
     dmap = renderer.read(abi.BUF_DOM)
-    want = oracle.hair_visibility(light.view(np.float32), dmap, *sc.dom_size, pts)
+    want = oracle.hair_visibility(np.atleast_1d(light).view(np.float32), dmap, *sc.dom_size, pts)
     np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-6)
     assert (want < 0.99).sum() > 100 and (want == 1.0).sum() > 100  # shadowed and unshadowed points
     g.close()
