@@ -55,6 +55,8 @@ def parse_args():
                     help="scale of the CPU sample (strand count and pixel count)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-surrogate", action="store_true", help="skip the shade-model-1 measurement")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-frame (config 4) measurement")
+    ap.add_argument("--batch-scale", type=float, default=1.0, help="scale of the config-4 batch")
     return ap.parse_args()
 
 
@@ -268,6 +270,140 @@ def pass_bytes(sc, seg_refs: dict) -> dict:
     }
 
 
+BATCH_WORKLOAD = ("config4: 64 seeded grooms of uneven size (1k-50k strands, 16-128 segments, mixed straight/wavy/"
+                  "curly), each with its own square camera view (side 256-1024) and 512^2 x16 deep opacity map, "
+                  "one launch per pass over all items, replayed as one CUDA graph")
+
+
+def batch_measure(r, stream, flush, steps: int, warmup: int, scale: float) -> dict:
+    """The config-4 batched frame: graph replay against direct batched
+    launches and against hg_groom_frame per groom, with the autotuner's table."""
+    import torch
+
+    from bevy_hair_gb300 import abi, configs
+    from bevy_hair_gb300.pipeline import HairBatch
+
+    t_bake = time.perf_counter()
+    bs = configs.config4(scale)
+    t_bake = time.perf_counter() - t_bake
+    grooms = [r.upload(sc.mesh) for sc in bs.scenes]
+    b = HairBatch(r, grooms, bs.sizes())
+    params = [sc.params() for sc in bs.scenes]
+    for k, (c, d) in enumerate(params):
+        b.set_params(k, c, d)
+    lights = bs.light_array()
+    b.frame(lights)
+    r.synchronize()
+    segs = refs = 0
+    for g in grooms:
+        total = int(g.read(abi.SLOT_CAMERA, abi.GBUF_INDIRECT)[0])
+        refs += total
+        segs += configs.segments_of(g.read(abi.SLOT_CAMERA, abi.GBUF_REFS), total)
+    tuning = b.tune(lights)
+
+    def timed(mode: int, n: int) -> float:
+        for _ in range(warmup):
+            flush.fill_(7)
+            b.frame(lights, mode)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(n)]
+        for i in range(n):
+            flush.fill_(i & 0xFF)
+            ev[i][0].record(stream)
+            b.frame(lights, mode)
+            ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        return float(np.mean([a.elapsed_time(z) for a, z in ev]))
+
+    graph_ms = timed(abi.BATCH_GRAPH, steps)
+    direct_ms = timed(abi.BATCH_LAUNCHES, max(3, steps // 2))
+    separate_ms = timed(abi.BATCH_SEPARATE, max(3, steps // 4))
+    phases = [b.profile(lights) for _ in range(3)]
+    phase_ms = {k: round(float(np.mean([p[k] for p in phases])), 4) for k in phases[0]}
+    # end to end: every item's uniforms from the host, the graph frame, and every
+    # item's colour + depth back into pinned host memory
+    sizes = bs.sizes()
+    px = [w * h for w, h, _, _ in sizes]
+    pinned = torch.empty(sum(px) * 5, dtype=torch.float32, pin_memory=True)
+    d2h = sum(px) * 20
+    h2d = len(params) * 2 * abi.HAIR_PARAMS.itemsize + lights.nbytes
+
+    def e2e_step():
+        for k, (c, d) in enumerate(params):
+            b.set_params(k, c, d)
+        b.frame(lights)
+        off = 0
+        for k, n in enumerate(px):
+            st1 = r.lib.hg_batch_copy_out(b.handle, k, abi.BUF_COLOR, pinned.data_ptr() + off * 4, n * 16)
+            st2 = r.lib.hg_batch_copy_out(b.handle, k, abi.BUF_DEPTH, pinned.data_ptr() + (off + 4 * n) * 4, n * 4)
+            assert st1 == 0 and st2 == 0
+            off += 5 * n
+
+    e2e_step()
+    n_e2e = max(3, steps // 4)
+    t = time.perf_counter()
+    for _ in range(n_e2e):
+        e2e_step()
+    e2e_ms = (time.perf_counter() - t) * 1e3 / n_e2e
+    out = {
+        "workload": BATCH_WORKLOAD if scale == 1.0 else f"config4 scale {scale}",
+        "items": len(grooms), "strands": sum(sc.mesh.strand_count() for sc in bs.scenes),
+        "camera_pixels": int(sum(px)), "camera_refs": refs, "camera_segments": segs,
+        "graph_ms": round(graph_ms, 4), "batched_launches_ms": round(direct_ms, 4),
+        "separate_ms": round(separate_ms, 4), "speedup_vs_separate": round(separate_ms / graph_ms, 3),
+        "gseg_per_s": round(segs / (graph_ms * 1e-3) / 1e9, 4),
+        "launches": {"graph": b.launches(abi.BATCH_GRAPH), "separate": b.launches(abi.BATCH_SEPARATE)},
+        "phase_ms": phase_ms,
+        "tuning": {"chosen": b.tuning(), "tried": tuning},
+        "e2e": {"ms_per_frame": round(e2e_ms, 4), "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "bake_s": round(t_bake, 1),
+    }
+    b.close()
+    for g in grooms:
+        g.close()
+    return out
+
+
+def run_batch(args, rank, world, local):
+    """bench.py --config 4: the batched frame is the step."""
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = Dist(world, "nccl")
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    from bevy_hair_gb300.pipeline import HairRenderer
+
+    r = HairRenderer(local, stream.cuda_stream)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    clocks = Clocks(local)
+    clocks.start()
+    m = batch_measure(r, stream, flush, args.steps, max(args.warmup, 3), args.scale)
+    clk = clocks.stop()
+    value, total_ms, _ = aggregate(dist, m["graph_ms"] * args.steps, float(m["camera_segments"]) * args.steps)
+    r.close()
+    dist.close()
+    if rank != 0:
+        return None
+    return {
+        "metric": "Gseg/s of a 64-groom batched frame (all camera segments; raster + DOM + shade + filter + "
+                  "composite of every item)",
+        "value": round(value, 4), "unit": "Gseg/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+u64",
+        "data": "synthetic (seeded grooms, baked by the project's baker; no dataset exists)",
+        "config": {"workload": m["workload"], "l2": "flushed between timed steps (256 MB device write)",
+                   "parallelism": f"replicas x{world}"},
+        "batch": m,
+        "e2e": {"value": round(m["camera_segments"] / (m["e2e"]["ms_per_frame"] * 1e-3) / 1e9, 4),
+                "unit": "Gseg/s", "ms_per_step": m["e2e"]["ms_per_frame"],
+                "h2d_bytes_per_step": m["e2e"]["h2d_bytes_per_step"],
+                "d2h_bytes_per_step": m["e2e"]["d2h_bytes_per_step"]},
+        "gpu_launches": m["launches"]["graph"] * args.steps,
+        "clocks": clk,
+    }
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -359,6 +495,8 @@ def run_ours(args, rank, world, local):
     per_pass = {p: round(v, 4) for p, v in acc.items()}
     surr = None if args.no_surrogate else surrogate_section(r, cam, lights, flush, stream, reps, acc["shade"],
                                                              hair_px)
+    batch = None if args.no_batch else batch_measure(r, stream, flush, max(5, min(args.steps, 10)), 3,
+                                                     args.batch_scale)
     nbytes = pass_bytes(sc, {"camera_refs": ref_c, "dom_refs": ref_d, "hair_pixels": hair_px,
                              "strands": sc.mesh.strand_count()})
     dominant = max((p for p in nbytes), key=lambda p: acc[p])
@@ -450,6 +588,7 @@ def run_ours(args, rank, world, local):
         "per_pass_ms": per_pass,
         "roofline": roofline,
         "surrogate": surr,
+        "batch": batch,
         "cpu_baseline": cpu,
         "e2e": {"value": round(e2e_value, 4), "unit": "Gseg/s", "ms_per_step": round(e2e_ms / args.steps, 4),
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -464,11 +603,13 @@ def cpu_baseline(args, sample: bool) -> dict:
     from bevy_hair_gb300 import configs
 
     scale = args.cpu_scale
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    if args.config == 4:
+        return run_reference_batch(args, world, threads)
     sc = configs.CONFIGS[args.config](scale)
     cam, dom = sc.params()
     lights = sc.light_array()
-    threads = os.cpu_count() or 1
-    oracle.set_threads(threads)
     t = time.perf_counter()
     out = oracle.frame(sc.mesh, cam, dom, lights)
     dt = time.perf_counter() - t
@@ -481,6 +622,42 @@ def cpu_baseline(args, sample: bool) -> dict:
             "seconds": round(dt, 3)}
 
 
+def run_reference_batch(args, world, threads):
+    """The CPU restatement over the config-4 items, one frame per item, until
+    the time budget runs out (a bounded sample of the batch)."""
+    import oracle
+    from bevy_hair_gb300 import configs
+
+    bs = configs.config4(args.scale)
+    lights = bs.light_array()
+    budget, t = 150.0, time.perf_counter()
+    segs = items = 0
+    for step in range(max(args.steps, 1)):
+        for sc in bs.scenes:
+            cam, dom = sc.params()
+            out = oracle.frame(sc.mesh, cam, dom, lights)
+            segs += int(out["counts_camera"]["segments"])
+            items += 1
+            if time.perf_counter() - t > budget:
+                break
+        if time.perf_counter() - t > budget:
+            break
+    dt = time.perf_counter() - t
+    value = segs / dt / 1e9
+    sample = f"{items} item frames of the config-4 batch (scale {args.scale}) on the CPU oracle, {dt:.1f} s"
+    return {
+        "impl": "reference", "metric": "Gseg/s of a 64-groom batched frame (all camera segments; raster + DOM + "
+                                       "shade + filter + composite of every item)",
+        "value": round(value, 6), "unit": "Gseg/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(dt * 1e3 * len(bs.scenes) / max(items, 1), 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32+u64", "data": "synthetic (seeded grooms)",
+        "config": {"workload": BATCH_WORKLOAD if args.scale == 1.0 else f"config4 scale {args.scale}"},
+        "cpu_baseline": {"value": round(value, 6), "unit": "Gseg/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 6), "unit": "Gseg/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return None
@@ -488,11 +665,13 @@ def run_reference(args, rank, world):
     from bevy_hair_gb300 import configs
 
     scale = args.cpu_scale
+    threads = os.cpu_count() or 1
+    oracle.set_threads(threads)
+    if args.config == 4:
+        return run_reference_batch(args, world, threads)
     sc = configs.CONFIGS[args.config](scale)
     cam, dom = sc.params()
     lights = sc.light_array()
-    threads = os.cpu_count() or 1
-    oracle.set_threads(threads)
     for _ in range(min(args.warmup, 1)):
         oracle.frame(sc.mesh, cam, dom, lights)
     steps = args.steps
@@ -538,6 +717,8 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         line = run_reference(args, rank, world)
+    elif args.config == 4:
+        line = run_batch(args, rank, world, local)
     else:
         line = run_ours(args, rank, world, local)
     if rank == 0 and line is not None:

@@ -104,6 +104,33 @@ class FrameDesc(C.Structure):
     ]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [
+        ("groom", C.c_void_p),
+        ("width", C.c_uint32),
+        ("height", C.c_uint32),
+        ("dom_w", C.c_uint32),
+        ("dom_h", C.c_uint32),
+    ]
+
+
+class BatchTuning(C.Structure):
+    _fields_ = [
+        ("raster_chunk", C.c_uint32),
+        ("raster_blocks_per_sm", C.c_uint32),
+        ("tile_w", C.c_uint32),
+        ("tile_h", C.c_uint32),
+        ("filter_tile", C.c_uint32),
+        ("ms", C.c_float),
+    ]
+
+    def as_dict(self) -> dict:
+        return {n: (round(float(getattr(self, n)), 4) if n == "ms" else int(getattr(self, n))) for n, _ in self._fields_}
+
+
+BATCH_GRAPH, BATCH_LAUNCHES, BATCH_SEPARATE = 0, 1, 2
+BATCH_MAX_ITEMS = 128
+
 # --------------------------------------------------------------------- loading
 
 _LIB = None
@@ -150,6 +177,17 @@ _SIGNATURES = {
     "hg_mlp_train_step": (_I32, [_VP, _VP, _VP, _U32, _F32, _VP]),
     "hg_mlp_bind": (_I32, [_VP, _VP]),
     "hg_karis_lobes": (_I32, [_VP, _VP, _U32, _F32, _VP]),
+    "hg_batch_create": (_I32, [_VP, _VP, _U32, C.POINTER(_VP)]),
+    "hg_batch_destroy": (None, [_VP]),
+    "hg_batch_set_params": (_I32, [_VP, _U32, _VP, _VP]),
+    "hg_batch_frame": (_I32, [_VP, C.POINTER(ShadeDesc), _I32]),
+    "hg_batch_launches": (_I32, [_VP, _I32, C.POINTER(_U32)]),
+    "hg_batch_profile": (_I32, [_VP, C.POINTER(ShadeDesc), _VP]),
+    "hg_batch_tune": (_I32, [_VP, C.POINTER(ShadeDesc), _VP, _U32, C.POINTER(_U32)]),
+    "hg_batch_set_tuning": (_I32, [_VP, C.POINTER(BatchTuning)]),
+    "hg_batch_get_tuning": (_I32, [_VP, C.POINTER(BatchTuning)]),
+    "hg_batch_buffer": (_I32, [_VP, _U32, _I32, C.POINTER(_VP), C.POINTER(_SZ)]),
+    "hg_batch_copy_out": (_I32, [_VP, _U32, _I32, _VP, _SZ]),
 }
 
 _BAKE_SIGNATURES = {

@@ -35,7 +35,7 @@ EXACT_UNITS = {"raster.cu", "filter.cu"}
 # distance, reconstructed position, decoded tangent) use explicitly rounded
 # intrinsics, which -use_fast_math does not change.
 FAST_UNITS = {"shade.cu"}
-CUDA_UNITS = ["api.cu", "raster.cu", "shade.cu", "filter.cu", "receiver.cu", "surrogate.cu"]
+CUDA_UNITS = ["api.cu", "raster.cu", "shade.cu", "filter.cu", "receiver.cu", "surrogate.cu", "batch.cu"]
 
 
 def nvcc() -> str:

@@ -8,6 +8,11 @@ Config 2: 100,000 wavy strands x 64 segments, 1920x1080, DOM 1024^2, key
 Config 3: 200,000 curly strands x 128 segments, 3840x2160, DOM 2048^2, LOD on
           with the camera far enough that bundles take several LOD levels,
           16 lights.
+Config 4: a batch of 64 independent grooms of uneven size (1k-50k strands,
+          16-128 segments, log-uniform from the seed, mixed straight / wavy /
+          curly), each with its own square camera view of side 256-1024
+          (log-uniform) and its own 512^2 deep opacity map; key directional
+          light plus 2 point lights shared by all.
 
 ``scale`` shrinks the strand count and the image/DOM sides for quick tests
 (the scene geometry stays the same).
@@ -72,7 +77,7 @@ def _ring_lights(n: int, radius: float, height: float, intensity: float, rng_see
     return out
 
 
-@functools.lru_cache(maxsize=8)
+@functools.lru_cache(maxsize=160)
 def _mesh(n_strands: int, segments: int, style: str, seed: int) -> groom.HairMesh:
     return groom.bake(groom.synthetic_strands(n_strands, segments, style, seed), ambient_occlusion=True)
 
@@ -118,6 +123,42 @@ def config3(scale: float = 1.0) -> Scene:
     lights = [key, fill] + _ring_lights(14, 600.0, 0.0, 8.0e4, SEED_BASE + 3)
     return Scene("config3", mesh, g, _camera(w, h, 1400.0), (dom, dom), lights,
                  [host.Directional(np.asarray(KEY_DIR, dtype=F), True)])
+
+
+@dataclass
+class BatchScene:
+    name: str
+    scenes: list[Scene]
+    lights: list[Light]
+
+    def light_array(self) -> np.ndarray:
+        return pack_lights(self.lights)
+
+    def sizes(self) -> list[tuple[int, int, int, int]]:
+        return [(s.view.width, s.view.height, *s.dom_size) for s in self.scenes]
+
+
+def config4(scale: float = 1.0, items: int = 64) -> BatchScene:
+    rng = np.random.default_rng(SEED_BASE + 4)
+    styles = ("straight", "wavy", "curly")
+    key = Light(kind=abi.LIGHT_DIRECTIONAL, color=(3.0, 2.9, 2.7), direction=KEY_DIR, casts_shadows=True)
+    lights = [key] + _ring_lights(2, 500.0, 50.0, 6.0e4, SEED_BASE + 4)
+    dom = _scaled(512, math.sqrt(scale), 16)
+    scenes = []
+    for k in range(items):
+        n = _scaled(int(round(math.exp(rng.uniform(math.log(1_000), math.log(50_000))))), scale, 16)
+        segments = int(round(math.exp(rng.uniform(math.log(16), math.log(128)))))
+        style = styles[int(rng.integers(0, 3))]
+        side = _scaled(int(round(math.exp(rng.uniform(math.log(256), math.log(1024))))), math.sqrt(scale), 32)
+        azimuth = float(rng.uniform(0.0, 2.0 * math.pi))
+        distance = float(rng.uniform(700.0, 1100.0))
+        mesh = _mesh(n, segments, style, SEED_BASE + 400 + k)
+        g = host.HairGroom(lam=3.0, albedo=tuple(float(v) for v in rng.uniform(0.05, 0.4, 3)), roughness=0.3,
+                           tilt=0.08, lod=True, filter=True, ambient_occlusion=True, deep_opacity=True,
+                           center_diameter=1.0)
+        scenes.append(Scene(f"config4[{k}]", mesh, g, _camera(side, side, distance, azimuth=azimuth), (dom, dom),
+                            lights, [host.Directional(np.asarray(KEY_DIR, dtype=F), True)]))
+    return BatchScene("config4", scenes, lights)
 
 
 CONFIGS = {1: config1, 2: config2, 3: config3}

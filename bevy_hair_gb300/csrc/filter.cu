@@ -13,7 +13,6 @@ namespace {
 
 constexpr int kFilterRadius = 5;
 constexpr int kTileX = 32, kTileY = 8;
-constexpr int kHaloX = kTileX + 2 * kFilterRadius, kHaloY = kTileY + 2 * kFilterRadius;
 
 struct FilterArgs {
     hg_hair_params p;
@@ -47,20 +46,23 @@ __device__ __forceinline__ float sqrt_bound(float r) {
     return x;
 }
 
-// One 32x8 tile per CTA.  The 42x18 neighbourhood is staged in shared memory
-// once: per texel the centre word's normalised depth f32(depth)/16777214 (the
-// exact value filter.wgsl:94 computes per tap; -1 marks an empty centre with a
-// conservative hit, -2 both empty) and the shaded colour.  Coverage decisions
-// use exact arithmetic; the colour weights only scale colour, so they use the
-// fast exponential.
-__global__ void __launch_bounds__(kTileX* kTileY) filter_kernel(const FilterArgs a) {
+// One TX x TY tile per CTA (tile (bx, by) of view a: fields p, center, cons,
+// shaded, filtered, filtered_depth).  The (TX+10) x (TY+10) neighbourhood is
+// staged in shared memory once: per texel the centre word's normalised depth
+// f32(depth)/16777214 (the exact value filter.wgsl:94 computes per tap; -1
+// marks an empty centre with a conservative hit, -2 both empty) and the shaded
+// colour.  Coverage decisions use exact arithmetic; the colour weights only
+// scale colour, so they use the fast exponential.
+template <int TX, int TY, class V>
+__device__ __forceinline__ void filter_tile(const V& a, int32_t bx, int32_t by) {
+    constexpr int kHaloX = TX + 2 * kFilterRadius, kHaloY = TY + 2 * kFilterRadius;
     __shared__ float s_norm[kHaloY][kHaloX];
     __shared__ float4 s_col[kHaloY][kHaloX];
     const hg_hair_params& p = a.p;
     const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
-    const int32_t x0 = blockIdx.x * kTileX - kFilterRadius, y0 = blockIdx.y * kTileY - kFilterRadius;
-    const int tid = threadIdx.y * kTileX + threadIdx.x;
-    for (int i = tid; i < kHaloX * kHaloY; i += kTileX * kTileY) {
+    const int32_t x0 = bx * TX - kFilterRadius, y0 = by * TY - kFilterRadius;
+    const int tid = threadIdx.y * TX + threadIdx.x;
+    for (int i = tid; i < kHaloX * kHaloY; i += TX * TY) {
         int hx = i % kHaloX, hy = i / kHaloX;
         int32_t gx = x0 + hx, gy = y0 + hy;
         float nrm = -2.0f;
@@ -80,7 +82,7 @@ __global__ void __launch_bounds__(kTileX* kTileY) filter_kernel(const FilterArgs
     }
     __syncthreads();
 
-    const int32_t px = blockIdx.x * kTileX + threadIdx.x, py = blockIdx.y * kTileY + threadIdx.y;
+    const int32_t px = bx * TX + threadIdx.x, py = by * TY + threadIdx.y;
     if (px >= width || py >= height) return;
     const uint32_t pix = (uint32_t)py * (uint32_t)width + (uint32_t)px;
     const unsigned long long center_word = __ldg(&a.center[pix]), cons_word = __ldg(&a.cons[pix]);
@@ -171,6 +173,31 @@ __global__ void __launch_bounds__(kTileX* kTileY) filter_kernel(const FilterArgs
     a.filtered_depth[pix] = view_dist;
 }
 
+__global__ void __launch_bounds__(kTileX* kTileY) filter_kernel(const FilterArgs a) {
+    filter_tile<kTileX, kTileY>(a, blockIdx.x, blockIdx.y);
+}
+
+// Tile t of the camera views' concatenated tile space -> (view, bx, by).
+__device__ __forceinline__ uint32_t tile_view(const uint32_t* __restrict__ prefix, uint32_t n, uint32_t t) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (prefix[mid] <= t) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+template <int TX, int TY>
+__global__ void __launch_bounds__(TX* TY) batch_filter_kernel(const BatchView* __restrict__ views,
+                                                             const uint32_t* __restrict__ prefix, uint32_t n_cam) {
+    const uint32_t v = tile_view(prefix, n_cam, blockIdx.x);
+    const BatchView& a = views[v];
+    const uint32_t t = blockIdx.x - prefix[v];
+    const uint32_t tiles_x = (a.width + TX - 1) / TX;
+    filter_tile<TX, TY>(a, (int32_t)(t % tiles_x), (int32_t)(t / tiles_x));
+}
+
 struct CompositeArgs {
     hg_hair_params p;
     const float4* color_src;
@@ -181,15 +208,16 @@ struct CompositeArgs {
 
 // composite.wgsl:162-181; blend src*a + dst*(1-a) (alpha: a + dst_a*(1-a)),
 // depth test GreaterEqual when reverse-Z else LessEqual, depth write on.
-__global__ void composite_kernel(const CompositeArgs a) {
+template <class V>
+__device__ __forceinline__ void composite_pixel(const V& a, const float4* __restrict__ color_src,
+                                                const float* __restrict__ depth_src, int32_t px, int32_t py) {
     const hg_hair_params& p = a.p;
     const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
-    const int32_t px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y * blockDim.y + threadIdx.y;
     if (px >= width || py >= height) return;
     const uint32_t pix = (uint32_t)py * (uint32_t)width + (uint32_t)px;
-    const float4 c = __ldg(&a.color_src[pix]);
+    const float4 c = __ldg(&color_src[pix]);
     if (c.w < 0.001f) return;
-    const float view_dist = __ldg(&a.depth_src[pix]);
+    const float view_dist = __ldg(&depth_src[pix]);
     const f3 world = reconstruct_world(p, px, py, view_dist);
     const float4 clip = mat_mul(p.clip_from_world, world.x, world.y, world.z, 1.0f);
     const float depth = clampf(__fdiv_rn(clip.z, fmaxf(clip.w, 1e-5f)), 0.0f, 1.0f);
@@ -204,6 +232,22 @@ __global__ void composite_kernel(const CompositeArgs a) {
     d.z = c.z * c.w + d.z * ia;
     d.w = c.w * 1.0f + d.w * ia;
     a.color[pix] = d;
+}
+
+__global__ void composite_kernel(const CompositeArgs a) {
+    composite_pixel(a, a.color_src, a.depth_src, blockIdx.x * blockDim.x + threadIdx.x,
+                    blockIdx.y * blockDim.y + threadIdx.y);
+}
+
+__global__ void batch_composite_kernel(const BatchView* __restrict__ views, const uint32_t* __restrict__ prefix,
+                                       uint32_t n_cam, uint32_t source_filtered) {
+    const uint32_t v = tile_view(prefix, n_cam, blockIdx.x);
+    const BatchView& a = views[v];
+    const uint32_t t = blockIdx.x - prefix[v];
+    const uint32_t tiles_x = (a.width + blockDim.x - 1) / blockDim.x;
+    composite_pixel(a, source_filtered ? a.filtered : a.shaded, source_filtered ? a.filtered_depth : a.shaded_depth,
+                    (int32_t)((t % tiles_x) * blockDim.x + threadIdx.x),
+                    (int32_t)((t / tiles_x) * blockDim.y + threadIdx.y));
 }
 
 __global__ void clear_color_kernel(float4* __restrict__ color, float* __restrict__ depth, size_t pixels,
@@ -241,6 +285,25 @@ cudaError_t launch_composite(hg_ctx* ctx, const hg_hair_params& p, uint32_t sour
     dim3 block(32, 8);
     dim3 grid((ctx->width + 31) / 32, (ctx->height + 7) / 8);
     composite_kernel<<<grid, block, 0, ctx->stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_filter_composite(hg_ctx* ctx, const BatchDev& b) {
+    cudaError_t e;
+    if (b.filter && b.total_ftiles) {
+        if (b.filter_tile == 1) batch_filter_kernel<16, 16><<<b.total_ftiles, dim3(16, 16), 0, ctx->stream>>>(
+            b.views, b.ftile_prefix, b.n_cam);
+        else batch_filter_kernel<kTileX, kTileY><<<b.total_ftiles, dim3(kTileX, kTileY), 0, ctx->stream>>>(
+            b.views, b.ftile_prefix, b.n_cam);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if (!b.composite || !b.total_px) return cudaSuccess;
+    const int threads = 256;
+    const int blocks = (int)std::min<uint64_t>((b.total_px + threads - 1) / threads, (uint64_t)ctx->sm_count * 8);
+    clear_color_kernel<<<blocks, threads, 0, ctx->stream>>>(b.color, b.depth, b.total_px, b.depth_clear);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    batch_composite_kernel<<<b.total_tiles, dim3(b.tile_w, b.tile_h), 0, ctx->stream>>>(b.views, b.tile_prefix,
+                                                                                       b.n_cam, b.filter);
     return cudaGetLastError();
 }
 

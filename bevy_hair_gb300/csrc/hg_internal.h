@@ -86,6 +86,72 @@ struct hg_ctx {
 
 namespace hg {
 
+// One view of a batched item (its camera view, or its deep-opacity view):
+// uniforms, groom buffers and targets.  A device table of these is read in
+// place by the batched kernels; the field names match the single-view
+// argument structs so the same device functions serve both.
+struct BatchView {
+    hg_hair_params p;
+    const hg_gpu_bundle* bundles;
+    const float4* layers;
+    const float4* style;
+    hg_lod_record* lod;
+    uint32_t* depth_key;
+    uint32_t* offsets;
+    uint32_t* indirect;
+    hg_strand_ref* refs;
+    float4* cache;                 // strand cache of the item's groom
+    const uint32_t* strand_base;
+    const uint32_t* strand_bundle;
+    unsigned long long* center;
+    unsigned long long* cons;
+    uint32_t* beta;
+    uint32_t* dom;                 // the item's deep opacity map (camera and DOM views)
+    float4* shaded;
+    float* shaded_depth;
+    float4* filtered;
+    float* filtered_depth;
+    float4* color;
+    float* depth;
+    const float* scene;
+    uint32_t* err;
+    uint32_t bundle_count;         // bundles of the groom
+    uint32_t count;                // bundles the view's lod/scan cover: min(pass_mode.y, bundle_count)
+    uint32_t capacity;             // strand-ref capacity
+    uint32_t strands;              // strands of the groom (the cache's extent)
+    uint32_t width, height;        // this view's target size
+    uint32_t dom_w, dom_h;
+};
+
+// Launch description of one batched frame: the view table (camera views
+// first, then deep-opacity views), prefix tables over views, the contiguous
+// target arenas and the tuning.
+struct BatchDev {
+    const BatchView* views = nullptr;
+    uint32_t n_views = 0, n_cam = 0;
+    const uint32_t* bundle_prefix = nullptr;  // n_views + 1, bundles covered by lod/scan
+    const uint32_t* strand_prefix = nullptr;  // n_cam + 1, strands to generate
+    const uint32_t* tile_prefix = nullptr;    // n_cam + 1, tile_w x tile_h pixel tiles
+    const uint32_t* ftile_prefix = nullptr;   // n_cam + 1, filter tiles
+    const uint32_t* dom_prefix = nullptr;     // n_cam + 1, DOM words (front + counters) per item
+    uint32_t total_bundles = 0, total_strands = 0, total_tiles = 0, total_ftiles = 0;
+    uint64_t total_px = 0, total_dom_words = 0;
+    unsigned long long* center = nullptr;     // arenas: every camera view's slice, concatenated
+    unsigned long long* cons = nullptr;
+    uint32_t* beta = nullptr;
+    uint32_t* dom = nullptr;
+    float4* color = nullptr;
+    float* depth = nullptr;
+    uint32_t* counters = nullptr;             // work counters of the two raster launches
+    const hg_light* lights = nullptr;
+    uint32_t n_lights = 0, ortho = 0;
+    float exposure = 1.0f, depth_clear = 0.0f;
+    uint32_t filter = 1, composite = 1;
+    uint32_t gen_blocks = 1;                  // grid of the generate pass (occupancy x SMs)
+    // tuning
+    uint32_t raster_chunk = 4, raster_blocks_per_sm = 1, tile_w = 32, tile_h = 8, filter_tile = 0;
+};
+
 // raster.cu
 cudaError_t launch_clear(hg_ctx* ctx);
 cudaError_t launch_clear_dom(hg_ctx* ctx);
@@ -99,6 +165,14 @@ constexpr uint32_t kStrandCacheCps = 65;
 cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights, uint32_t ortho, float exposure,
                          uint32_t model);
 cudaError_t launch_karis_lobes(hg_ctx* ctx, const float* inputs, uint32_t n, float tilt, float* lobes);
+
+// batched passes (raster.cu, shade.cu, filter.cu)
+cudaError_t batch_occupancy(uint32_t* raster_per_sm, uint32_t* gen_per_sm);
+cudaError_t launch_batch_setup(hg_ctx* ctx, const BatchDev& b);     // clears, lod, scan, generate
+cudaError_t launch_batch_raster(hg_ctx* ctx, const BatchDev& b);    // camera + DOM depth, then DOM layers
+cudaError_t launch_batch_shade(hg_ctx* ctx, const BatchDev& b);
+cudaError_t launch_batch_filter_composite(hg_ctx* ctx, const BatchDev& b);
+constexpr uint32_t kBatchMaxViews = 256;
 
 // surrogate.cu
 cudaError_t launch_mlp_infer(hg_mlp* m, const float* inputs, uint32_t n, float* lobes, float* net);

@@ -83,12 +83,9 @@ constexpr uint32_t kDepthBuckets = 1024;
 // lod.wgsl:6-59, one warp per bundle (two of the 64 cage corners per lane).
 // Also writes the bundle's nearest view distance as one of kDepthBuckets
 // buckets between near and far, for the front-to-back draw order.
-__global__ void lod_kernel(const hg_hair_params p, const hg_gpu_bundle* __restrict__ bundles,
-                           const float4* __restrict__ layers, hg_lod_record* __restrict__ out,
-                           uint32_t* __restrict__ depth_key, uint32_t count) {
-    uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    uint32_t lane = threadIdx.x & 31u;
-    if (b >= count) return;
+__device__ __forceinline__ void lod_bundle(const hg_hair_params& p, const hg_gpu_bundle* __restrict__ bundles,
+                                           const float4* __restrict__ layers, hg_lod_record* __restrict__ out,
+                                           uint32_t* __restrict__ depth_key, uint32_t b, uint32_t lane) {
     hg_gpu_bundle bundle = bundles[b];
     float mnx = 1e20f, mny = 1e20f, mxx = -1e20f, mxy = -1e20f, mnd = 3.0e38f;
     bool front = false;
@@ -141,6 +138,15 @@ __global__ void lod_kernel(const hg_hair_params p, const hg_gpu_bundle* __restri
     out[b] = hg_lod_record{n_lod, cps, bundle.strand_count, 0u};
 }
 
+__global__ void lod_kernel(const hg_hair_params p, const hg_gpu_bundle* __restrict__ bundles,
+                           const float4* __restrict__ layers, hg_lod_record* __restrict__ out,
+                           uint32_t* __restrict__ depth_key, uint32_t count) {
+    uint32_t b = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    uint32_t lane = threadIdx.x & 31u;
+    if (b >= count) return;
+    lod_bundle(p, bundles, layers, out, depth_key, b, lane);
+}
+
 // ------------------------------------------------------------------ scan
 
 // scan.wgsl:6-24 in two parallel steps.  Step 1 (one CTA): exclusive scan of
@@ -178,14 +184,12 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
     return r;
 }
 
-__global__ void __launch_bounds__(kScanThreads) scan_offsets_kernel(const hg_lod_record* __restrict__ lod,
-                                                                    uint32_t count, uint32_t capacity,
-                                                                    uint32_t* __restrict__ offsets,
-                                                                    uint32_t* __restrict__ indirect,
-                                                                    const uint32_t* __restrict__ depth_key,
-                                                                    uint32_t* __restrict__ sorted,
-                                                                    uint32_t* __restrict__ sorted_off,
-                                                                    uint32_t* __restrict__ order_meta) {
+__device__ __forceinline__ void scan_offsets_block(const hg_lod_record* __restrict__ lod, uint32_t count,
+                                                   uint32_t capacity, uint32_t* __restrict__ offsets,
+                                                   uint32_t* __restrict__ indirect,
+                                                   const uint32_t* __restrict__ depth_key,
+                                                   uint32_t* __restrict__ sorted, uint32_t* __restrict__ sorted_off,
+                                                   uint32_t* __restrict__ order_meta) {
     __shared__ uint32_t warp_sums[33];
     __shared__ uint32_t carry;
     __shared__ uint32_t bucket[kDepthBuckets];
@@ -261,6 +265,17 @@ __global__ void __launch_bounds__(kScanThreads) scan_offsets_kernel(const hg_lod
         order_meta[0] = live;
         order_meta[1] = full <= capacity ? 1u : 0u;  // every ref exists, so the order is a permutation
     }
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_offsets_kernel(const hg_lod_record* __restrict__ lod,
+                                                                    uint32_t count, uint32_t capacity,
+                                                                    uint32_t* __restrict__ offsets,
+                                                                    uint32_t* __restrict__ indirect,
+                                                                    const uint32_t* __restrict__ depth_key,
+                                                                    uint32_t* __restrict__ sorted,
+                                                                    uint32_t* __restrict__ sorted_off,
+                                                                    uint32_t* __restrict__ order_meta) {
+    scan_offsets_block(lod, count, capacity, offsets, indirect, depth_key, sorted, sorted_off, order_meta);
 }
 
 // Step 2: one warp per bundle writes its StrandRefs (bundle-major order, as
@@ -512,8 +527,8 @@ __device__ __forceinline__ void generate_slot(const hg_hair_params& p, StrandSme
 // world tangents, w and ao in shared memory.  Strands at kCacheCps control
 // points come from the frame's strand cache when one is given; the DOM passes
 // need positions only.
-template <int MODE>
-__device__ __forceinline__ uint32_t generate_strand(const RasterArgs& a, StrandSmem& sm, const hg_strand_ref& ref,
+template <int MODE, class Args>
+__device__ __forceinline__ uint32_t generate_strand(const Args& a, StrandSmem& sm, const hg_strand_ref& ref,
                                                     const hg_gpu_bundle& bundle, float2 uv, uint32_t lane) {
     const hg_hair_params& p = a.p;
     const uint32_t ncp = min(max(ref.control_points, 2u), 127u);
@@ -569,7 +584,8 @@ __device__ __forceinline__ bool on_screen(int32_t x, int32_t y, int32_t w, int32
 // floor(mix(a, b, (i-1)/n)) the DDA loop carries.  Each sample computes its
 // payload once (raster.wgsl:83-108) and writes the centre pixel and, on a
 // diagonal step, the two side pixels.
-__device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& sm, uint32_t ncp, float2 uv,
+template <class Args>
+__device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uint32_t ncp, float2 uv,
                                               float beta, uint32_t lane) {
     const hg_hair_params& p = a.p;
     const int32_t nseg = (int32_t)ncp - 1;
@@ -704,8 +720,8 @@ __device__ __forceinline__ void raster_camera(const RasterArgs& a, StrandSmem& s
 
 // write_dom_pixel (raster.wgsl:118-148) for the Bresenham pixel (px, py) of
 // the segment p0-p1 (screen a -> a + seg).
-template <int MODE>
-__device__ __forceinline__ void dom_write(const RasterArgs& a, int32_t px, int32_t py, int32_t width, int32_t height,
+template <int MODE, class Args>
+__device__ __forceinline__ void dom_write(const Args& a, int32_t px, int32_t py, int32_t width, int32_t height,
                                           float2 A, float2 seg, float seg_len2, f3 p0, f3 p1) {
     const hg_hair_params& p = a.p;
     if (px < 0 || py < 0 || px >= width || py >= height) return;
@@ -736,8 +752,8 @@ __device__ __forceinline__ void dom_write(const RasterArgs& a, int32_t px, int32
 }
 
 // draw_dom_segment (raster.wgsl:150-190), one segment per lane.
-template <int MODE>
-__device__ __forceinline__ void raster_dom(const RasterArgs& a, StrandSmem& sm, uint32_t ncp, uint32_t lane) {
+template <int MODE, class Args>
+__device__ __forceinline__ void raster_dom(const Args& a, StrandSmem& sm, uint32_t ncp, uint32_t lane) {
     const hg_hair_params& p = a.p;
     const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
     for (uint32_t j = lane; j + 1u < ncp; j += 32u) {
@@ -787,37 +803,42 @@ struct GenArgs {
     uint32_t strands;
 };
 
+// Strand g of a groom into its cache slot (one warp).
+template <class Args>
+__device__ __forceinline__ void generate_one(const Args& a, uint32_t g, float4* lp, float4* lt, uint32_t lane) {
+    const uint32_t b = a.strand_bundle[g];
+    const uint32_t s = g - a.strand_base[b];
+    const hg_gpu_bundle bundle = a.bundles[b];
+    const float2 uv = pcg_uv(s ^ (b * 0x85ebca6bu));
+    f3 mp[4];
+    float wk[4], aok[4];
+    model_cps(a.layers, a.style, lp, lt, bundle, uv, kCacheCps, lane, mp, wk, aok);
+    float4* pos = a.cache + (size_t)g * (2u * kCacheCps);
+    float4* tan = pos + kCacheCps;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        f3 prev, next;
+        if (k == 0) cp_neighbours<0>(mp, lane, prev, next);
+        if (k == 1) cp_neighbours<1>(mp, lane, prev, next);
+        if (k == 2) cp_neighbours<2>(mp, lane, prev, next);
+        const uint32_t idx = lane + 32u * k;
+        if (idx < kCacheCps) {
+            const f3 wp = to_world(a.p, mp[k]);
+            const f3 wt = cp_world_tangent(a.p, idx, kCacheCps, prev, mp[k], next);
+            pos[idx] = make_float4(wp.x, wp.y, wp.z, aok[k]);
+            tan[idx] = make_float4(wt.x, wt.y, wt.z, wk[k]);
+        }
+    }
+    __syncwarp();
+}
+
 __global__ void __launch_bounds__(kRasterThreads) generate_kernel(const GenArgs a) {
     __shared__ float4 lp[kRasterWarps][16];
     __shared__ float4 lt[kRasterWarps][16];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t nwarps = gridDim.x * kRasterWarps;
-    for (uint32_t g = blockIdx.x * kRasterWarps + warp; g < a.strands; g += nwarps) {
-        const uint32_t b = a.strand_bundle[g];
-        const uint32_t s = g - a.strand_base[b];
-        const hg_gpu_bundle bundle = a.bundles[b];
-        const float2 uv = pcg_uv(s ^ (b * 0x85ebca6bu));
-        f3 mp[4];
-        float wk[4], aok[4];
-        model_cps(a.layers, a.style, lp[warp], lt[warp], bundle, uv, kCacheCps, lane, mp, wk, aok);
-        float4* pos = a.cache + (size_t)g * (2u * kCacheCps);
-        float4* tan = pos + kCacheCps;
-#pragma unroll
-        for (int k = 0; k < 3; ++k) {
-            f3 prev, next;
-            if (k == 0) cp_neighbours<0>(mp, lane, prev, next);
-            if (k == 1) cp_neighbours<1>(mp, lane, prev, next);
-            if (k == 2) cp_neighbours<2>(mp, lane, prev, next);
-            const uint32_t idx = lane + 32u * k;
-            if (idx < kCacheCps) {
-                const f3 wp = to_world(a.p, mp[k]);
-                const f3 wt = cp_world_tangent(a.p, idx, kCacheCps, prev, mp[k], next);
-                pos[idx] = make_float4(wp.x, wp.y, wp.z, aok[k]);
-                tan[idx] = make_float4(wt.x, wt.y, wt.z, wk[k]);
-            }
-        }
-        __syncwarp();
-    }
+    for (uint32_t g = blockIdx.x * kRasterWarps + warp; g < a.strands; g += nwarps)
+        generate_one(a, g, lp[warp], lt[warp], lane);
 }
 
 // raster.wgsl:225-337: one warp per strand ref, persistent over the refs.
@@ -848,6 +869,149 @@ __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) raster_kerne
     }
 }
 
+// ------------------------------------------------------------------ batched frame
+// Every pass of a batch of (groom, camera view, deep-opacity view) items in
+// one launch each.  Work is indexed across views through prefix tables; a
+// view's arguments are read in place from the device view table.
+
+// Largest v in [0, n) with prefix[v] <= x, for x < prefix[n].  Plain loads:
+// the prefix is in global memory for some callers and shared for others.
+__device__ __forceinline__ uint32_t find_view(const uint32_t* prefix, uint32_t n, uint32_t x) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (prefix[mid] <= x) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// grid (X, items): block (x, i) clears item i's deep opacity map.
+__global__ void batch_clear_dom_kernel(const BatchView* __restrict__ views, const uint32_t* __restrict__ dom_prefix,
+                                       uint32_t* __restrict__ dom) {
+    const BatchView& v = views[blockIdx.y];
+    const size_t texels = (size_t)v.dom_w * v.dom_h, words = texels * (1 + kDomLayers);
+    uint32_t* map = dom + dom_prefix[blockIdx.y];
+    for (size_t w = (size_t)blockIdx.x * blockDim.x + threadIdx.x; w < words; w += (size_t)gridDim.x * blockDim.x)
+        map[w] = w < texels ? kDomEmpty : 0u;
+}
+
+__global__ void batch_lod_kernel(const BatchView* __restrict__ views, const uint32_t* __restrict__ prefix,
+                                 uint32_t n_views, uint32_t total) {
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (w >= total) return;
+    const uint32_t v = find_view(prefix, n_views, w);
+    const BatchView& a = views[v];
+    lod_bundle(a.p, a.bundles, a.layers, a.lod, a.depth_key, w - prefix[v], lane);
+}
+
+__global__ void __launch_bounds__(kScanThreads) batch_scan_offsets_kernel(const BatchView* __restrict__ views) {
+    const BatchView& a = views[blockIdx.x];
+    scan_offsets_block(a.lod, a.count, a.capacity, a.offsets, a.indirect, nullptr, nullptr, nullptr, nullptr);
+}
+
+__global__ void batch_scan_expand_kernel(const BatchView* __restrict__ views, const uint32_t* __restrict__ prefix,
+                                         uint32_t n_views, uint32_t total) {
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (w >= total) return;
+    const uint32_t v = find_view(prefix, n_views, w);
+    const BatchView& a = views[v];
+    const uint32_t b = w - prefix[v];
+    const hg_lod_record rec = a.lod[b];
+    const uint32_t off = a.offsets[b];
+    for (uint32_t s = lane; s < rec.n_lod; s += 32u) {
+        const uint32_t i = off + s;
+        if (i >= a.capacity) break;
+        reinterpret_cast<uint4*>(a.refs)[i] = make_uint4(b, s, rec.n_lod, rec.control_points);
+    }
+}
+
+__global__ void __launch_bounds__(kRasterThreads) batch_generate_kernel(const BatchView* __restrict__ views,
+                                                                        const uint32_t* __restrict__ prefix,
+                                                                        uint32_t n_cam, uint32_t total) {
+    __shared__ float4 lp[kRasterWarps][16];
+    __shared__ float4 lt[kRasterWarps][16];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const uint32_t nwarps = gridDim.x * kRasterWarps;
+    for (uint32_t g = blockIdx.x * kRasterWarps + warp; g < total; g += nwarps) {
+        const uint32_t v = find_view(prefix, n_cam, g);
+        generate_one(views[v], g - prefix[v], lp[warp], lt[warp], lane);
+    }
+}
+
+// Persistent raster over the refs of views [first, first + n): warps take
+// `chunk` consecutive refs of the concatenated ref space at a time from a
+// global counter, so grooms of very different sizes share the SMs.  PHASE 0
+// runs camera views (pass_mode.x 0) and DOM depth views; PHASE 1 runs the
+// DOM views' layer pass.
+template <int PHASE>
+__global__ void __launch_bounds__(kRasterThreads, 6) batch_raster_kernel(const BatchView* __restrict__ views,
+                                                                         uint32_t first, uint32_t n,
+                                                                         uint32_t* __restrict__ counter,
+                                                                         uint32_t chunk) {
+    __shared__ StrandSmem smem[kRasterWarps];
+    __shared__ uint32_t prefix[kBatchMaxViews + 1];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    // prefix of the views' ref totals: warp 0, eight views per lane
+    if (warp == 0) {
+        uint32_t t[kBatchMaxViews / 32];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int k = 0; k < (int)(kBatchMaxViews / 32); ++k) {
+            const uint32_t v = lane * (kBatchMaxViews / 32) + k;
+            t[k] = v < n ? min(views[first + v].indirect[0], views[first + v].capacity) : 0u;
+            sum += t[k];
+        }
+        uint32_t incl = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        uint32_t run = incl - sum;
+#pragma unroll
+        for (int k = 0; k < (int)(kBatchMaxViews / 32); ++k) {
+            prefix[lane * (kBatchMaxViews / 32) + k] = run;
+            run += t[k];
+        }
+        if (lane == 31) prefix[kBatchMaxViews] = incl;
+    }
+    __syncthreads();
+    const uint32_t total = prefix[kBatchMaxViews];
+    StrandSmem& sm = smem[warp];
+    uint32_t v = 0;
+    for (;;) {
+        uint32_t start = 0;
+        if (lane == 0) start = atomicAdd(counter, chunk);
+        start = __shfl_sync(0xffffffffu, start, 0);
+        if (start >= total) break;
+        const uint32_t end = min(start + chunk, total);
+        for (uint32_t r = start; r < end; ++r) {
+            if (r < prefix[v] || r >= prefix[v + 1]) v = find_view(prefix, n, r);
+            const BatchView& a = views[first + v];
+            const hg_strand_ref ref = a.refs[r - prefix[v]];
+            if (ref.bundle >= a.bundle_count) {
+                if (lane == 0) atomicOr(a.err, kErrBadRef);
+                continue;
+            }
+            const hg_gpu_bundle bundle = a.bundles[ref.bundle];
+            const float2 uv = pcg_uv(ref.strand ^ (ref.bundle * 0x85ebca6bu));
+            if (PHASE == 1) {
+                const uint32_t ncp = generate_strand<2>(a, sm, ref, bundle, uv, lane);
+                raster_dom<2>(a, sm, ncp, lane);
+            } else if (a.p.pass_mode[0] == 0u) {
+                const uint32_t ncp = generate_strand<0>(a, sm, ref, bundle, uv, lane);
+                float beta = __fdiv_rn(__uint2float_rn(ref.n_lod), __uint2float_rn(max(bundle.strand_count, 1u)));
+                raster_camera(a, sm, ncp, uv, beta, lane);
+            } else {
+                const uint32_t ncp = generate_strand<1>(a, sm, ref, bundle, uv, lane);
+                raster_dom<1>(a, sm, ncp, lane);
+            }
+            __syncwarp();
+        }
+    }
+}
+
 int blocks_for(hg_ctx* ctx, const void* fn, int threads, size_t work_items, int per_block_items) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
@@ -856,6 +1020,25 @@ int blocks_for(hg_ctx* ctx, const void* fn, int threads, size_t work_items, int 
     size_t cap = (size_t)ctx->sm_count * per_sm;
     size_t b = need < cap ? need : cap;
     return b < 1 ? 1 : (int)b;
+}
+
+// Screen targets of every camera view (contiguous arenas) and every deep
+// opacity map.
+cudaError_t launch_clear_arena(hg_ctx* ctx, const BatchDev& b) {
+    const int threads = 256;
+    if (b.total_px) {
+        const int blocks = (int)std::min<uint64_t>((b.total_px / 4 + threads - 1) / threads + 1,
+                                                   (uint64_t)ctx->sm_count * 8);
+        clear_kernel<<<blocks, threads, 0, ctx->stream>>>(b.center, b.cons, b.beta, b.total_px);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (b.total_dom_words) {
+        dim3 grid(std::max(1, 4 * ctx->sm_count / (int)std::max(b.n_cam, 1u)), b.n_cam);
+        batch_clear_dom_kernel<<<grid, threads, 0, ctx->stream>>>(b.views, b.dom_prefix, b.dom);
+        return cudaGetLastError();
+    }
+    return cudaSuccess;
 }
 
 }  // namespace
@@ -949,12 +1132,8 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
     a.err = ctx->err;
     a.bundle_count = g->bundle_count;
     uint32_t mode = p.pass_mode[0];
-    const void* fn = mode == 0 ? (const void*)raster_kernel<0>
-                     : mode == 1 ? (const void*)raster_kernel<1>
-                                 : (const void*)raster_kernel<2>;
     // One warp per ref slot, no persistence: raster launches on different
     // streams then share the SMs through the block scheduler.
-    (void)fn;
     int blocks = (int)std::max<size_t>((g->ref_capacity + kRasterWarps - 1) / kRasterWarps, 1);
     if (mode == 0) {
         raster_kernel<0><<<blocks, kRasterThreads, 0, ctx->stream>>>(a);
@@ -964,6 +1143,61 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
         raster_kernel<2><<<blocks, kRasterThreads, 0, ctx->stream>>>(a);
     }
     return cudaGetLastError();
+}
+
+cudaError_t launch_batch_setup(hg_ctx* ctx, const BatchDev& b) {
+    cudaError_t e = launch_clear_arena(ctx, b);
+    if (e != cudaSuccess) return e;
+    const int threads = 256;
+    if (b.total_bundles) {
+        const uint32_t blocks = (b.total_bundles * 32u + threads - 1) / threads;
+        batch_lod_kernel<<<blocks, threads, 0, ctx->stream>>>(b.views, b.bundle_prefix, b.n_views, b.total_bundles);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    batch_scan_offsets_kernel<<<b.n_views, kScanThreads, 0, ctx->stream>>>(b.views);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (b.total_bundles) {
+        const uint32_t blocks = (b.total_bundles * 32u + threads - 1) / threads;
+        batch_scan_expand_kernel<<<blocks, threads, 0, ctx->stream>>>(b.views, b.bundle_prefix, b.n_views,
+                                                                      b.total_bundles);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    if (b.total_strands) {
+        const uint32_t need = (b.total_strands + kRasterWarps - 1) / kRasterWarps;
+        const uint32_t blocks = std::max(1u, std::min(need, b.gen_blocks));
+        batch_generate_kernel<<<blocks, kRasterThreads, 0, ctx->stream>>>(b.views, b.strand_prefix, b.n_cam,
+                                                                          b.total_strands);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// Resident blocks per SM of the batched raster and generate kernels (queried
+// once, outside any stream capture).
+cudaError_t batch_occupancy(uint32_t* raster_per_sm, uint32_t* gen_per_sm) {
+    int r = 0, g = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, batch_raster_kernel<0>, kRasterThreads, 0);
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g, batch_generate_kernel, kRasterThreads, 0);
+    *raster_per_sm = (uint32_t)std::max(r, 1);
+    *gen_per_sm = (uint32_t)std::max(g, 1);
+    return e;
+}
+
+cudaError_t launch_batch_raster(hg_ctx* ctx, const BatchDev& b) {
+    cudaError_t e = cudaMemsetAsync(b.counters, 0, 2 * sizeof(uint32_t), ctx->stream);
+    if (e != cudaSuccess) return e;
+    const uint32_t per_sm = std::max(1u, b.raster_blocks_per_sm);
+    const int blocks = ctx->sm_count * (int)per_sm;
+    const uint32_t chunk = b.raster_chunk ? b.raster_chunk : 1u;
+    batch_raster_kernel<0><<<blocks, kRasterThreads, 0, ctx->stream>>>(b.views, 0u, b.n_views, b.counters, chunk);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if (b.n_views > b.n_cam) {
+        batch_raster_kernel<1><<<blocks, kRasterThreads, 0, ctx->stream>>>(b.views, b.n_cam, b.n_views - b.n_cam,
+                                                                           b.counters + 1, chunk);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
 }
 
 }  // namespace hg

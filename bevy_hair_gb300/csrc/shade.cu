@@ -277,13 +277,14 @@ struct ShadeArgs {
     float exposure;
 };
 
-// fs (shade.wesl:523-593).  Lights arrive sorted by kind (point, spot,
-// directional, rect), the order the reference's loops visit them.
-__global__ void __launch_bounds__(256, 3) shade_kernel(const ShadeArgs a) {
+// fs (shade.wesl:523-593) for pixel (x, y) of view v (fields p, center,
+// beta, dom, shaded, shaded_depth).  Lights arrive sorted by kind (point,
+// spot, directional, rect), the order the reference's loops visit them.
+template <class V>
+__device__ __forceinline__ void shade_pixel(const V& a, const hg_light* __restrict__ lights, uint32_t n_lights,
+                                            uint32_t ortho, float exposure, uint32_t x, uint32_t y) {
     const hg_hair_params& p = a.p;
     const uint32_t width = f2u(p.screen[0]), height = f2u(p.screen[1]);
-    const uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= width || y >= height) return;
     const uint32_t pix = y * width + x;
     const unsigned long long word = __ldg(&a.center[pix]);
@@ -304,7 +305,7 @@ __global__ void __launch_bounds__(256, 3) shade_kernel(const ShadeArgs a) {
     const float ascale = 0.65f + 0.35f * uvw_z;
     const f3 albedo = {p.albedo[0] * ascale, p.albedo[1] * ascale, p.albedo[2] * ascale};
     f3 view;
-    if (a.ortho) {
+    if (ortho) {
         view = safe_normalize(mk3(p.clip_from_world[2], p.clip_from_world[6], p.clip_from_world[10]));
     } else {
         view = safe_normalize(sub3(ld3(p.camera_pos), world));
@@ -318,8 +319,8 @@ __global__ void __launch_bounds__(256, 3) shade_kernel(const ShadeArgs a) {
     const Dual ds = dual_scatter(cos_theta_o, sigma_a, shape);
     f3 color = spl(0.0f);
     bool dom_left = true;
-    for (uint32_t i = 0; i < a.n_lights; ++i) {
-        const hg_light& L = a.lights[i];
+    for (uint32_t i = 0; i < n_lights; ++i) {
+        const hg_light& L = lights[i];
         const uint32_t kind = L.kind;
         if (kind == HG_LIGHT_POINT || kind == HG_LIGHT_SPOT) {
             f3 to_l = sub3(ld3(L.position), world);
@@ -359,9 +360,32 @@ __global__ void __launch_bounds__(256, 3) shade_kernel(const ShadeArgs a) {
             }
         }
     }
-    color = mul3s(color, a.exposure);
+    color = mul3s(color, exposure);
     a.shaded[pix] = make_float4(color.x, color.y, color.z, 1.0f);
     a.shaded_depth[pix] = view_dist;
+}
+
+__global__ void __launch_bounds__(256, 3) shade_kernel(const ShadeArgs a) {
+    shade_pixel(a, a.lights, a.n_lights, a.ortho, a.exposure, blockIdx.x * blockDim.x + threadIdx.x,
+                blockIdx.y * blockDim.y + threadIdx.y);
+}
+
+// Batched: one tile (blockDim.x x blockDim.y pixels) of one camera view per block.
+__global__ void __launch_bounds__(256, 3) batch_shade_kernel(const BatchView* __restrict__ views,
+                                                             const uint32_t* __restrict__ tile_prefix, uint32_t n_cam,
+                                                             const hg_light* __restrict__ lights, uint32_t n_lights,
+                                                             uint32_t ortho, float exposure) {
+    uint32_t lo = 0, hi = n_cam;
+    while (hi - lo > 1u) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (tile_prefix[mid] <= blockIdx.x) lo = mid;
+        else hi = mid;
+    }
+    const BatchView& v = views[lo];
+    const uint32_t t = blockIdx.x - tile_prefix[lo];
+    const uint32_t tiles_x = (v.width + blockDim.x - 1) / blockDim.x;
+    shade_pixel(v, lights, n_lights, ortho, exposure, (t % tiles_x) * blockDim.x + threadIdx.x,
+                (t / tiles_x) * blockDim.y + threadIdx.y);
 }
 
 // The learned-surrogate variant of fs: the network gives R, TT, TRT and the
@@ -599,6 +623,14 @@ cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights
     dim3 block(32, 8);
     dim3 grid((ctx->width + 31) / 32, (ctx->height + 7) / 8);
     shade_kernel<<<grid, block, 0, ctx->stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_batch_shade(hg_ctx* ctx, const BatchDev& b) {
+    if (!b.total_tiles) return cudaSuccess;
+    dim3 block(b.tile_w, b.tile_h);
+    batch_shade_kernel<<<b.total_tiles, block, 0, ctx->stream>>>(b.views, b.tile_prefix, b.n_cam, b.lights,
+                                                                  b.n_lights, b.ortho, b.exposure);
     return cudaGetLastError();
 }
 

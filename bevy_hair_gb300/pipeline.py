@@ -99,6 +99,91 @@ class GpuGroom:
             self.handle = None
 
 
+class HairBatch:
+    """hg_batch: many grooms with their own camera views and deep opacity maps,
+    one launch per pass, replayed as a CUDA graph."""
+
+    def __init__(self, renderer: "HairRenderer", grooms: list["GpuGroom"], sizes: list[tuple[int, int, int, int]]):
+        self.renderer, self.lib = renderer, renderer.lib
+        items = (abi.BatchItem * len(grooms))()
+        for k, (g, (w, h, dw, dh)) in enumerate(zip(grooms, sizes)):
+            items[k] = abi.BatchItem(g.handle.value, w, h, dw, dh)
+        handle = C.c_void_p()
+        _check(self.lib, renderer.ctx, self.lib.hg_batch_create(renderer.ctx, items, len(grooms), C.byref(handle)))
+        self.handle, self.sizes, self.grooms = handle, list(sizes), list(grooms)
+        if not hasattr(renderer, "_batches"):
+            renderer._batches = []
+        renderer._batches.append(self)
+
+    def _check(self, status: int) -> None:
+        _check(self.lib, self.renderer.ctx, status)
+
+    def set_params(self, item: int, camera: np.ndarray, dom: np.ndarray | None) -> None:
+        self._check(self.lib.hg_batch_set_params(self.handle, item, camera.ctypes.data,
+                                                 dom.ctypes.data if dom is not None else None))
+
+    @staticmethod
+    def _desc(lights: np.ndarray, exposure: float, ortho: bool) -> tuple[abi.ShadeDesc, np.ndarray]:
+        lights = np.ascontiguousarray(lights, dtype=abi.LIGHT)
+        return abi.ShadeDesc(abi.ptr(lights) if len(lights) else None, len(lights), int(ortho), exposure, 0), lights
+
+    def frame(self, lights: np.ndarray, mode: int = abi.BATCH_GRAPH, exposure: float = 1.0,
+              ortho: bool = False) -> None:
+        d, keep = self._desc(lights, exposure, ortho)
+        self._check(self.lib.hg_batch_frame(self.handle, C.byref(d), mode))
+
+    def profile(self, lights: np.ndarray, exposure: float = 1.0) -> dict:
+        """Per-phase milliseconds of one directly launched batched frame."""
+        d, keep = self._desc(lights, exposure, False)
+        ms = np.zeros(4, dtype=np.float32)
+        self._check(self.lib.hg_batch_profile(self.handle, C.byref(d), ms.ctypes.data))
+        return dict(zip(("setup", "raster", "shade", "filter_composite"), (round(float(v), 4) for v in ms)))
+
+    def launches(self, mode: int) -> int:
+        n = C.c_uint32()
+        self._check(self.lib.hg_batch_launches(self.handle, mode, C.byref(n)))
+        return int(n.value)
+
+    def tune(self, lights: np.ndarray, exposure: float = 1.0) -> list[dict]:
+        d, keep = self._desc(lights, exposure, False)
+        res = (abi.BatchTuning * 64)()
+        n = C.c_uint32()
+        self._check(self.lib.hg_batch_tune(self.handle, C.byref(d), res, 64, C.byref(n)))
+        return [res[k].as_dict() for k in range(min(int(n.value), 64))]
+
+    def tuning(self) -> dict:
+        t = abi.BatchTuning()
+        self._check(self.lib.hg_batch_get_tuning(self.handle, C.byref(t)))
+        return t.as_dict()
+
+    def set_tuning(self, **kw) -> None:
+        t = abi.BatchTuning()
+        self._check(self.lib.hg_batch_get_tuning(self.handle, C.byref(t)))
+        for k, v in kw.items():
+            setattr(t, k, v)
+        self._check(self.lib.hg_batch_set_tuning(self.handle, C.byref(t)))
+
+    def buffer(self, item: int, which: int) -> tuple[int, int]:
+        p, n = C.c_void_p(), C.c_size_t()
+        self._check(self.lib.hg_batch_buffer(self.handle, item, which, C.byref(p), C.byref(n)))
+        return p.value or 0, n.value
+
+    def read(self, item: int, which: int) -> np.ndarray:
+        _, nbytes = self.buffer(item, which)
+        dt = HairRenderer._DTYPES[which]
+        out = np.empty(nbytes // np.dtype(dt).itemsize, dtype=dt)
+        if nbytes:
+            self._check(self.lib.hg_batch_copy_out(self.handle, item, which, abi.ptr(out), out.nbytes))
+        return out
+
+    def close(self) -> None:
+        if self.handle:
+            self.lib.hg_batch_destroy(self.handle)
+            self.handle = None
+            if self in getattr(self.renderer, "_batches", []):
+                self.renderer._batches.remove(self)
+
+
 class HairRenderer:
     """One hairgb context: targets, grooms and the passes of hair_pass."""
 
@@ -208,7 +293,7 @@ class HairRenderer:
 
     def close(self) -> None:
         if self.ctx:
-            for s in list(getattr(self, "_surrogates", ())):
+            for s in list(getattr(self, "_surrogates", ())) + list(getattr(self, "_batches", ())):
                 s.close()
             self.lib.hg_destroy(self.ctx)
             self.ctx = None

@@ -331,6 +331,79 @@ hg_status hg_hair_visibility(hg_ctx* ctx, const hg_shadow_light* light, const fl
 hg_status hg_scan_noalloc(const hg_lod_record* lod, uint32_t bundle_count, uint32_t capacity,
                           hg_strand_ref* refs, uint32_t* indirect, void* stream);
 
+/* ---------------------------------------------------------------- batched frames */
+
+/* Many independent grooms, each with its own camera view and deep opacity
+ * map, drawn as one batch: every pass runs as one launch over all items (the
+ * camera and DOM-depth rasters of all items share one persistent launch whose
+ * warps take strand refs from a global counter), and the whole frame is
+ * captured once into a CUDA graph and replayed.  This has no counterpart in
+ * the reference, which records one hair_pass per groom
+ * (src/render/pass.rs:259-657); per item the results are those of
+ * hg_groom_frame with the item's params: visibility bit for bit, colour to
+ * the last bit of the same kernels' arithmetic.
+ *
+ * A batch owns every item's targets (one arena per buffer kind) and keeps a
+ * pinned copy of the items' uniforms that the graph uploads at replay.  Each
+ * groom may appear in one item only (its strand cache holds one transform). */
+#define HG_BATCH_MAX_ITEMS 128u
+
+typedef struct hg_batch hg_batch;
+
+typedef struct hg_batch_item {
+    hg_groom* groom;
+    uint32_t width, height;   /* camera targets, 1..16384 */
+    uint32_t dom_w, dom_h;    /* deep opacity map, 1..16384, or 0 x 0 for none */
+} hg_batch_item;
+
+/* Launch shapes the autotuner chooses among. */
+typedef struct hg_batch_tuning {
+    uint32_t raster_chunk;          /* strand refs a warp takes per grab, 1..64 */
+    uint32_t raster_blocks_per_sm;  /* persistent raster grid = SMs x this, 1..resident limit */
+    uint32_t tile_w, tile_h;        /* shade / composite pixel tile: tile_w in {16, 32, 64}, tile_w * tile_h == 256 */
+    uint32_t filter_tile;           /* 0: 32 x 8, 1: 16 x 16 */
+    float ms;                       /* output of hg_batch_tune: measured frame time of this shape */
+} hg_batch_tuning;
+
+typedef enum hg_batch_mode {
+    HG_BATCH_GRAPH = 0,     /* replay the captured graph (recaptured when shapes or shade settings change) */
+    HG_BATCH_LAUNCHES = 1,  /* the same batched launches issued directly */
+    HG_BATCH_SEPARATE = 2   /* hg_groom_frame per item (the unbatched path, for comparison) */
+} hg_batch_mode;
+
+hg_status hg_batch_create(hg_ctx* ctx, const hg_batch_item* items, uint32_t count, hg_batch** out);
+void hg_batch_destroy(hg_batch* batch);
+/* Uniforms of one item: camera params (pass_mode.x 0, screen = the item's
+ * size) and, when the item has a map, DOM params (pass_mode.x 1, screen and
+ * dom_info = the map size; camera flags[3] must be 1).  All items must agree
+ * on flags[1] (filter) and pass_mode.z (reverse Z).  Waits for the previous
+ * frame to finish reading the pinned uniforms. */
+hg_status hg_batch_set_params(hg_batch* batch, uint32_t item, const hg_hair_params* camera,
+                              const hg_hair_params* dom);
+/* One frame of every item: clear, lod, scan, generate, raster (camera + DOM
+ * depth, then DOM layers), shade, filter, clear colour, composite.  shade:
+ * lights as for hg_shade (shade_model 0 only).  Every item's params must have
+ * been set. */
+hg_status hg_batch_frame(hg_batch* batch, const hg_shade_desc* shade, hg_batch_mode mode);
+/* One frame of batched launches with events between its phases: ms[0..4) =
+ * setup (clears, lod, scan, generate), raster (camera + DOM depth, DOM
+ * layers), shade, filter + colour clear + composite.  Synchronous. */
+hg_status hg_batch_profile(hg_batch* batch, const hg_shade_desc* shade, float* ms);
+/* Kernel launches one frame issues in `mode`. */
+hg_status hg_batch_launches(hg_batch* batch, hg_batch_mode mode, uint32_t* launches);
+/* Autotuner: times graph frames over a set of launch shapes (coordinate
+ * search over raster chunk x grid, pixel tile, filter tile), keeps the
+ * fastest, and reports every shape tried in results[0..*count) (up to
+ * capacity). */
+hg_status hg_batch_tune(hg_batch* batch, const hg_shade_desc* shade, hg_batch_tuning* results, uint32_t capacity,
+                        uint32_t* count);
+hg_status hg_batch_set_tuning(hg_batch* batch, const hg_batch_tuning* tuning);
+hg_status hg_batch_get_tuning(hg_batch* batch, hg_batch_tuning* tuning);
+/* An item's target (the hg_buffer_id kinds) as a device pointer and size. */
+hg_status hg_batch_buffer(hg_batch* batch, uint32_t item, hg_buffer_id which, void** ptr, size_t* bytes);
+/* Copy an item's target to host memory (bytes must equal its size); synchronous. */
+hg_status hg_batch_copy_out(hg_batch* batch, uint32_t item, hg_buffer_id which, void* host, size_t bytes);
+
 /* ---------------------------------------------------------------- learned shading surrogate */
 
 /* A small network that stands in for the Karis-fit lobes of shade.wesl:94-190
