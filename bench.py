@@ -39,7 +39,8 @@ sys.path.insert(0, str(ROOT))
 L2_FLUSH_BYTES = 256 << 20
 MEASURED_PEAKS = ROOT / "MEASURED_PEAKS.json"
 WORKLOAD = ("config2: 100k wavy strands x 64 segs (seeded synthetic, baked), 1920x1080, DOM 1024^2 x16, "
-            "key directional + 8 point lights, LOD on (lambda 3), filter on, composite")
+            "key directional + 8 point lights, LOD on (lambda 3), light probe (seeded 512^2 x 9-level RGB9E5 sky), "
+            "filter on, composite")
 METRIC = "Gseg/s at 1080p, 6.4M segs (whole hair frame: raster + DOM + shade + filter + composite)"
 
 
@@ -190,6 +191,22 @@ def peaks() -> tuple[float, str]:
         return float(p["hbm_gbs"]), "measured"
     except (OSError, KeyError, ValueError):
         return 6800.0, "fallback"
+
+
+_ENV = {}
+
+
+def bench_env(config: int):
+    """Config 2's light probe ("env lookup on"): a seeded 512^2 x 9-level
+    procedural sky in the reference probes' RGB9E5 format (the reference's own
+    KTX2 asset is not available where the bench runs)."""
+    if config != 2:
+        return None
+    if "env" not in _ENV:
+        from bevy_hair_gb300 import envmap
+
+        _ENV["env"] = envmap.procedural()
+    return _ENV["env"]
 
 
 def tensor_peak() -> tuple[float, str]:
@@ -423,6 +440,7 @@ def run_ours(args, rank, world, local):
     lights = sc.light_array()
     r = HairRenderer(local, stream.cuda_stream)
     r.ensure_targets(sc.view.width, sc.view.height, *sc.dom_size)
+    r.set_environment(bench_env(args.config))
     g = r.upload(sc.mesh)
 
     # one frame to count the work it does
@@ -495,8 +513,10 @@ def run_ours(args, rank, world, local):
     per_pass = {p: round(v, 4) for p, v in acc.items()}
     surr = None if args.no_surrogate else surrogate_section(r, cam, lights, flush, stream, reps, acc["shade"],
                                                              hair_px)
-    batch = None if args.no_batch else batch_measure(r, stream, flush, max(5, min(args.steps, 10)), 3,
-                                                     args.batch_scale)
+    batch = None
+    if not args.no_batch:
+        r.set_environment(None)  # config 4 has no light probe
+        batch = batch_measure(r, stream, flush, max(5, min(args.steps, 10)), 3, args.batch_scale)
     nbytes = pass_bytes(sc, {"camera_refs": ref_c, "dom_refs": ref_d, "hair_pixels": hair_px,
                              "strands": sc.mesh.strand_count()})
     dominant = max((p for p in nbytes), key=lambda p: acc[p])
@@ -605,13 +625,11 @@ def cpu_baseline(args, sample: bool) -> dict:
     scale = args.cpu_scale
     threads = os.cpu_count() or 1
     oracle.set_threads(threads)
-    if args.config == 4:
-        return run_reference_batch(args, world, threads)
     sc = configs.CONFIGS[args.config](scale)
     cam, dom = sc.params()
     lights = sc.light_array()
     t = time.perf_counter()
-    out = oracle.frame(sc.mesh, cam, dom, lights)
+    out = oracle.frame(sc.mesh, cam, dom, lights, env=bench_env(args.config))
     dt = time.perf_counter() - t
     segs = int(out["counts_camera"]["segments"])
     return {"value": round(segs / dt / 1e9, 6), "unit": "Gseg/s", "cores": threads, "kind": "port",
@@ -672,15 +690,16 @@ def run_reference(args, rank, world):
     sc = configs.CONFIGS[args.config](scale)
     cam, dom = sc.params()
     lights = sc.light_array()
+    env = bench_env(args.config)
     for _ in range(min(args.warmup, 1)):
-        oracle.frame(sc.mesh, cam, dom, lights)
+        oracle.frame(sc.mesh, cam, dom, lights, env=env)
     steps = args.steps
     t = time.perf_counter()
     budget = 150.0
     done = 0
     segs = 0
     for _ in range(steps):
-        out = oracle.frame(sc.mesh, cam, dom, lights)
+        out = oracle.frame(sc.mesh, cam, dom, lights, env=env)
         segs += int(out["counts_camera"]["segments"])
         done += 1
         if time.perf_counter() - t > budget:

@@ -104,6 +104,19 @@ class FrameDesc(C.Structure):
     ]
 
 
+class EnvDesc(C.Structure):
+    _fields_ = [
+        ("specular", C.c_void_p),
+        ("specular_size", C.c_uint32),
+        ("specular_levels", C.c_uint32),
+        ("diffuse", C.c_void_p),
+        ("diffuse_size", C.c_uint32),
+        ("diffuse_levels", C.c_uint32),
+        ("rotation", C.c_float * 4),
+        ("intensity", C.c_float),
+    ]
+
+
 class BatchItem(C.Structure):
     _fields_ = [
         ("groom", C.c_void_p),
@@ -177,6 +190,7 @@ _SIGNATURES = {
     "hg_mlp_train_step": (_I32, [_VP, _VP, _VP, _U32, _F32, _VP]),
     "hg_mlp_bind": (_I32, [_VP, _VP]),
     "hg_karis_lobes": (_I32, [_VP, _VP, _U32, _F32, _VP]),
+    "hg_env_set": (_I32, [_VP, C.POINTER(EnvDesc)]),
     "hg_batch_create": (_I32, [_VP, _VP, _U32, C.POINTER(_VP)]),
     "hg_batch_destroy": (None, [_VP]),
     "hg_batch_set_params": (_I32, [_VP, _U32, _VP, _VP]),

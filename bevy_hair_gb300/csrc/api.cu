@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -161,6 +162,8 @@ hg_status hg_destroy(hg_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     free_targets(ctx);
+    free_dev(ctx->env_spec);
+    free_dev(ctx->env_diff);
     free_dev(ctx->err);
     free_dev(ctx->lights);
     if (ctx->lights_host) cudaFreeHost(ctx->lights_host);
@@ -174,6 +177,58 @@ hg_status hg_destroy(hg_ctx* ctx) {
         if (ev) cudaEventDestroy(ev);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
+    return HG_OK;
+}
+
+// Texels of a cubemap mip chain: six faces of max(size >> l, 1)^2 per level.
+static size_t cube_texels(uint32_t size, uint32_t levels) {
+    size_t n = 0;
+    for (uint32_t l = 0; l < levels; ++l) {
+        const size_t s = std::max<size_t>(size >> l, 1);
+        n += 6 * s * s;
+    }
+    return n;
+}
+
+static bool cube_shape_ok(uint32_t size, uint32_t levels) {
+    if (size < 1 || size > 4096 || levels < 1) return false;
+    uint32_t max_levels = 1;
+    while ((size >> max_levels) > 0) ++max_levels;
+    return levels <= max_levels;
+}
+
+hg_status hg_env_set(hg_ctx* ctx, const hg_env_desc* env) {
+    if (!ctx) return HG_INVALID_ARG;
+    cudaSetDevice(ctx->device);
+    if (!env) {
+        HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        free_dev(ctx->env_spec);
+        free_dev(ctx->env_diff);
+        ctx->env_spec_size = ctx->env_spec_levels = ctx->env_diff_size = ctx->env_diff_levels = 0;
+        return HG_OK;
+    }
+    if (!env->specular || !env->diffuse) return fail(ctx, HG_INVALID_ARG, "null cubemap texels");
+    if (!cube_shape_ok(env->specular_size, env->specular_levels) ||
+        !cube_shape_ok(env->diffuse_size, env->diffuse_levels))
+        return fail(ctx, HG_INVALID_ARG, "cubemap size must be 1..4096 with 1..1+log2(size) levels");
+    for (float v : {env->rotation[0], env->rotation[1], env->rotation[2], env->rotation[3], env->intensity})
+        if (!std::isfinite(v)) return fail(ctx, HG_INVALID_ARG, "non-finite probe rotation or intensity");
+    HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    free_dev(ctx->env_spec);
+    free_dev(ctx->env_diff);
+    ctx->env_spec_size = ctx->env_spec_levels = ctx->env_diff_size = ctx->env_diff_levels = 0;
+    const size_t ns = cube_texels(env->specular_size, env->specular_levels);
+    const size_t nd = cube_texels(env->diffuse_size, env->diffuse_levels);
+    HG_CUDA(ctx, cudaMalloc((void**)&ctx->env_spec, ns * 4));
+    HG_CUDA(ctx, cudaMalloc((void**)&ctx->env_diff, nd * 4));
+    HG_CUDA(ctx, cudaMemcpy(ctx->env_spec, env->specular, ns * 4, cudaMemcpyHostToDevice));
+    HG_CUDA(ctx, cudaMemcpy(ctx->env_diff, env->diffuse, nd * 4, cudaMemcpyHostToDevice));
+    ctx->env_spec_size = env->specular_size;
+    ctx->env_spec_levels = env->specular_levels;
+    ctx->env_diff_size = env->diffuse_size;
+    ctx->env_diff_levels = env->diffuse_levels;
+    std::memcpy(ctx->env_rot, env->rotation, sizeof(ctx->env_rot));
+    ctx->env_intensity = env->intensity;
     return HG_OK;
 }
 

@@ -81,6 +81,12 @@ struct hg_ctx {
     cudaEvent_t ev_fork = nullptr, ev_gen = nullptr, ev_join = nullptr;
     int sm_count = 0;
     hg_mlp* surrogate = nullptr;   // bound by hg_mlp_bind, used by shade_model 1
+    // light probe (hg_env_set): RGB9E5 mip chains, six faces per level
+    uint32_t* env_spec = nullptr;
+    uint32_t* env_diff = nullptr;
+    uint32_t env_spec_size = 0, env_spec_levels = 0, env_diff_size = 0, env_diff_levels = 0;
+    float env_rot[4] = {0.0f, 0.0f, 0.0f, 1.0f};
+    float env_intensity = 0.0f;
     std::string last_error;
 };
 

@@ -207,6 +207,129 @@ __device__ f3 hair_bsdf(f3 tangent, f3 view, f3 light, f3 sigma_a, const Shape& 
     return color;
 }
 
+// ---------------------------------------------------------------- light probe
+// probe_radiance (shade.wesl:330-427, the ENVIRONMENT_MAP specialization)
+// over RGB9E5 cubemaps: major-axis face selection, bilinear within the face
+// with clamp-to-edge, linear between mip levels.
+
+struct EnvArgs {
+    const uint32_t* spec;
+    const uint32_t* diff;
+    uint32_t spec_size, spec_levels, diff_size, diff_levels;
+    float rot[4];
+    float intensity;
+};
+
+__device__ __forceinline__ f3 rgb9e5(uint32_t w) {
+    const int e = (int)(w >> 27) - 24;
+    return {ldexpf((float)(w & 0x1ffu), e), ldexpf((float)((w >> 9) & 0x1ffu), e),
+            ldexpf((float)((w >> 18) & 0x1ffu), e)};
+}
+
+// Direction -> face (+X -X +Y -Y +Z -Z) and (s, t) in [0, 1].
+__device__ __forceinline__ int cube_face_uv(f3 d, float& s, float& t) {
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    int face;
+    float ma, sc, tc;
+    if (ax >= ay && ax >= az) {
+        face = d.x >= 0.0f ? 0 : 1;
+        ma = ax;
+        sc = d.x >= 0.0f ? -d.z : d.z;
+        tc = -d.y;
+    } else if (ay >= az) {
+        face = d.y >= 0.0f ? 2 : 3;
+        ma = ay;
+        sc = d.x;
+        tc = d.y >= 0.0f ? d.z : -d.z;
+    } else {
+        face = d.z >= 0.0f ? 4 : 5;
+        ma = az;
+        sc = d.z >= 0.0f ? d.x : -d.x;
+        tc = -d.y;
+    }
+    const float inv = 1.0f / fmaxf(ma, 1e-20f);
+    s = 0.5f * (sc * inv + 1.0f);
+    t = 0.5f * (tc * inv + 1.0f);
+    return face;
+}
+
+__device__ __forceinline__ f3 cube_bilinear(const uint32_t* __restrict__ level, uint32_t n, int face, float s,
+                                            float t) {
+    const float u = s * (float)n - 0.5f, v = t * (float)n - 0.5f;
+    const float fu = floorf(u), fv = floorf(v);
+    const float wu = u - fu, wv = v - fv;
+    const int last = (int)n - 1;
+    const int x0 = min(max((int)fu, 0), last), x1 = min(max((int)fu + 1, 0), last);
+    const int y0 = min(max((int)fv, 0), last), y1 = min(max((int)fv + 1, 0), last);
+    const uint32_t* f = level + (size_t)face * n * n;
+    const f3 c00 = rgb9e5(__ldg(f + y0 * n + x0)), c10 = rgb9e5(__ldg(f + y0 * n + x1));
+    const f3 c01 = rgb9e5(__ldg(f + y1 * n + x0)), c11 = rgb9e5(__ldg(f + y1 * n + x1));
+    const f3 a = add3(mul3s(c00, 1.0f - wu), mul3s(c10, wu));
+    const f3 b = add3(mul3s(c01, 1.0f - wu), mul3s(c11, wu));
+    return add3(mul3s(a, 1.0f - wv), mul3s(b, wv));
+}
+
+__device__ f3 sample_cube(const uint32_t* __restrict__ texels, uint32_t size, uint32_t levels, f3 dir, float lod) {
+    float s, t;
+    const int face = cube_face_uv(dir, s, t);
+    lod = clampf(lod, 0.0f, (float)(levels - 1));
+    const uint32_t l0 = (uint32_t)lod, l1 = min(l0 + 1u, levels - 1u);
+    const float w = lod - (float)l0;
+    size_t off = 0;
+    for (uint32_t l = 0; l < l0; ++l) {
+        const size_t n = max(size >> l, 1u);
+        off += 6 * n * n;
+    }
+    const uint32_t n0 = max(size >> l0, 1u);
+    const f3 a = cube_bilinear(texels + off, n0, face, s, t);
+    if (l1 == l0 || w <= 0.0f) return a;
+    off += 6 * (size_t)n0 * n0;
+    const f3 b = cube_bilinear(texels + off, max(size >> l1, 1u), face, s, t);
+    return add3(mul3s(a, 1.0f - w), mul3s(b, w));
+}
+
+// quat_rotate + the left-handed flip (shade.wesl:329-339)
+__device__ __forceinline__ f3 cubemap_dir(const float q[4], f3 dir) {
+    const f3 qv = {q[0], q[1], q[2]};
+    const f3 t = mul3s(cross3(qv, dir), 2.0f);
+    f3 r = add3(add3(dir, mul3s(t, q[3])), cross3(qv, t));
+    r.z = -r.z;
+    return r;
+}
+
+// scatter_tint (shade.wesl:81-85) with luminance (:62-64)
+__device__ __forceinline__ f3 scatter_tint(f3 albedo, float shadow) {
+    const float lum = albedo.x * 0.2126f + albedo.y * 0.7152f + albedo.z * 0.0722f;
+    const f3 hue = mul3s(albedo, 1.0f / fmaxf(lum, 1e-4f));
+    const float e = 0.5f - 0.5f * clampf(shadow, 0.0f, 1.0f);
+    return {powf(hue.x, e), powf(hue.y, e), powf(hue.z, e)};
+}
+
+__device__ f3 probe_radiance(const EnvArgs& env, f3 tangent, f3 fiber_n, f3 view, f3 albedo, float roughness,
+                             float tilt) {
+    const float theta_o = asinf(clampf(dot3(tangent, view), -1.0f, 1.0f));
+    const float theta_i = tilt - theta_o;
+    const f3 spec_dir = cubemap_dir(env.rot, add3(mul3s(tangent, sinf(theta_i)), mul3s(fiber_n, cosf(theta_i))));
+    const f3 diff_dir = cubemap_dir(env.rot, fiber_n);
+    const f3 spec = sample_cube(env.spec, env.spec_size, env.spec_levels, spec_dir,
+                                roughness * (float)(env.spec_levels - 1));
+    const f3 diff = sample_cube(env.diff, env.diff_size, env.diff_levels, diff_dir, 0.0f);
+    const float cos_o = fmaxf(cosf(theta_o), 1e-3f);
+    const float f_r = fresnel(cos_o);
+    const float f_trt = fresnel(cos_o * 0.5f);
+    const f3 sigma_a = absorption_from_color(albedo, roughness);
+    const float k = 0.76f * (1.0f - f_trt) * (1.0f - f_trt) * f_trt;
+    const f3 trt = {k * expf(-sigma_a.x * 3.2f / cos_o), k * expf(-sigma_a.y * 3.2f / cos_o),
+                    k * expf(-sigma_a.z * 3.2f / cos_o)};
+    const f3 scatter = vmul(albedo, scatter_tint(albedo, 0.5f));
+    const f3 r = add3(vmul(spec, add3(spl(f_r), trt)), vmul(diff, scatter));
+    return mul3s(r, env.intensity);
+}
+
+__device__ __forceinline__ float pixel_ao(const hg_hair_params& p, uint32_t low) {
+    return p.flags[2] == 0u ? 1.0f : (float)(low & 0x3fu) / 63.0f;
+}
+
 // dom_texel_visibility (shade.wesl:262-277)
 __device__ __forceinline__ float dom_texel_visibility(const uint32_t* __restrict__ dom, float sigma, int32_t x,
                                                       int32_t y, float dist, float near_, float far_,
@@ -282,7 +405,8 @@ struct ShadeArgs {
 // spot, directional, rect), the order the reference's loops visit them.
 template <class V>
 __device__ __forceinline__ void shade_pixel(const V& a, const hg_light* __restrict__ lights, uint32_t n_lights,
-                                            uint32_t ortho, float exposure, uint32_t x, uint32_t y) {
+                                            uint32_t ortho, float exposure, const EnvArgs& env, uint32_t x,
+                                            uint32_t y) {
     const hg_hair_params& p = a.p;
     const uint32_t width = f2u(p.screen[0]), height = f2u(p.screen[1]);
     if (x >= width || y >= height) return;
@@ -360,13 +484,18 @@ __device__ __forceinline__ void shade_pixel(const V& a, const hg_light* __restri
             }
         }
     }
+    if (env.spec) {
+        const f3 fiber_n = safe_normalize(sub3(view, mul3s(tangent, dot3(view, tangent))));
+        const f3 pr = probe_radiance(env, tangent, fiber_n, view, albedo, roughness, tilt);
+        color = add3(color, mul3s(pr, pixel_ao(p, low)));
+    }
     color = mul3s(color, exposure);
     a.shaded[pix] = make_float4(color.x, color.y, color.z, 1.0f);
     a.shaded_depth[pix] = view_dist;
 }
 
-__global__ void __launch_bounds__(256, 3) shade_kernel(const ShadeArgs a) {
-    shade_pixel(a, a.lights, a.n_lights, a.ortho, a.exposure, blockIdx.x * blockDim.x + threadIdx.x,
+__global__ void __launch_bounds__(256, 3) shade_kernel(const ShadeArgs a, const EnvArgs env) {
+    shade_pixel(a, a.lights, a.n_lights, a.ortho, a.exposure, env, blockIdx.x * blockDim.x + threadIdx.x,
                 blockIdx.y * blockDim.y + threadIdx.y);
 }
 
@@ -374,7 +503,7 @@ __global__ void __launch_bounds__(256, 3) shade_kernel(const ShadeArgs a) {
 __global__ void __launch_bounds__(256, 3) batch_shade_kernel(const BatchView* __restrict__ views,
                                                              const uint32_t* __restrict__ tile_prefix, uint32_t n_cam,
                                                              const hg_light* __restrict__ lights, uint32_t n_lights,
-                                                             uint32_t ortho, float exposure) {
+                                                             uint32_t ortho, float exposure, const EnvArgs env) {
     uint32_t lo = 0, hi = n_cam;
     while (hi - lo > 1u) {
         const uint32_t mid = (lo + hi) >> 1;
@@ -384,7 +513,7 @@ __global__ void __launch_bounds__(256, 3) batch_shade_kernel(const BatchView* __
     const BatchView& v = views[lo];
     const uint32_t t = blockIdx.x - tile_prefix[lo];
     const uint32_t tiles_x = (v.width + blockDim.x - 1) / blockDim.x;
-    shade_pixel(v, lights, n_lights, ortho, exposure, (t % tiles_x) * blockDim.x + threadIdx.x,
+    shade_pixel(v, lights, n_lights, ortho, exposure, env, (t % tiles_x) * blockDim.x + threadIdx.x,
                 (t / tiles_x) * blockDim.y + threadIdx.y);
 }
 
@@ -437,7 +566,8 @@ __device__ __forceinline__ float light_weight(const hg_light& L, f3 world, f3& i
 }
 
 __global__ void __launch_bounds__(kSurrogateWarps * 32, 2)
-    shade_surrogate_kernel(const ShadeArgs a, const __half* __restrict__ w16, const float* __restrict__ mparams) {
+    shade_surrogate_kernel(const ShadeArgs a, const __half* __restrict__ w16, const float* __restrict__ mparams,
+                           const EnvArgs env) {
     extern __shared__ __align__(16) unsigned char smem[];
     mlp::FwdWeights& w = *reinterpret_cast<mlp::FwdWeights*>(smem);
     mlp::WarpIo& io = reinterpret_cast<mlp::WarpIo*>(smem + sizeof(mlp::FwdWeights))[threadIdx.x >> 5];
@@ -542,6 +672,11 @@ __global__ void __launch_bounds__(kSurrogateWarps * 32, 2)
             }
         }
         if (active) {
+            if (env.spec) {
+                const f3 fiber_n = safe_normalize(sub3(view, mul3s(tangent, dot3(view, tangent))));
+                const f3 pr = probe_radiance(env, tangent, fiber_n, view, albedo, roughness, p.appearance[1]);
+                color = add3(color, mul3s(pr, pixel_ao(p, low)));
+            }
             color = mul3s(color, a.exposure);
             a.shaded[pix] = make_float4(color.x, color.y, color.z, 1.0f);
             a.shaded_depth[pix] = view_dist;
@@ -584,8 +719,23 @@ int g_surrogate_per_sm[64] = {};  // resident blocks per SM, 0 until the attribu
 
 }  // namespace
 
+EnvArgs env_args(const hg_ctx* ctx) {
+    EnvArgs e;
+    e.spec = ctx->env_spec;
+    e.diff = ctx->env_diff;
+    e.spec_size = ctx->env_spec_size;
+    e.spec_levels = ctx->env_spec_levels;
+    e.diff_size = ctx->env_diff_size;
+    e.diff_levels = ctx->env_diff_levels;
+    for (int i = 0; i < 4; ++i) e.rot[i] = ctx->env_rot[i];
+    e.intensity = ctx->env_intensity;
+    if (!e.diff) e.spec = nullptr;
+    return e;
+}
+
 cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights, uint32_t ortho, float exposure,
                          uint32_t model) {
+    const EnvArgs env = env_args(ctx);
     ShadeArgs a;
     a.p = p;
     a.center = ctx->center;
@@ -617,12 +767,12 @@ cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights
         uint32_t blocks = (uint32_t)ctx->sm_count * (uint32_t)per_sm;
         if (blocks > tiles) blocks = tiles;
         shade_surrogate_kernel<<<blocks, kSurrogateWarps * 32, kSurrogateSmem, ctx->stream>>>(
-            a, reinterpret_cast<const __half*>(ctx->surrogate->w16), ctx->surrogate->params);
+            a, reinterpret_cast<const __half*>(ctx->surrogate->w16), ctx->surrogate->params, env);
         return cudaGetLastError();
     }
     dim3 block(32, 8);
     dim3 grid((ctx->width + 31) / 32, (ctx->height + 7) / 8);
-    shade_kernel<<<grid, block, 0, ctx->stream>>>(a);
+    shade_kernel<<<grid, block, 0, ctx->stream>>>(a, env);
     return cudaGetLastError();
 }
 
@@ -630,7 +780,7 @@ cudaError_t launch_batch_shade(hg_ctx* ctx, const BatchDev& b) {
     if (!b.total_tiles) return cudaSuccess;
     dim3 block(b.tile_w, b.tile_h);
     batch_shade_kernel<<<b.total_tiles, block, 0, ctx->stream>>>(b.views, b.tile_prefix, b.n_cam, b.lights,
-                                                                  b.n_lights, b.ortho, b.exposure);
+                                                                  b.n_lights, b.ortho, b.exposure, env_args(ctx));
     return cudaGetLastError();
 }
 

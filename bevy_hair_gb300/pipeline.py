@@ -285,6 +285,13 @@ class HairRenderer:
         self._frame_keepalive = (lights, camera, dom)
         _check(self.lib, self.ctx, self.lib.hg_groom_frame(self.ctx, groom.handle, C.byref(d)))
 
+    def set_environment(self, env) -> None:
+        """Upload a light probe (a bevy_hair_gb300.envmap.Environment), or drop it with None."""
+        from . import envmap
+
+        d, keep = envmap.env_desc(env)
+        _check(self.lib, self.ctx, self.lib.hg_env_set(self.ctx, C.byref(d) if d is not None else None))
+
     def bind_surrogate(self, surrogate) -> None:
         """Make `surrogate` (a bevy_hair_gb300.surrogate.Surrogate, or None) the
         network that shade model 1 evaluates."""

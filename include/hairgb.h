@@ -331,6 +331,35 @@ hg_status hg_hair_visibility(hg_ctx* ctx, const hg_shadow_light* light, const fl
 hg_status hg_scan_noalloc(const hg_lod_record* lod, uint32_t bundle_count, uint32_t capacity,
                           hg_strand_ref* refs, uint32_t* indirect, void* stream);
 
+/* ---------------------------------------------------------------- environment light probe */
+
+/* The light probe that shade.wesl's probe_radiance samples (shade.wesl:330-427,
+ * the ENVIRONMENT_MAP specialization): a specular cubemap sampled trilinearly
+ * at mip roughness x (levels - 1) along the R cone, and a diffuse irradiance
+ * cubemap at mip 0 along the fibre normal.  Texels are RGB9E5
+ * (VK_FORMAT_E5B9G9R9_UFLOAT_PACK32, the format of the reference's KTX2
+ * probes); each array holds the mip levels from 0, each level the six faces
+ * +X, -X, +Y, -Y, +Z, -Z of max(size >> level, 1)^2 texels, row-major.  The
+ * face of a direction and its (s, t) follow the usual major-axis rule; within
+ * a face the sampler is bilinear with clamp-to-edge (Bevy's GPU sampler also
+ * filters across face edges, so colour parity with it is unpinned).
+ * rotation is light_probes.view_rotation (x, y, z, w) and intensity
+ * light_probes.intensity_for_view.  Without a probe (the default, or after
+ * hg_env_set(ctx, NULL)) probe_radiance is zero, the reference's behaviour
+ * without ENVIRONMENT_MAP. */
+typedef struct hg_env_desc {
+    const uint32_t* specular;    /* host, RGB9E5 */
+    uint32_t specular_size, specular_levels;
+    const uint32_t* diffuse;     /* host, RGB9E5 */
+    uint32_t diffuse_size, diffuse_levels;
+    float rotation[4];
+    float intensity;
+} hg_env_desc;
+
+/* Upload (or, with NULL, drop) the context's light probe; every later shade
+ * call adds probe_radiance x AO.  Sizes 1..4096, levels 1..1 + log2(size). */
+hg_status hg_env_set(hg_ctx* ctx, const hg_env_desc* env);
+
 /* ---------------------------------------------------------------- batched frames */
 
 /* Many independent grooms, each with its own camera view and deep opacity

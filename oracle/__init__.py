@@ -20,6 +20,22 @@ HERE = Path(__file__).resolve().parent
 SO = HERE / "_build" / "libhair_oracle.so"
 
 
+class Env(C.Structure):
+    _fields_ = [("spec", C.c_void_p), ("spec_size", C.c_uint32), ("spec_levels", C.c_uint32),
+                ("diff", C.c_void_p), ("diff_size", C.c_uint32), ("diff_levels", C.c_uint32),
+                ("rot", C.c_float * 4), ("intensity", C.c_float)]
+
+
+def _env(env):
+    """An oracle_env for a bevy_hair_gb300.envmap.Environment (or None), plus keep-alive arrays."""
+    if env is None:
+        return None, ()
+    spec, diff = env.specular.packed(), env.diffuse.packed()
+    e = Env(spec.ctypes.data, env.specular.size, len(env.specular.levels), diff.ctypes.data, env.diffuse.size,
+            len(env.diffuse.levels), (C.c_float * 4)(*[float(v) for v in env.rotation]), float(env.intensity))
+    return e, (spec, diff)
+
+
 class Counts(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("samples", "cons_min", "center_min", "beta_min", "dom_min", "dom_add",
                                           "segments")]
@@ -53,7 +69,8 @@ _SIGS = {
     "oracle_scan": (None, [_VP, _VP, _VP, _U32, _VP]),
     "oracle_strand_points": (_U32, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "oracle_raster": (None, [_VP, _VP, _VP, _VP, _VP, _U32, _VP, _VP, _VP, _VP, _VP, C.POINTER(Counts)]),
-    "oracle_shade": (None, [_VP, _VP, _VP, _VP, _VP, _U32, _U32, _F, _VP, _VP, _VP]),
+    "oracle_shade": (None, [_VP, _VP, _VP, _VP, _VP, _U32, _U32, _F, _VP, _VP, _VP, _VP]),
+    "oracle_sample_cube": (None, [_VP, _U32, _U32, _VP, _F, _VP]),
     "oracle_mlp_forward": (None, [_VP, _VP, _U32, _VP]),
     "oracle_filter": (None, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "oracle_composite": (None, [_VP, _VP, _VP, _VP, _VP]),
@@ -140,17 +157,28 @@ def raster(params, mesh, refs, total, center, cons, beta, dom, scene_depth=None)
     return counts.as_dict()
 
 
-def shade(params, center, beta, dom, lights, exposure=1.0, ortho=False, mlp=None):
-    """Shade model 0 (Karis fit), or model 1 when `mlp` holds the surrogate's parameters."""
+def shade(params, center, beta, dom, lights, exposure=1.0, ortho=False, mlp=None, env=None):
+    """Shade model 0 (Karis fit), or model 1 when `mlp` holds the surrogate's parameters;
+    env: a bevy_hair_gb300.envmap.Environment for the light-probe term."""
     w, h = int(params["screen"][0]), int(params["screen"][1])
     shaded = np.empty(w * h * 4, dtype=np.float32)
     sdepth = np.empty(w * h, dtype=np.float32)
     lights = np.ascontiguousarray(lights, dtype=abi.LIGHT)
     dom_arr = dom if dom is not None else np.zeros(16, dtype=np.uint32)
     mlp_arr = None if mlp is None else np.ascontiguousarray(mlp, dtype=np.float32)
+    e, keep = _env(env)
     lib().oracle_shade(_p(params), _p(center), _p(beta), _p(dom_arr), _p(lights) if len(lights) else None,
-                       len(lights), int(ortho), float(exposure), _p(mlp_arr), _p(shaded), _p(sdepth))
+                       len(lights), int(ortho), float(exposure), _p(mlp_arr), C.byref(e) if e else None,
+                       _p(shaded), _p(sdepth))
     return shaded, sdepth
+
+
+def sample_cube(texels: np.ndarray, size: int, levels: int, direction, lod: float) -> np.ndarray:
+    out = np.zeros(3, dtype=np.float32)
+    d = np.asarray(direction, dtype=np.float32)
+    t = np.ascontiguousarray(texels, dtype=np.uint32)
+    lib().oracle_sample_cube(_p(t), size, levels, _p(d), float(lod), _p(out))
+    return out
 
 
 def mlp_forward(params: np.ndarray, raw: np.ndarray) -> np.ndarray:
@@ -176,7 +204,7 @@ def composite(params, color_src, depth_src, color_dst, depth_dst) -> None:
                            _p(np.ascontiguousarray(depth_src, dtype=np.float32)), _p(color_dst), _p(depth_dst))
 
 
-def frame(mesh, camera, dom_params, lights, exposure=1.0, ortho=False, scene_depth=None, mlp=None) -> dict:
+def frame(mesh, camera, dom_params, lights, exposure=1.0, ortho=False, scene_depth=None, mlp=None, env=None) -> dict:
     """The per-groom sequence of hair_pass (src/render/pass.rs:375-643) on the CPU."""
     w, h = int(camera["screen"][0]), int(camera["screen"][1])
     out: dict = {}
@@ -197,7 +225,7 @@ def frame(mesh, camera, dom_params, lights, exposure=1.0, ortho=False, scene_dep
         layers = dom_params.copy()
         layers["pass_mode"][0] = 2
         out["counts_dom_layers"] = raster(layers, mesh, refs_d, total_d, center, cons, beta, dom)
-    shaded, sdepth = shade(camera, center, beta, dom, lights, exposure, ortho, mlp)
+    shaded, sdepth = shade(camera, center, beta, dom, lights, exposure, ortho, mlp, env)
     out.update(center=center, cons=cons, beta=beta, dom=dom, shaded=shaded, shaded_depth=sdepth)
     if int(camera["flags"][1]):
         filt, fdepth = filter_(camera, center, cons, shaded, sdepth)

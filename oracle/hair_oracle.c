@@ -1025,6 +1025,125 @@ static v3 light_lobe(const float* mlp, v3 tangent, v3 view, v3 incident, v3 sigm
     return hair_bsdf(tangent, view, incident, sigma_a, shape, ds, 1.0f, depth);
 }
 
+/* ------------------------------------------------- light probe
+ * probe_radiance (shade.wesl:330-427, ENVIRONMENT_MAP): RGB9E5 cubemaps,
+ * major-axis face selection, bilinear within a face with clamp-to-edge,
+ * linear between mips.  Bevy's GPU sampler also filters across face edges
+ * (seamless cubemaps), so parity with the reference here is unpinned; the
+ * oracle defines the sampler the kernel follows. */
+static v3 rgb9e5(uint32_t w) {
+    int e = (int)(w >> 27) - 24;
+    return V3(ldexpf((float)(w & 0x1ffu), e), ldexpf((float)((w >> 9) & 0x1ffu), e),
+              ldexpf((float)((w >> 18) & 0x1ffu), e));
+}
+
+static int cube_face_uv(v3 d, float* s, float* t) {
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z), ma, sc, tc;
+    int face;
+    if (ax >= ay && ax >= az) {
+        face = d.x >= 0.0f ? 0 : 1;
+        ma = ax;
+        sc = d.x >= 0.0f ? -d.z : d.z;
+        tc = -d.y;
+    } else if (ay >= az) {
+        face = d.y >= 0.0f ? 2 : 3;
+        ma = ay;
+        sc = d.x;
+        tc = d.y >= 0.0f ? d.z : -d.z;
+    } else {
+        face = d.z >= 0.0f ? 4 : 5;
+        ma = az;
+        sc = d.z >= 0.0f ? d.x : -d.x;
+        tc = -d.y;
+    }
+    float inv = 1.0f / fmaxf(ma, 1e-20f);
+    *s = 0.5f * (sc * inv + 1.0f);
+    *t = 0.5f * (tc * inv + 1.0f);
+    return face;
+}
+
+static v3 cube_bilinear(const uint32_t* level, uint32_t n, int face, float s, float t) {
+    float u = s * (float)n - 0.5f, v = t * (float)n - 0.5f;
+    float fu = floorf(u), fv = floorf(v), wu = u - fu, wv = v - fv;
+    int last = (int)n - 1;
+    int x0 = (int)fu, y0 = (int)fv;
+    int x1 = x0 + 1, y1 = y0 + 1;
+    x0 = x0 < 0 ? 0 : (x0 > last ? last : x0);
+    x1 = x1 < 0 ? 0 : (x1 > last ? last : x1);
+    y0 = y0 < 0 ? 0 : (y0 > last ? last : y0);
+    y1 = y1 < 0 ? 0 : (y1 > last ? last : y1);
+    const uint32_t* f = level + (size_t)face * n * n;
+    v3 c00 = rgb9e5(f[y0 * n + x0]), c10 = rgb9e5(f[y0 * n + x1]);
+    v3 c01 = rgb9e5(f[y1 * n + x0]), c11 = rgb9e5(f[y1 * n + x1]);
+    v3 a = add3(mul3s(c00, 1.0f - wu), mul3s(c10, wu));
+    v3 b = add3(mul3s(c01, 1.0f - wu), mul3s(c11, wu));
+    return add3(mul3s(a, 1.0f - wv), mul3s(b, wv));
+}
+
+static v3 sample_cube(const uint32_t* texels, uint32_t size, uint32_t levels, v3 dir, float lod) {
+    float s, t;
+    int face = cube_face_uv(dir, &s, &t);
+    lod = clampf(lod, 0.0f, (float)(levels - 1));
+    uint32_t l0 = (uint32_t)lod, l1 = l0 + 1u < levels ? l0 + 1u : levels - 1u;
+    float w = lod - (float)l0;
+    size_t off = 0;
+    for (uint32_t l = 0; l < l0; ++l) {
+        size_t n = size >> l ? size >> l : 1;
+        off += 6 * n * n;
+    }
+    uint32_t n0 = size >> l0 ? size >> l0 : 1;
+    v3 a = cube_bilinear(texels + off, n0, face, s, t);
+    if (l1 == l0 || w <= 0.0f) return a;
+    off += 6 * (size_t)n0 * n0;
+    v3 b = cube_bilinear(texels + off, size >> l1 ? size >> l1 : 1, face, s, t);
+    return add3(mul3s(a, 1.0f - w), mul3s(b, w));
+}
+
+void oracle_sample_cube(const uint32_t* texels, uint32_t size, uint32_t levels, const float dir[3], float lod,
+                        float out[3]) {
+    v3 c = sample_cube(texels, size, levels, V3(dir[0], dir[1], dir[2]), lod);
+    out[0] = c.x;
+    out[1] = c.y;
+    out[2] = c.z;
+}
+
+/* quat_rotate + the left-handed flip (shade.wesl:329-339) */
+static v3 cubemap_dir(const float q[4], v3 dir) {
+    v3 qv = V3(q[0], q[1], q[2]);
+    v3 t = mul3s(cross3(qv, dir), 2.0f);
+    v3 r = add3(add3(dir, mul3s(t, q[3])), cross3(qv, t));
+    r.z = -r.z;
+    return r;
+}
+
+/* scatter_tint (shade.wesl:81-85), luminance (:62-64) */
+static v3 scatter_tint(v3 albedo, float shadow) {
+    float lum = albedo.x * 0.2126f + albedo.y * 0.7152f + albedo.z * 0.0722f;
+    v3 hue = mul3s(albedo, 1.0f / fmaxf(lum, 1e-4f));
+    float e = 0.5f - 0.5f * clampf(shadow, 0.0f, 1.0f);
+    return V3(powf(hue.x, e), powf(hue.y, e), powf(hue.z, e));
+}
+
+static v3 probe_radiance(const oracle_env* env, v3 tangent, v3 fiber_n, v3 view, v3 albedo, float roughness,
+                         float tilt) {
+    float theta_o = asinf(clampf(dot3(tangent, view), -1.0f, 1.0f));
+    float theta_i = tilt - theta_o;
+    v3 spec_dir = cubemap_dir(env->rot, add3(mul3s(tangent, sinf(theta_i)), mul3s(fiber_n, cosf(theta_i))));
+    v3 diff_dir = cubemap_dir(env->rot, fiber_n);
+    v3 spec = sample_cube(env->spec, env->spec_size, env->spec_levels, spec_dir,
+                          roughness * (float)(env->spec_levels - 1));
+    v3 diff = sample_cube(env->diff, env->diff_size, env->diff_levels, diff_dir, 0.0f);
+    float cos_o = fmaxf(cosf(theta_o), 1e-3f);
+    float f_r = fresnel(cos_o), f_trt = fresnel(cos_o * 0.5f);
+    v3 sigma_a = absorption_from_color(albedo, roughness);
+    float k = 0.76f * (1.0f - f_trt) * (1.0f - f_trt) * f_trt;
+    v3 trt = V3(k * expf(-sigma_a.x * 3.2f / cos_o), k * expf(-sigma_a.y * 3.2f / cos_o),
+                k * expf(-sigma_a.z * 3.2f / cos_o));
+    v3 scatter = mul3(albedo, scatter_tint(albedo, 0.5f));
+    v3 r = add3(mul3(spec, add3(spl3(f_r), trt)), mul3(diff, scatter));
+    return mul3s(r, env->intensity);
+}
+
 /* shade.wesl:262-277 */
 static float dom_texel_visibility(const hg_hair_params* p, const uint32_t* dom, int32_t x, int32_t y, float dist,
                                   float near_, float far_, uint32_t dom_w, uint32_t dom_h) {
@@ -1142,7 +1261,7 @@ static v3 direct_light(const hg_hair_params* p, const uint32_t* dom, const hg_li
  * in the specialization without ENVIRONMENT_MAP, shade.wesl:384-394). */
 void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_t* beta_buf, const uint32_t* dom,
                   const hg_light* lights, uint32_t n_lights, uint32_t ortho, float exposure, const float* mlp,
-                  float* shaded, float* shaded_depth) {
+                  const oracle_env* env, float* shaded, float* shaded_depth) {
     uint32_t width = f2u(p->screen[0]), height = f2u(p->screen[1]);
     int nthreads = oracle_get_threads();
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads)
@@ -1163,7 +1282,6 @@ void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_
         v3 uvw = V3((float)u[3] / 63.0f, (float)u[4] / 63.0f, (float)u[5] / 63.0f);
         float ao = (float)u[6] / 63.0f;
         if (p->flags[2] == 0u) ao = 1.0f;
-        (void)ao;
         float beta = (float)(beta_buf[pix] & 0xffu) / 255.0f;
         float roughness = fmaxf(p->appearance[0] * (0.65f + 0.7f * uvw.z), 0.04f);
         float tilt = p->appearance[1];
@@ -1175,6 +1293,10 @@ void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_
             view = safe_normalize(sub3(ld3(p->camera_pos), world));
         }
         v3 color = direct_light(p, dom, lights, n_lights, world, tangent, view, albedo, roughness, tilt, beta, mlp);
+        if (env) {
+            v3 fiber_n = safe_normalize(sub3(view, mul3s(tangent, dot3(view, tangent))));
+            color = add3(color, mul3s(probe_radiance(env, tangent, fiber_n, view, albedo, roughness, tilt), ao));
+        }
         color = mul3s(color, exposure);
         shaded[4 * pix + 0] = color.x;
         shaded[4 * pix + 1] = color.y;

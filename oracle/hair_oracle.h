@@ -80,11 +80,24 @@ void oracle_raster(const hg_hair_params* p, const hg_gpu_bundle* bundles, const 
                    const float* style, const hg_strand_ref* refs, uint32_t n_refs,
                    uint64_t* center, uint64_t* cons, uint32_t* beta, uint32_t* dom,
                    const float* scene_depth, oracle_counts* counts);
+/* The light probe of shade.wesl:330-427 (hg_env_desc with host texels). */
+typedef struct oracle_env {
+    const uint32_t* spec;
+    uint32_t spec_size, spec_levels;
+    const uint32_t* diff;
+    uint32_t diff_size, diff_levels;
+    float rot[4];
+    float intensity;
+} oracle_env;
+
 /* mlp: NULL for shade model 0 (Karis fit); the surrogate's HG_MLP_PARAMS
- * floats for shade model 1. */
+ * floats for shade model 1.  env: NULL without a light probe. */
 void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_t* beta, const uint32_t* dom,
                   const hg_light* lights, uint32_t n_lights, uint32_t ortho, float exposure, const float* mlp,
-                  float* shaded, float* shaded_depth);
+                  const oracle_env* env, float* shaded, float* shaded_depth);
+/* One trilinear cubemap sample (RGB9E5 mip chain) for the sampler tests. */
+void oracle_sample_cube(const uint32_t* texels, uint32_t size, uint32_t levels, const float dir[3], float lod,
+                        float out[3]);
 /* The surrogate network on raw inputs (n x 10) -> raw outputs (n x 12). */
 void oracle_mlp_forward(const float* params, const float* raw, uint32_t n, float* net);
 void oracle_filter(const hg_hair_params* p, const uint64_t* center, const uint64_t* cons,
