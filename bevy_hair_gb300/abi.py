@@ -22,7 +22,7 @@ SCAN_NOALLOC_MAX_BUNDLES = 65536
 MLP_PARAMS = 14608
 MLP_INPUTS = 10
 MLP_OUTPUTS = 12
-SHADE_KARIS, SHADE_SURROGATE = 0, 1
+SHADE_KARIS, SHADE_SURROGATE, SHADE_SURROGATE_MMA = 0, 1, 2
 
 # --------------------------------------------------------------------- dtypes
 
@@ -186,6 +186,7 @@ _SIGNATURES = {
     "hg_mlp_get_params": (_I32, [_VP, _VP, _U32]),
     "hg_mlp_samples": (_I32, [_VP, C.c_uint64, C.c_uint64, _U32, _F32, _VP, _VP, _VP]),
     "hg_mlp_infer": (_I32, [_VP, _VP, _U32, _VP, _VP]),
+    "hg_mlp_infer_tc": (_I32, [_VP, _VP, _U32, _VP, _VP]),
     "hg_mlp_gradients": (_I32, [_VP, _VP, _VP, _U32, _VP, C.POINTER(_F32)]),
     "hg_mlp_train_step": (_I32, [_VP, _VP, _VP, _U32, _F32, _VP]),
     "hg_mlp_bind": (_I32, [_VP, _VP]),

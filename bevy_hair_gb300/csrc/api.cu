@@ -51,6 +51,8 @@ void free_targets(hg_ctx* ctx) {
     free_dev(ctx->filtered_depth);
     free_dev(ctx->color);
     free_dev(ctx->depth);
+    free_dev(ctx->hair_list);
+    free_dev(ctx->hair_count);
     ctx->width = ctx->height = ctx->dom_w = ctx->dom_h = 0;
 }
 
@@ -240,7 +242,8 @@ hg_status hg_synchronize(hg_ctx* ctx, uint32_t* device_error) {
     if (device_error) *device_error = word;
     if (word != 0) {
         HG_CUDA(ctx, cudaMemsetAsync(ctx->err, 0, sizeof(uint32_t), ctx->stream));
-        return fail(ctx, HG_DEVICE_ERROR, "a kernel reported an invalid strand reference");
+        return fail(ctx, word & 2u ? HG_DEVICE_TIMEOUT : HG_DEVICE_ERROR,
+                    word & 2u ? "a tensor-core wait timed out" : "a kernel reported an invalid strand reference");
     }
     return HG_OK;
 }
@@ -272,6 +275,8 @@ hg_status hg_ensure_targets(hg_ctx* ctx, uint32_t width, uint32_t height, uint32
     alloc(ctx->filtered_depth, px * 4);
     alloc(ctx->color, px * 16);
     alloc(ctx->depth, px * 4);
+    alloc(ctx->hair_list, px * 4);
+    alloc(ctx->hair_count, 16);
     if (e != cudaSuccess) {
         free_targets(ctx);
         return cuda_fail(ctx, e, "allocating screen targets");
@@ -496,9 +501,9 @@ hg_status hg_shade(hg_ctx* ctx, const hg_hair_params* p, const hg_shade_desc* d)
     if (!ctx || !p || !d) return HG_INVALID_ARG;
     if (d->light_count > HG_MAX_LIGHTS) return fail(ctx, HG_CAPACITY_EXCEEDED, "more than HG_MAX_LIGHTS lights");
     if (d->light_count && !d->lights) return fail(ctx, HG_INVALID_ARG, "null light array");
-    if (d->shade_model > 1u) return fail(ctx, HG_INVALID_ARG, "unknown shade model");
-    if (d->shade_model == 1u && !ctx->surrogate)
-        return fail(ctx, HG_NOT_READY, "shade model 1 needs a surrogate bound with hg_mlp_bind");
+    if (d->shade_model > 2u) return fail(ctx, HG_INVALID_ARG, "unknown shade model");
+    if (d->shade_model != 0u && !ctx->surrogate)
+        return fail(ctx, HG_NOT_READY, "shade models 1 and 2 need a surrogate bound with hg_mlp_bind");
     hg_status s = check_screen(ctx, p);
     if (s != HG_OK) return s;
     if (p->pass_mode[0] != 0u) return fail(ctx, HG_INVALID_ARG, "shade takes the camera params (pass_mode.x == 0)");

@@ -68,6 +68,8 @@ struct hg_ctx {
     float* filtered_depth = nullptr;
     float4* color = nullptr;
     float* depth = nullptr;
+    uint32_t* hair_list = nullptr;  // pixels with hair (shade model 1), W*H
+    uint32_t* hair_count = nullptr;
     uint32_t* err = nullptr;       // device error word
     hg_light* lights = nullptr;    // device copy, HG_MAX_LIGHTS
     // Pinned staging ring for the light list; slot k is reused only after
@@ -182,6 +184,7 @@ constexpr uint32_t kBatchMaxViews = 256;
 
 // surrogate.cu
 cudaError_t launch_mlp_infer(hg_mlp* m, const float* inputs, uint32_t n, float* lobes, float* net);
+cudaError_t launch_mlp_infer_tc(hg_mlp* m, const float* inputs, uint32_t n, float* lobes, float* net);
 
 // filter.cu
 cudaError_t launch_filter(hg_ctx* ctx, const hg_hair_params& p);

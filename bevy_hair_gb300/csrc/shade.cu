@@ -9,6 +9,7 @@
 #include "hg_device.cuh"
 #include "hg_internal.h"
 #include "hg_mlp.cuh"
+#include "hg_mlp_tc.cuh"
 
 namespace hg {
 namespace {
@@ -714,8 +715,150 @@ __global__ void karis_lobes_kernel(const float* __restrict__ in, uint32_t n, flo
     }
 }
 
+// ---------------------------------------------------------------- surrogate on tcgen05
+// Shade model 1: the surrogate with the network on the tcgen05 tensor cores
+// (hg_mlp_tc.cuh).  A prepass lists the pixels with hair, so every one of the
+// 128 MMA rows of a chunk is a real pixel; each warpgroup of a CTA shades its
+// own chunks, one network evaluation per light.  The light loop, the DOM
+// spread and the probe are those of shade_surrogate_kernel.
+
+// Pixels whose centre word is not empty, appended in warp order; the others
+// get the empty shade outputs.
+__global__ void hair_list_kernel(const unsigned long long* __restrict__ center, uint32_t pixels,
+                                 uint32_t* __restrict__ list, uint32_t* __restrict__ count,
+                                 float4* __restrict__ shaded, float* __restrict__ shaded_depth) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    bool hair = false;
+    if (pix < pixels) {
+        hair = !is_empty(__ldg(&center[pix]));
+        if (!hair) {
+            shaded[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            shaded_depth[pix] = 0.0f;
+        }
+    }
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t m = __ballot_sync(0xffffffffu, hair);
+    uint32_t base = 0;
+    if (lane == 0 && m) base = atomicAdd(count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (hair) list[base + __popc(m & ((1u << lane) - 1u))] = pix;
+}
+
+__global__ void __launch_bounds__(256, 2)
+    shade_tc_kernel(const ShadeArgs a, const __half* __restrict__ w16, const float* __restrict__ mparams,
+                    const EnvArgs env, const uint32_t* __restrict__ list, const uint32_t* __restrict__ count,
+                    uint32_t* __restrict__ err) {
+    extern __shared__ __align__(128) uint8_t smem_tc[];
+    mlp::tc::Chain c = mlp::tc::setup(smem_tc, w16, mparams);
+    const hg_hair_params& p = a.p;
+    const uint32_t width = f2u(p.screen[0]);
+    const uint32_t g = threadIdx.x >> 7;
+    int dom_light = -1;
+    for (uint32_t i = 0; i < a.n_lights; ++i)
+        if (a.lights[i].kind == HG_LIGHT_DIRECTIONAL && (a.lights[i].flags & HG_LIGHT_CASTS_SHADOWS)) {
+            dom_light = (int)i;
+            break;
+        }
+    const uint32_t n = *count;
+    const uint32_t chunks = (n + mlp::tc::kM - 1) / mlp::tc::kM;
+    bool failed = false;
+    for (uint32_t ch = blockIdx.x * mlp::tc::kChains + g; ch < chunks; ch += gridDim.x * mlp::tc::kChains) {
+        const uint32_t idx = ch * mlp::tc::kM + c.row;
+        const bool active = idx < n;
+        const uint32_t pix = active ? __ldg(&list[idx]) : 0u;
+        const uint32_t x = pix % width, y = pix / width;
+        const unsigned long long word = active ? __ldg(&a.center[pix]) : 0ull;
+        const uint32_t low = (uint32_t)word, high = (uint32_t)(word >> 32);
+        const float view_dist = dequantize_depth(high >> 8u, p.screen[2], p.screen[3]);
+        const f3 world = reconstruct_world(p, (int32_t)x, (int32_t)y, view_dist);
+        const f3 tangent = oct_decode(high & 0xffu, low >> 24u);
+        const float uvw_z = (float)((low >> 6u) & 0x3fu) / 63.0f;
+        const float roughness = fmaxf(p.appearance[0] * (0.65f + 0.7f * uvw_z), 0.04f);
+        const float ascale = 0.65f + 0.35f * uvw_z;
+        const f3 albedo = {p.albedo[0] * ascale, p.albedo[1] * ascale, p.albedo[2] * ascale};
+        f3 view;
+        if (a.ortho) {
+            view = safe_normalize(mk3(p.clip_from_world[2], p.clip_from_world[6], p.clip_from_world[10]));
+        } else {
+            view = safe_normalize(sub3(ld3(p.camera_pos), world));
+        }
+        const Shape shape = lobe_shape(roughness, p.appearance[1]);
+        const f3 sigma_a = absorption_from_color(albedo, roughness);
+        const float beta_n = clampf(roughness, 0.2f, 0.8f);
+        const f3 t_n = safe_normalize(tangent), v_n = safe_normalize(view);
+        const float sin_o = clampf(dot3(t_n, v_n), -1.0f, 1.0f);
+        const f3 t_o = sub3(v_n, mul3s(t_n, sin_o));
+        const float to2 = dot3(t_o, t_o);
+        // the per-pixel network inputs (absorption, roughnesses, IOR)
+        float xin[10];
+        {
+            const float raw[10] = {0.0f, 0.0f, 1.0f, 0.0f, sigma_a.x, sigma_a.y, sigma_a.z, shape.beta.x, beta_n, kIor};
+            mlp::normalise(raw, xin);
+        }
+        f3 color = spl(0.0f);
+        float dom_direct = 1.0f;
+        if (dom_light >= 0 && active) {
+            const hg_light& L = a.lights[dom_light];
+            const float beta = (float)(__ldg(&a.beta[pix]) & 0xffu) / 255.0f;
+            const float depth = -logf(fmaxf(dom_visibility(p, a.dom, world, beta), 1e-6f));
+            dom_direct = expf(-depth);
+            if (depth > 1e-3f) {
+                const float tv = dot3(tangent, view);
+                const Dual ds = dual_scatter(sqrtf(fmaxf(1.0f - tv * tv, 1e-6f)), sigma_a, shape);
+                const Geometry gm = light_geometry(tangent, view, ld3(L.direction));
+                color = vmul(spread_term(shape, ds, gm.theta_h, depth, dom_direct), ld3(L.color));
+            }
+        }
+        for (uint32_t i = 0; i < a.n_lights; ++i) {
+            const hg_light& L = a.lights[i];
+            f3 incident;
+            float weight = light_weight(L, world, incident);
+            if ((int)i == dom_light) weight = dom_direct;
+            const bool use = active && weight > 0.0f;
+            const f3 l = safe_normalize(incident);
+            const float sin_i = clampf(dot3(t_n, l), -1.0f, 1.0f);
+            const f3 t_i = sub3(l, mul3s(t_n, sin_i));
+            const float proj = sqrtf(fmaxf(dot3(t_i, t_i) * to2, 1e-8f));
+            const float cos_phi = clampf(dot3(t_i, t_o) / proj, -1.0f, 1.0f);
+            xin[0] = use ? sin_i : 0.0f;
+            xin[1] = use ? sin_o : 0.0f;
+            xin[2] = use ? cos_phi : 1.0f;
+            xin[3] = use ? sqrtf(fmaxf(1.0f - cos_phi * cos_phi, 0.0f)) : 0.0f;
+            mlp::tc::write_input_row(c, xin);
+            float yv[12];
+            if (!mlp::tc::forward(c, yv)) {
+                failed = true;
+                break;
+            }
+            if (use) {
+                f3 lobe = {mlp::decode_fast(yv[0]) + mlp::decode_fast(yv[3]) + mlp::decode_fast(yv[6]),
+                           mlp::decode_fast(yv[1]) + mlp::decode_fast(yv[4]) + mlp::decode_fast(yv[7]),
+                           mlp::decode_fast(yv[2]) + mlp::decode_fast(yv[5]) + mlp::decode_fast(yv[8])};
+                lobe = add3(lobe, mul3s(mk3(mlp::decode_fast(yv[9]), mlp::decode_fast(yv[10]),
+                                            mlp::decode_fast(yv[11])),
+                                        kDensityBack));
+                color = add3(color, mul3s(vmul(lobe, ld3(L.color)), weight));
+            }
+        }
+        if (failed) break;
+        if (active) {
+            if (env.spec) {
+                const f3 fiber_n = safe_normalize(sub3(view, mul3s(tangent, dot3(view, tangent))));
+                const f3 pr = probe_radiance(env, tangent, fiber_n, view, albedo, roughness, p.appearance[1]);
+                color = add3(color, mul3s(pr, pixel_ao(p, low)));
+            }
+            color = mul3s(color, a.exposure);
+            a.shaded[pix] = make_float4(color.x, color.y, color.z, 1.0f);
+            a.shaded_depth[pix] = view_dist;
+        }
+    }
+    if (failed && c.row == 0) atomicOr(err, mlp::tc::kErrTimeout);
+    mlp::tc::teardown(smem_tc, c, failed);
+}
+
 std::mutex g_surrogate_attr_mutex;
 int g_surrogate_per_sm[64] = {};  // resident blocks per SM, 0 until the attribute is set
+bool g_tc_attr[64] = {};
 
 }  // namespace
 
@@ -748,6 +891,30 @@ cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights
     a.ortho = ortho;
     a.exposure = exposure;
     if (model == 1u) {
+        {
+            std::lock_guard<std::mutex> lock(g_surrogate_attr_mutex);
+            if (ctx->device < 0 || ctx->device >= 64) return cudaErrorInvalidDevice;
+            if (!g_tc_attr[ctx->device]) {
+                cudaError_t e = cudaFuncSetAttribute(shade_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)mlp::tc::kSmemBytes);
+                if (e != cudaSuccess) return e;
+                g_tc_attr[ctx->device] = true;
+            }
+        }
+        const uint32_t pixels = ctx->width * ctx->height;
+        cudaError_t e = cudaMemsetAsync(ctx->hair_count, 0, sizeof(uint32_t), ctx->stream);
+        if (e != cudaSuccess) return e;
+        hair_list_kernel<<<(pixels + 255u) / 256u, 256, 0, ctx->stream>>>(ctx->center, pixels, ctx->hair_list,
+                                                                          ctx->hair_count, ctx->shaded,
+                                                                          ctx->shaded_depth);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        // two CTAs per SM: shared memory admits two and together they hold all 512 TMEM columns
+        shade_tc_kernel<<<ctx->sm_count * 2, 256, mlp::tc::kSmemBytes, ctx->stream>>>(
+            a, reinterpret_cast<const __half*>(ctx->surrogate->w16), ctx->surrogate->params, env, ctx->hair_list,
+            ctx->hair_count, ctx->err);
+        return cudaGetLastError();
+    }
+    if (model == 2u) {
         int per_sm = 0;
         {
             std::lock_guard<std::mutex> lock(g_surrogate_attr_mutex);

@@ -13,6 +13,7 @@
 
 #include "hg_internal.h"
 #include "hg_mlp.cuh"
+#include "hg_mlp_tc.cuh"
 
 namespace hg {
 namespace {
@@ -261,6 +262,36 @@ __global__ void __launch_bounds__(kWarps * 32) infer_kernel(const InferArgs a) {
             }
         }
     }
+}
+
+// The same evaluation on tcgen05: two chains of 128 rows per CTA.
+__global__ void __launch_bounds__(256, 2) infer_tc_kernel(const InferArgs a, uint32_t* err) {
+    extern __shared__ __align__(128) uint8_t smem_tc[];
+    tc::Chain c = tc::setup(smem_tc, a.w16, a.params);
+    const uint32_t g = threadIdx.x >> 7;
+    const uint32_t chunks = (a.n + tc::kM - 1) / tc::kM;
+    bool failed = false;
+    for (uint32_t ch = blockIdx.x * tc::kChains + g; ch < chunks; ch += gridDim.x * tc::kChains) {
+        const uint32_t i = ch * tc::kM + c.row;
+        const bool valid = i < a.n;
+        float raw[10], x[10], y[12];
+        load_raw(a.inputs, i, valid, raw);
+        normalise(raw, x);
+        tc::write_input_row(c, x);
+        if (!tc::forward(c, y)) {
+            failed = true;
+            break;
+        }
+        if (valid) {
+#pragma unroll
+            for (int k = 0; k < 12; ++k) {
+                if (a.lobes) a.lobes[(size_t)i * 12 + k] = decode(y[k]);
+                if (a.net) a.net[(size_t)i * 12 + k] = y[k];
+            }
+        }
+    }
+    if (failed && c.row == 0) atomicOr(err, tc::kErrTimeout);
+    tc::teardown(smem_tc, c, failed);
 }
 
 // ------------------------------------------------------------ training
@@ -556,6 +587,7 @@ static_assert(kTrainSmem <= 227 * 1024, "train kernel shared memory");
 std::mutex g_init_mutex;
 bool g_gl_ready[64] = {};
 bool g_attr_ready[64] = {};
+static_assert(tc::kSmemBytes <= 227 * 1024, "tcgen05 kernel shared memory");
 
 // Gauss-Legendre nodes by Newton iteration on P_64, mapped to gamma_i in
 // [-pi/2, pi/2] with the Jacobian cos(gamma_i) folded into the weights.
@@ -604,6 +636,9 @@ cudaError_t ensure_device_setup(int device) {
         e = cudaFuncSetAttribute(infer_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFwdSmem);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrainSmem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tc::kSmemBytes);
         if (e != cudaSuccess) return e;
         g_attr_ready[device] = true;
     }
@@ -696,6 +731,24 @@ cudaError_t run_gradients(hg_mlp* m, const float* inputs, const float* targets, 
 }
 
 }  // namespace
+
+cudaError_t launch_mlp_infer_tc(hg_mlp* m, const float* inputs, uint32_t n, float* lobes, float* net) {
+    InferArgs a;
+    a.inputs = inputs;
+    a.n = n;
+    a.w16 = reinterpret_cast<const __half*>(m->w16);
+    a.params = m->params;
+    a.lobes = lobes;
+    a.net = net;
+    const uint32_t chunks = (n + tc::kM - 1) / tc::kM;
+    uint32_t blocks = (chunks + tc::kChains - 1) / tc::kChains;
+    // two CTAs per SM: shared memory admits two, and together they hold all 512 TMEM columns
+    const uint32_t cap = (uint32_t)m->ctx->sm_count * 2u;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    infer_tc_kernel<<<blocks, 256, tc::kSmemBytes, m->ctx->stream>>>(a, m->ctx->err);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_mlp_infer(hg_mlp* m, const float* inputs, uint32_t n, float* lobes, float* net) {
     InferArgs a;
@@ -814,6 +867,14 @@ hg_status hg_mlp_infer(hg_mlp* m, const float* inputs, uint32_t count, float* lo
     if (count == 0) return HG_OK;
     if (!inputs || (!lobes && !net)) return fail(m->ctx, HG_INVALID_ARG, "null buffer");
     MLP_CUDA(m->ctx, hg::launch_mlp_infer(m, inputs, count, lobes, net));
+    return HG_OK;
+}
+
+hg_status hg_mlp_infer_tc(hg_mlp* m, const float* inputs, uint32_t count, float* lobes, float* net) {
+    if (!m) return HG_INVALID_ARG;
+    if (count == 0) return HG_OK;
+    if (!inputs || (!lobes && !net)) return fail(m->ctx, HG_INVALID_ARG, "null buffer");
+    MLP_CUDA(m->ctx, hg::launch_mlp_infer_tc(m, inputs, count, lobes, net));
     return HG_OK;
 }
 

@@ -104,6 +104,10 @@ class Surrogate:
         """Device float[n][10] inputs -> device float[n][12] decoded lobes and/or raw outputs."""
         self._check(self.lib.hg_mlp_infer(self.handle, _ptr(inputs), n, _ptr(lobes), _ptr(net)))
 
+    def infer_tc(self, inputs, n: int, lobes=None, net=None) -> None:
+        """The same evaluation on the tcgen05 tensor cores (128 rows per MMA, TMEM accumulators)."""
+        self._check(self.lib.hg_mlp_infer_tc(self.handle, _ptr(inputs), n, _ptr(lobes), _ptr(net)))
+
     def gradients(self, inputs, targets, n: int) -> tuple[np.ndarray, float]:
         """Gradient of sum((net - target)^2) over one device batch, and that sum."""
         g = np.empty(abi.MLP_PARAMS, dtype=np.float32)

@@ -151,7 +151,8 @@ typedef struct hg_shade_desc {
     uint32_t light_count;
     uint32_t ortho;           /* 1 when the camera projection is orthographic */
     float exposure;           /* view.exposure */
-    uint32_t shade_model;     /* 0: Karis fit (shade.wesl), 1: learned surrogate */
+    uint32_t shade_model;     /* 0: Karis fit (shade.wesl); 1: learned surrogate on tcgen05;
+                                 2: the surrogate on mma.sync (for comparison) */
 } hg_shade_desc;
 
 /* Buffers a context owns. */
@@ -467,6 +468,10 @@ hg_status hg_mlp_samples(hg_ctx* ctx, uint64_t seed, uint64_t first, uint32_t co
  * float[count][12] (decoded, nullable); net float[count][12] (raw outputs,
  * nullable). */
 hg_status hg_mlp_infer(hg_mlp* mlp, const float* inputs, uint32_t count, float* lobes, float* net);
+/* The same evaluation on the tcgen05 tensor cores: 128 rows per MMA,
+ * accumulators in tensor memory, biases as two extra FP16 (high, low)
+ * product columns.  Outputs match hg_mlp_infer to FP16 rounding. */
+hg_status hg_mlp_infer_tc(hg_mlp* mlp, const float* inputs, uint32_t count, float* lobes, float* net);
 /* Gradient of the sum over samples and outputs of (net - target)^2 for one
  * batch (device inputs/targets), into host float[HG_MLP_PARAMS]; the loss sum
  * into *loss (nullable).  Parameters are unchanged. */

@@ -260,6 +260,29 @@ def test_network_forward_matches_the_oracle_emulation(renderer, which):
 
 
 @gpu
+@pytest.mark.parametrize("n", [5000, 128, 77])
+def test_tcgen05_inference_matches_mma_sync_and_the_oracle(renderer, n):
+    torch, dev = _torch()
+    p = S.load_params()
+    s = S.Surrogate(renderer, p)
+    xs = _inputs(n, 13)
+    x = torch.from_numpy(xs).to(dev)
+    net_tc = torch.full((n, 12), float("nan"), dtype=torch.float32, device=dev)
+    lob_tc = torch.empty((n, 12), dtype=torch.float32, device=dev)
+    net_ms = torch.empty((n, 12), dtype=torch.float32, device=dev)
+    s.infer_tc(x, n, lob_tc, net_tc)
+    s.infer(x, n, None, net_ms)
+    assert renderer.synchronize() == 0
+    tc, ms = net_tc.cpu().numpy(), net_ms.cpu().numpy()
+    assert np.isfinite(tc).all()
+    want = oracle.mlp_forward(p, xs)
+    assert np.abs(tc - ms).mean() < 2e-3 and np.abs(tc - want).mean() < 2e-3
+    np.testing.assert_allclose(tc, ms, rtol=0, atol=5e-2)
+    np.testing.assert_allclose(lob_tc.cpu().numpy(), 1e-3 * np.expm1(np.maximum(tc, 0)), rtol=1e-5, atol=1e-9)
+    s.close()
+
+
+@gpu
 def test_gradients_match_the_fp64_reference(renderer):
     torch, dev = _torch()
     n = 3000  # not a multiple of 32: the ragged last warp must contribute nothing extra
@@ -308,7 +331,8 @@ def test_training_reduces_the_loss(renderer):
 
 
 @gpu
-def test_shade_model_one_matches_the_oracle(renderer):
+@pytest.mark.parametrize("model", [abi.SHADE_SURROGATE, abi.SHADE_SURROGATE_MMA])
+def test_shade_model_one_matches_the_oracle(renderer, model):
     sc = configs.config2(scale=0.02)
     cam, dom = sc.params()
     lights = sc.light_array()
@@ -318,11 +342,11 @@ def test_shade_model_one_matches_the_oracle(renderer):
     renderer.render_groom(g, cam, dom, lights)  # G-buffer and map
     assert renderer.synchronize() == 0
     with pytest.raises(abi.HairGbError):
-        renderer.shade(cam, lights, model=abi.SHADE_SURROGATE)  # nothing bound
+        renderer.shade(cam, lights, model=model)  # nothing bound
     p = S.load_params()
     s = S.Surrogate(renderer, p)
     renderer.bind_surrogate(s)
-    renderer.shade(cam, lights, model=abi.SHADE_SURROGATE)
+    renderer.shade(cam, lights, model=model)
     assert renderer.synchronize() == 0
     center, beta, dmap = renderer.read(abi.BUF_CENTER), renderer.read(abi.BUF_BETA), renderer.read(abi.BUF_DOM)
     shaded, sdepth = renderer.read(abi.BUF_SHADED), renderer.read(abi.BUF_SHADED_DEPTH)
@@ -335,7 +359,7 @@ def test_shade_model_one_matches_the_oracle(renderer):
     assert S.relative_l1(got, want) < 2e-3
     np.testing.assert_allclose(got, want, rtol=3e-2, atol=1e-3 * np.abs(want).max())
     # the frame entry point takes the same model
-    renderer.render_groom(g, cam, dom, lights, model=abi.SHADE_SURROGATE)
+    renderer.render_groom(g, cam, dom, lights, model=model)
     assert renderer.synchronize() == 0
     np.testing.assert_array_equal(renderer.read(abi.BUF_SHADED), shaded)
     renderer.bind_surrogate(None)
