@@ -6,12 +6,15 @@
 // weights are the FP16 high and low parts of the bias, which keeps the bias
 // to ~2^-22 relative.
 //
-// A "chain" is one warpgroup (4 warps, 128 threads; thread r owns row r) with
-// its own input tile X (128 x 16), hidden tile H (128 x 80), 80 TMEM columns
-// and an mbarrier.  Per layer one thread issues the MMAs and commits them to
-// the mbarrier; all 128 threads wait (bounded), read their row of the
-// accumulator with tcgen05.ld, apply ReLU + FP16 conversion and write it as
-// the next layer's input row.
+// A "chain" is one warpgroup (4 warps, 128 threads; thread r owns row r) that
+// runs two evaluations at once, each with its own input tile X (128 x 16),
+// hidden tile H (128 x 80), 64 TMEM columns and mbarrier.  Per layer one
+// thread issues an evaluation's MMAs and commits them to its mbarrier; all
+// 128 threads wait (bounded), read their row of the accumulator with
+// tcgen05.ld, apply ReLU + FP16 conversion and write it as the next layer's
+// input row.  While the warps work on one evaluation's accumulator the
+// tensor core runs the other's layer.  A CTA holds four chains (512
+// threads), all of the SM's 512 TMEM columns and 227 KB of shared memory.
 //
 // Shared-memory operand layout (K-major, no swizzle): 8 x 16-byte core
 // matrices; element (row, k) at (row/8)*SBO + (k/8)*LBO + (row%8)*16 + (k%8)*2
@@ -43,11 +46,16 @@ constexpr uint32_t kOffW4 = kOffW3 + kHid * kKhid * 2;
 constexpr uint32_t kOffW5 = kOffW4 + kHid * kKhid * 2;
 constexpr uint32_t kWeightBytes = kOffW5 + kOut * kKhid * 2;  // 35,328
 constexpr uint32_t kXBytes = kM * kKin * 2, kHBytes = kM * kKhid * 2;
-constexpr uint32_t kGroupBytes = kXBytes + kHBytes;
-constexpr uint32_t kChains = 2;
-constexpr uint32_t kOffBar = kWeightBytes + kChains * kGroupBytes;  // two mbarriers, then the TMEM address
-constexpr uint32_t kSmemBytes = kOffBar + 64;
-constexpr uint32_t kTmemCols = 256;  // 128 per chain: hidden accumulator at +0 (64), output at +64 (16)
+constexpr uint32_t kEvals = 2;    // evaluations in flight per chain
+constexpr uint32_t kChains = 4;   // warpgroups per CTA
+constexpr uint32_t kEvalBytes = kXBytes + kHBytes;
+constexpr uint32_t kGroupBytes = kEvals * kEvalBytes;
+constexpr uint32_t kOffBar = kWeightBytes + kChains * kGroupBytes;  // kChains * kEvals mbarriers, then the TMEM address
+constexpr uint32_t kOffSlot = kOffBar + 8 * kChains * kEvals;
+constexpr uint32_t kSmemBytes = kOffSlot + 16;
+constexpr uint32_t kTmemCols = 512;  // per chain 128: per evaluation 64 (hidden accumulator; the output reuses 0..15)
+constexpr uint32_t kThreads = 128 * kChains;
+static_assert(kSmemBytes <= 232448, "shared memory per CTA");
 static_assert(kWeightBytes % 128 == 0 && kGroupBytes % 128 == 0, "tile alignment");
 // Instruction descriptors (kind::f16): D F32, A and B F16, both K-major, M = 128.
 constexpr uint32_t kIdescHid = (1u << 4) | ((64u >> 3) << 17) | ((kM >> 4) << 24);
@@ -205,27 +213,28 @@ __device__ __forceinline__ void load_weights(uint8_t* smem, const __half* __rest
 }
 
 struct Chain {
-    uint32_t w;       // shared address of the weights
-    uint32_t x, h;    // shared addresses of this chain's tiles
-    uint32_t mbar;    // shared address of its mbarrier
-    uint32_t tmem;    // TMEM address of its accumulators (lane 0)
-    uint32_t phase;   // parity of the next mbarrier phase
-    uint32_t bar_id;  // named barrier of the warpgroup
-    uint32_t row;     // this thread's row, 0..127
+    uint32_t w;              // shared address of the weights
+    uint32_t x[kEvals];      // shared addresses of the input tiles
+    uint32_t h[kEvals];      // and of the hidden tiles
+    uint32_t mbar[kEvals];   // shared addresses of the mbarriers
+    uint32_t tmem[kEvals];   // TMEM addresses of the accumulators (lane 0)
+    uint32_t phase[kEvals];  // parity of each mbarrier's next phase
+    uint32_t bar_id;         // named barrier of the warpgroup
+    uint32_t row;            // this thread's row, 0..127
 };
 
-// Row r of H: the constant columns 64..79 (1, 1, then zeros), written once.
-__device__ __forceinline__ void init_hidden_row(const Chain& c) {
+// Row r of an H tile: the constant columns 64..79 (1, 1, then zeros), written once.
+__device__ __forceinline__ void init_hidden_row(uint32_t h, uint32_t row) {
     const uint32_t one2 = 0x3C003C00u;  // two FP16 ones
-    st_shared_v4(c.h + canon(c.row, 64, kSboHid), one2, 0u, 0u, 0u);
-    st_shared_v4(c.h + canon(c.row, 72, kSboHid), 0u, 0u, 0u, 0u);
+    st_shared_v4(h + canon(row, 64, kSboHid), one2, 0u, 0u, 0u);
+    st_shared_v4(h + canon(row, 72, kSboHid), 0u, 0u, 0u, 0u);
 }
 
-// Row r of X from the normalised inputs (columns 10, 11 are the bias ones).
-__device__ __forceinline__ void write_input_row(const Chain& c, const float x[kUsedIn]) {
-    st_shared_v4(c.x + canon(c.row, 0, kSboIn), pack_h2(x[0], x[1]), pack_h2(x[2], x[3]), pack_h2(x[4], x[5]),
+// Row r of evaluation e's X from the normalised inputs (columns 10, 11 are the bias ones).
+__device__ __forceinline__ void write_input_row(const Chain& c, uint32_t e, const float x[kUsedIn]) {
+    st_shared_v4(c.x[e] + canon(c.row, 0, kSboIn), pack_h2(x[0], x[1]), pack_h2(x[2], x[3]), pack_h2(x[4], x[5]),
                  pack_h2(x[6], x[7]));
-    st_shared_v4(c.x + canon(c.row, 8, kSboIn), pack_h2(x[8], x[9]), 0x3C003C00u, 0u, 0u);
+    st_shared_v4(c.x[e] + canon(c.row, 8, kSboIn), pack_h2(x[8], x[9]), 0x3C003C00u, 0u, 0u);
 }
 
 __device__ __forceinline__ void issue(uint32_t d, uint32_t a, uint32_t a_sbo, uint32_t b, uint32_t b_sbo,
@@ -234,98 +243,120 @@ __device__ __forceinline__ void issue(uint32_t d, uint32_t a, uint32_t a_sbo, ui
         mma(d, desc(a + ks * 2u * kLbo, a_sbo), desc(b + ks * 2u * kLbo, b_sbo), idesc, ks);
 }
 
-// One evaluation of the 128 rows whose inputs are in X: y[] receives this
-// thread's 12 network outputs.  Every thread of the warpgroup calls it.
-// Returns false (for the whole warpgroup) when an MMA did not complete in
-// time; the chain is then unusable.
-__device__ __forceinline__ bool forward(Chain& c, float y[kUsedOut]) {
+// Epilogue of one hidden layer of evaluation e: accumulator -> ReLU -> FP16 -> H row.
+__device__ __forceinline__ void hidden_epilogue(const Chain& c, uint32_t e) {
     const uint32_t lane_base = (c.row & ~31u) << 16;
+    uint32_t v[64];
+    tmem_ld32(c.tmem[e] + lane_base, v);
+    tmem_ld32(c.tmem[e] + lane_base + 32u, v + 32);
+    tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        st_shared_v4(c.h[e] + canon(c.row, 8u * j, kSboHid),
+                     pack_relu(__uint_as_float(v[8 * j]), __uint_as_float(v[8 * j + 1])),
+                     pack_relu(__uint_as_float(v[8 * j + 2]), __uint_as_float(v[8 * j + 3])),
+                     pack_relu(__uint_as_float(v[8 * j + 4]), __uint_as_float(v[8 * j + 5])),
+                     pack_relu(__uint_as_float(v[8 * j + 6]), __uint_as_float(v[8 * j + 7])));
+}
+
+// The evaluations whose inputs are in X[0] (and X[1] when `two`): y0 / y1
+// receive this thread's 12 network outputs of each.  Every thread of the
+// warpgroup calls it with the same `two`.  Returns false (for the whole
+// warpgroup) when an MMA did not complete in time; the chain is then
+// unusable.
+__device__ __forceinline__ bool forward2(Chain& c, bool two, float y0[kUsedOut], float y1[kUsedOut]) {
+    const uint32_t ne = two ? 2u : 1u;
     fence_proxy_async();
     if (group_sync_or(c.bar_id, false)) return false;
     if (c.row == 0) {
         fence_after();
-        issue(c.tmem, c.x, kSboIn, c.w + kOffW1, kSboIn, kKin / 16, kIdescHid);
-        commit(c.mbar);
+        for (uint32_t e = 0; e < ne; ++e) {
+            issue(c.tmem[e], c.x[e], kSboIn, c.w + kOffW1, kSboIn, kKin / 16, kIdescHid);
+            commit(c.mbar[e]);
+        }
     }
     const uint32_t next_w[4] = {kOffW2, kOffW3, kOffW4, kOffW5};
     for (int layer = 0; layer < 4; ++layer) {
-        const bool ok = mbar_wait(c.mbar, c.phase);
-        if (ok) c.phase ^= 1u;  // after a timeout the phase stays the outstanding one
-        fence_after();
-        uint32_t v[64];
-        tmem_ld32(c.tmem + lane_base, v);
-        tmem_ld32(c.tmem + lane_base + 32u, v + 32);
-        tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 8; ++j)
-            st_shared_v4(c.h + canon(c.row, 8u * j, kSboHid),
-                         pack_relu(__uint_as_float(v[8 * j]), __uint_as_float(v[8 * j + 1])),
-                         pack_relu(__uint_as_float(v[8 * j + 2]), __uint_as_float(v[8 * j + 3])),
-                         pack_relu(__uint_as_float(v[8 * j + 4]), __uint_as_float(v[8 * j + 5])),
-                         pack_relu(__uint_as_float(v[8 * j + 6]), __uint_as_float(v[8 * j + 7])));
-        fence_proxy_async();
-        fence_before();
-        if (group_sync_or(c.bar_id, !ok)) return false;
-        if (c.row == 0) {
+        for (uint32_t e = 0; e < ne; ++e) {
+            const bool ok = mbar_wait(c.mbar[e], c.phase[e]);
+            if (ok) c.phase[e] ^= 1u;  // after a timeout the phase stays the outstanding one
             fence_after();
-            if (layer < 3) issue(c.tmem, c.h, kSboHid, c.w + next_w[layer], kSboHid, kKhid / 16, kIdescHid);
-            else issue(c.tmem + 64u, c.h, kSboHid, c.w + next_w[layer], kSboHid, kKhid / 16, kIdescOut);
-            commit(c.mbar);
+            hidden_epilogue(c, e);
+            fence_proxy_async();
+            fence_before();
+            if (group_sync_or(c.bar_id, !ok)) return false;
+            if (c.row == 0) {
+                fence_after();
+                if (layer < 3)
+                    issue(c.tmem[e], c.h[e], kSboHid, c.w + next_w[layer], kSboHid, kKhid / 16, kIdescHid);
+                else
+                    issue(c.tmem[e], c.h[e], kSboHid, c.w + next_w[layer], kSboHid, kKhid / 16, kIdescOut);
+                commit(c.mbar[e]);
+            }
         }
     }
-    const bool ok = mbar_wait(c.mbar, c.phase);
-    if (ok) c.phase ^= 1u;
-    fence_after();
-    uint32_t o[16];
-    tmem_ld16(c.tmem + lane_base + 64u, o);
-    tmem_wait_ld();
+    const uint32_t lane_base = (c.row & ~31u) << 16;
+    bool ok_all = true;
+    for (uint32_t e = 0; e < ne; ++e) {
+        const bool ok = mbar_wait(c.mbar[e], c.phase[e]);
+        if (ok) c.phase[e] ^= 1u;
+        ok_all = ok_all && ok;
+        fence_after();
+        uint32_t o[16];
+        tmem_ld16(c.tmem[e] + lane_base, o);
+        tmem_wait_ld();
+        float* y = e == 0 ? y0 : y1;
 #pragma unroll
-    for (int i = 0; i < kUsedOut; ++i) y[i] = __uint_as_float(o[i]);
+        for (int i = 0; i < kUsedOut; ++i) y[i] = __uint_as_float(o[i]);
+    }
     fence_before();
-    return !group_sync_or(c.bar_id, !ok);
+    return !group_sync_or(c.bar_id, !ok_all);
 }
 
-// CTA set-up: weights, the chains' constant columns, mbarriers, TMEM.  Every
-// thread calls it; returns this thread's chain.
+// CTA set-up: weights, the constant columns of every H tile, mbarriers, TMEM.
+// Every thread calls it; returns this thread's chain.
 __device__ __forceinline__ Chain setup(uint8_t* smem, const __half* w16, const float* params) {
     const uint32_t tid = threadIdx.x, g = tid >> 7;
     const uint32_t base = smem_addr(smem);
     Chain c;
     c.w = base;
-    c.x = base + kWeightBytes + g * kGroupBytes;
-    c.h = c.x + kXBytes;
-    c.mbar = base + kOffBar + 8u * g;
-    c.phase = 0;
     c.bar_id = 1u + g;
     c.row = tid & 127u;
+    for (uint32_t e = 0; e < kEvals; ++e) {
+        c.x[e] = base + kWeightBytes + g * kGroupBytes + e * kEvalBytes;
+        c.h[e] = c.x[e] + kXBytes;
+        c.mbar[e] = base + kOffBar + 8u * (g * kEvals + e);
+        c.phase[e] = 0;
+        init_hidden_row(c.h[e], c.row);
+    }
     load_weights(smem, w16, params, (int)tid, (int)blockDim.x);
-    init_hidden_row(c);
     if (tid == 0) {
-        for (uint32_t k = 0; k < kChains; ++k) mbar_init(base + kOffBar + 8u * k, 1);
+        for (uint32_t k = 0; k < kChains * kEvals; ++k) mbar_init(base + kOffBar + 8u * k, 1);
         fence_mbar_init();
     }
     if (tid < 32) {
-        tmem_alloc(base + kOffBar + 32u, kTmemCols);
+        tmem_alloc(base + kOffSlot, kTmemCols);
         tmem_relinquish();
     }
     fence_proxy_async();
     fence_before();
     __syncthreads();
     fence_after();
-    const uint32_t tbase = *reinterpret_cast<volatile uint32_t*>(smem + kOffBar + 32u);
-    c.tmem = tbase + g * 128u;
+    const uint32_t tbase = *reinterpret_cast<volatile uint32_t*>(smem + kOffSlot);
+    for (uint32_t e = 0; e < kEvals; ++e) c.tmem[e] = tbase + g * 128u + e * 64u;
     return c;
 }
 
-// CTA tear-down after every chain has finished (or given up): a bounded wait
-// for a chain's last commit if it failed, then the TMEM is freed.
+// CTA tear-down after every chain has finished (or given up): bounded waits
+// for a failed chain's outstanding commits, then the TMEM is freed.
 __device__ __forceinline__ void teardown(uint8_t* smem, Chain& c, bool failed) {
-    if (failed) (void)mbar_wait(c.mbar, c.phase);
+    if (failed)
+        for (uint32_t e = 0; e < kEvals; ++e) (void)mbar_wait(c.mbar[e], c.phase[e]);
     fence_before();
     __syncthreads();
     if (threadIdx.x < 32) {
         fence_after();
-        tmem_dealloc(*reinterpret_cast<volatile uint32_t*>(smem + kOffBar + 32u), kTmemCols);
+        tmem_dealloc(*reinterpret_cast<volatile uint32_t*>(smem + kOffSlot), kTmemCols);
     }
 }
 

@@ -722,6 +722,8 @@ __global__ void karis_lobes_kernel(const float* __restrict__ in, uint32_t n, flo
 // own chunks, one network evaluation per light.  The light loop, the DOM
 // spread and the probe are those of shade_surrogate_kernel.
 
+constexpr uint32_t kLightsPerStep = 1;
+
 // Pixels whose centre word is not empty, appended in warp order; the others
 // get the empty shade outputs.
 __global__ void hair_list_kernel(const unsigned long long* __restrict__ center, uint32_t pixels,
@@ -744,7 +746,7 @@ __global__ void hair_list_kernel(const unsigned long long* __restrict__ center, 
     if (hair) list[base + __popc(m & ((1u << lane) - 1u))] = pix;
 }
 
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(mlp::tc::kThreads, 1)
     shade_tc_kernel(const ShadeArgs a, const __half* __restrict__ w16, const float* __restrict__ mparams,
                     const EnvArgs env, const uint32_t* __restrict__ list, const uint32_t* __restrict__ count,
                     uint32_t* __restrict__ err) {
@@ -809,35 +811,42 @@ __global__ void __launch_bounds__(256, 2)
                 color = vmul(spread_term(shape, ds, gm.theta_h, depth, dom_direct), ld3(L.color));
             }
         }
-        for (uint32_t i = 0; i < a.n_lights; ++i) {
-            const hg_light& L = a.lights[i];
-            f3 incident;
-            float weight = light_weight(L, world, incident);
-            if ((int)i == dom_light) weight = dom_direct;
-            const bool use = active && weight > 0.0f;
-            const f3 l = safe_normalize(incident);
-            const float sin_i = clampf(dot3(t_n, l), -1.0f, 1.0f);
-            const f3 t_i = sub3(l, mul3s(t_n, sin_i));
-            const float proj = sqrtf(fmaxf(dot3(t_i, t_i) * to2, 1e-8f));
-            const float cos_phi = clampf(dot3(t_i, t_o) / proj, -1.0f, 1.0f);
-            xin[0] = use ? sin_i : 0.0f;
-            xin[1] = use ? sin_o : 0.0f;
-            xin[2] = use ? cos_phi : 1.0f;
-            xin[3] = use ? sqrtf(fmaxf(1.0f - cos_phi * cos_phi, 0.0f)) : 0.0f;
-            mlp::tc::write_input_row(c, xin);
-            float yv[12];
-            if (!mlp::tc::forward(c, yv)) {
+        // lights two at a time: the chain's two evaluations
+        for (uint32_t i = 0; i < a.n_lights; i += kLightsPerStep) {
+            const bool two = kLightsPerStep == 2 && i + 1 < a.n_lights;
+            float weight[2] = {0.0f, 0.0f};
+            for (uint32_t e = 0; e < (two ? 2u : 1u); ++e) {
+                const hg_light& L = a.lights[i + e];
+                f3 incident;
+                float w = light_weight(L, world, incident);
+                if ((int)(i + e) == dom_light) w = dom_direct;
+                const bool use = active && w > 0.0f;
+                weight[e] = use ? w : 0.0f;
+                const f3 l = safe_normalize(incident);
+                const float sin_i = clampf(dot3(t_n, l), -1.0f, 1.0f);
+                const f3 t_i = sub3(l, mul3s(t_n, sin_i));
+                const float proj = sqrtf(fmaxf(dot3(t_i, t_i) * to2, 1e-8f));
+                const float cos_phi = clampf(dot3(t_i, t_o) / proj, -1.0f, 1.0f);
+                xin[0] = use ? sin_i : 0.0f;
+                xin[1] = use ? sin_o : 0.0f;
+                xin[2] = use ? cos_phi : 1.0f;
+                xin[3] = use ? sqrtf(fmaxf(1.0f - cos_phi * cos_phi, 0.0f)) : 0.0f;
+                mlp::tc::write_input_row(c, e, xin);
+            }
+            float yv[2][12];
+            if (!mlp::tc::forward2(c, two, yv[0], yv[1])) {
                 failed = true;
                 break;
             }
-            if (use) {
-                f3 lobe = {mlp::decode_fast(yv[0]) + mlp::decode_fast(yv[3]) + mlp::decode_fast(yv[6]),
-                           mlp::decode_fast(yv[1]) + mlp::decode_fast(yv[4]) + mlp::decode_fast(yv[7]),
-                           mlp::decode_fast(yv[2]) + mlp::decode_fast(yv[5]) + mlp::decode_fast(yv[8])};
-                lobe = add3(lobe, mul3s(mk3(mlp::decode_fast(yv[9]), mlp::decode_fast(yv[10]),
-                                            mlp::decode_fast(yv[11])),
+            for (uint32_t e = 0; e < (two ? 2u : 1u); ++e) {
+                if (!(weight[e] > 0.0f)) continue;
+                const float* q = yv[e];
+                f3 lobe = {mlp::decode_fast(q[0]) + mlp::decode_fast(q[3]) + mlp::decode_fast(q[6]),
+                           mlp::decode_fast(q[1]) + mlp::decode_fast(q[4]) + mlp::decode_fast(q[7]),
+                           mlp::decode_fast(q[2]) + mlp::decode_fast(q[5]) + mlp::decode_fast(q[8])};
+                lobe = add3(lobe, mul3s(mk3(mlp::decode_fast(q[9]), mlp::decode_fast(q[10]), mlp::decode_fast(q[11])),
                                         kDensityBack));
-                color = add3(color, mul3s(vmul(lobe, ld3(L.color)), weight));
+                color = add3(color, mul3s(vmul(lobe, ld3(a.lights[i + e].color)), weight[e]));
             }
         }
         if (failed) break;
@@ -908,8 +917,8 @@ cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights
                                                                           ctx->hair_count, ctx->shaded,
                                                                           ctx->shaded_depth);
         if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        // two CTAs per SM: shared memory admits two and together they hold all 512 TMEM columns
-        shade_tc_kernel<<<ctx->sm_count * 2, 256, mlp::tc::kSmemBytes, ctx->stream>>>(
+        // one CTA per SM: it holds all 512 TMEM columns and most of the shared memory
+        shade_tc_kernel<<<ctx->sm_count, mlp::tc::kThreads, mlp::tc::kSmemBytes, ctx->stream>>>(
             a, reinterpret_cast<const __half*>(ctx->surrogate->w16), ctx->surrogate->params, env, ctx->hair_list,
             ctx->hair_count, ctx->err);
         return cudaGetLastError();

@@ -264,29 +264,37 @@ __global__ void __launch_bounds__(kWarps * 32) infer_kernel(const InferArgs a) {
     }
 }
 
-// The same evaluation on tcgen05: two chains of 128 rows per CTA.
-__global__ void __launch_bounds__(256, 2) infer_tc_kernel(const InferArgs a, uint32_t* err) {
+// The same evaluation on tcgen05: four chains of two 128-row evaluations per CTA.
+__global__ void __launch_bounds__(tc::kThreads, 1) infer_tc_kernel(const InferArgs a, uint32_t* err) {
     extern __shared__ __align__(128) uint8_t smem_tc[];
     tc::Chain c = tc::setup(smem_tc, a.w16, a.params);
     const uint32_t g = threadIdx.x >> 7;
     const uint32_t chunks = (a.n + tc::kM - 1) / tc::kM;
+    const uint32_t pairs = (chunks + 1) / 2;
     bool failed = false;
-    for (uint32_t ch = blockIdx.x * tc::kChains + g; ch < chunks; ch += gridDim.x * tc::kChains) {
-        const uint32_t i = ch * tc::kM + c.row;
-        const bool valid = i < a.n;
-        float raw[10], x[10], y[12];
-        load_raw(a.inputs, i, valid, raw);
-        normalise(raw, x);
-        tc::write_input_row(c, x);
-        if (!tc::forward(c, y)) {
+    for (uint32_t pc = blockIdx.x * tc::kChains + g; pc < pairs; pc += gridDim.x * tc::kChains) {
+        const bool two = 2 * pc + 1 < chunks;
+        uint32_t idx[2];
+        bool valid[2];
+        for (uint32_t e = 0; e < 2; ++e) {
+            idx[e] = (2 * pc + e) * tc::kM + c.row;
+            valid[e] = idx[e] < a.n && (e == 0 || two);
+            float raw[10], x[10];
+            load_raw(a.inputs, idx[e], valid[e], raw);
+            normalise(raw, x);
+            tc::write_input_row(c, e, x);
+        }
+        float y[2][12];
+        if (!tc::forward2(c, two, y[0], y[1])) {
             failed = true;
             break;
         }
-        if (valid) {
+        for (uint32_t e = 0; e < 2; ++e) {
+            if (!valid[e]) continue;
 #pragma unroll
             for (int k = 0; k < 12; ++k) {
-                if (a.lobes) a.lobes[(size_t)i * 12 + k] = decode(y[k]);
-                if (a.net) a.net[(size_t)i * 12 + k] = y[k];
+                if (a.lobes) a.lobes[(size_t)idx[e] * 12 + k] = decode(y[e][k]);
+                if (a.net) a.net[(size_t)idx[e] * 12 + k] = y[e][k];
             }
         }
     }
@@ -740,13 +748,13 @@ cudaError_t launch_mlp_infer_tc(hg_mlp* m, const float* inputs, uint32_t n, floa
     a.params = m->params;
     a.lobes = lobes;
     a.net = net;
-    const uint32_t chunks = (n + tc::kM - 1) / tc::kM;
-    uint32_t blocks = (chunks + tc::kChains - 1) / tc::kChains;
-    // two CTAs per SM: shared memory admits two, and together they hold all 512 TMEM columns
-    const uint32_t cap = (uint32_t)m->ctx->sm_count * 2u;
+    const uint32_t pairs = ((n + tc::kM - 1) / tc::kM + 1) / 2;
+    uint32_t blocks = (pairs + tc::kChains - 1) / tc::kChains;
+    // one CTA per SM: it holds all 512 TMEM columns and most of the shared memory
+    const uint32_t cap = (uint32_t)m->ctx->sm_count;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    infer_tc_kernel<<<blocks, 256, tc::kSmemBytes, m->ctx->stream>>>(a, m->ctx->err);
+    infer_tc_kernel<<<blocks, tc::kThreads, tc::kSmemBytes, m->ctx->stream>>>(a, m->ctx->err);
     return cudaGetLastError();
 }
 
