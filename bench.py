@@ -535,6 +535,11 @@ def run_ours(args, rank, world, local):
         traffic, traffic_src = tj["per_launch"][dominant]["dram_bytes"], tj["profile"]
     except (OSError, KeyError, ValueError):
         pass
+    per_pass_roofline = {
+        p: {"bytes": int(nbytes[p]), "ms": round(acc[p], 4),
+            "gbs": round(nbytes[p] / (acc[p] * 1e-3) / 1e9, 1) if acc[p] > 0 else None,
+            "frac_of_hbm": round(nbytes[p] / (acc[p] * 1e-3) / 1e9 / peak, 4) if acc[p] > 0 else None}
+        for p in nbytes}
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 2), "peak": peak,
                 "peak_source": peak_kind, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "traffic": traffic, "traffic_source": traffic_src, "bytes_per_launch": nbytes[dominant],
@@ -613,6 +618,7 @@ def run_ours(args, rank, world, local):
                    "lights": int(len(lights)), "l2": "flushed between timed steps (256 MB device write)",
                    "parallelism": f"replicas x{world}"},
         "per_pass_ms": per_pass,
+        "per_pass_roofline": per_pass_roofline,
         "roofline": roofline,
         "surrogate": surr,
         "batch": batch,
@@ -625,25 +631,25 @@ def run_ours(args, rank, world, local):
 
 
 def cpu_baseline(args, sample: bool) -> dict:
-    """The oracle on a scaled copy of the workload, all host cores."""
-    import oracle
+    """The oracle on a scaled copy of the workload, all host cores: one warm-up
+    frame, then the median of three frames, per pass (oracle/timing.py)."""
+    from oracle import timing
     from bevy_hair_gb300 import configs
 
     scale = args.cpu_scale
     threads = os.cpu_count() or 1
-    oracle.set_threads(threads)
     sc = configs.CONFIGS[args.config](scale)
     cam, dom = sc.params()
     lights = sc.light_array()
     t = time.perf_counter()
-    out = oracle.frame(sc.mesh, cam, dom, lights, env=bench_env(args.config))
+    r = timing.per_pass(sc.mesh, cam, dom, lights, env=bench_env(args.config), runs=3, threads=threads)
     dt = time.perf_counter() - t
-    segs = int(out["counts_camera"]["segments"])
-    return {"value": round(segs / dt / 1e9, 6), "unit": "Gseg/s", "cores": threads, "kind": "port",
-            "counts_camera": out["counts_camera"],
-            "sample": (f"one whole frame of config{args.config} at scale {scale}: {sc.mesh.strand_count()} "
-                       f"strands, {sc.view.width}x{sc.view.height}, DOM {sc.dom_size[0]}^2, "
-                       f"{segs} camera segments, {dt:.2f} s"),
+    segs = r["camera_segments"]
+    return {"value": r["gseg_per_s"], "unit": "Gseg/s", "cores": threads, "kind": "port",
+            "counts_camera": r["counts_camera"], "per_pass_ms": r["per_pass_ms"], "ms_per_frame": r["frame_ms"],
+            "sample": (f"config{args.config} at scale {scale}: {sc.mesh.strand_count()} strands, "
+                       f"{sc.view.width}x{sc.view.height}, DOM {sc.dom_size[0]}^2, {segs} camera segments; "
+                       f"1 warm-up + median of 3 frames, {dt:.1f} s in all"),
             "seconds": round(dt, 3)}
 
 
