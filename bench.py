@@ -290,7 +290,8 @@ def pass_bytes(sc, seg_refs: dict) -> dict:
         "raster_dom_layers": 68 * tex + 65 * 16 * seg_refs["dom_refs"],
         "shade": 12 * px + 20 * px + 4 * 68 * seg_refs["hair_pixels"],
         "filter": 32 * px + 20 * px,
-        "composite": 20 * px + 40 * px,
+        # colour alpha of every pixel; depth source, target colour and depth (read + write) where covered
+        "composite": 16 * px + (4 + 16 + 16 + 4 + 4) * seg_refs["covered_pixels"],
     }
 
 
@@ -458,6 +459,7 @@ def run_ours(args, rank, world, local):
     seg_c = configs.segments_of(g.read(abi.SLOT_CAMERA, abi.GBUF_REFS), ref_c)
     seg_d = configs.segments_of(g.read(abi.SLOT_DOM, abi.GBUF_REFS), ref_d)
     hair_px = int((r.read(abi.BUF_CENTER) != np.uint64(0xFFFFFFFFFFFFFFFF)).sum())
+    covered_px = int((r.read(abi.BUF_FILTERED).reshape(-1, 4)[:, 3] >= 0.001).sum())
 
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
 
@@ -525,7 +527,7 @@ def run_ours(args, rank, world, local):
         r.set_environment(None)  # config 4 has no light probe
         batch = batch_measure(r, stream, flush, max(5, min(args.steps, 10)), 3, args.batch_scale)
     nbytes = pass_bytes(sc, {"camera_refs": ref_c, "dom_refs": ref_d, "hair_pixels": hair_px,
-                             "strands": sc.mesh.strand_count()})
+                             "strands": sc.mesh.strand_count(), "covered_pixels": covered_px})
     dominant = max((p for p in nbytes), key=lambda p: acc[p])
     peak, peak_kind = peaks()
     achieved = nbytes[dominant] / (acc[dominant] * 1e-3) / 1e9
@@ -571,7 +573,10 @@ def run_ours(args, rank, world, local):
         e2e_step()
         e2e_total += time.perf_counter() - t_s
     e2e_value, e2e_ms, _ = aggregate(dist, e2e_total * 1e3, float(seg_c) * args.steps)
-    launches = 16 * args.steps
+    # per frame: clear, 2 x lod, 2 x (scan offsets + expand), clear_dom, generate,
+    # camera raster (2 stages + tile depths between them), 2 x DOM raster,
+    # shade, filter, clear_color, composite
+    launches = 18 * args.steps
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -53,6 +53,7 @@ void free_targets(hg_ctx* ctx) {
     free_dev(ctx->depth);
     free_dev(ctx->hair_list);
     free_dev(ctx->hair_count);
+    free_dev(ctx->tile_depth);
     ctx->width = ctx->height = ctx->dom_w = ctx->dom_h = 0;
 }
 
@@ -277,6 +278,7 @@ hg_status hg_ensure_targets(hg_ctx* ctx, uint32_t width, uint32_t height, uint32
     alloc(ctx->depth, px * 4);
     alloc(ctx->hair_list, px * 4);
     alloc(ctx->hair_count, 16);
+    alloc(ctx->tile_depth, (size_t)((width + 7) / 8) * ((height + 7) / 8) * 4);
     if (e != cudaSuccess) {
         free_targets(ctx);
         return cuda_fail(ctx, e, "allocating screen targets");

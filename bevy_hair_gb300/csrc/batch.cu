@@ -33,6 +33,11 @@ struct hg_batch {
     float* filtered_depth = nullptr;
     float4* color = nullptr;
     float* depth = nullptr;
+    // Scratch of the per-groom (HG_BATCH_SEPARATE) frames, which run one after
+    // another on the context's stream: sized for the largest item.
+    uint32_t* tile_depth = nullptr;
+    uint32_t* hair_list = nullptr;
+    uint32_t* hair_count = nullptr;
     uint64_t total_px = 0, total_dom = 0;
     // tables: pinned host copies and their device twins
     hg::BatchView* h_views = nullptr;
@@ -112,6 +117,9 @@ void free_batch(hg_batch* b) {
     free_dev(b->filtered_depth);
     free_dev(b->color);
     free_dev(b->depth);
+    free_dev(b->tile_depth);
+    free_dev(b->hair_list);
+    free_dev(b->hair_count);
     free_dev(b->d_views);
     free_dev(b->d_tab);
     free_dev(b->d_lights);
@@ -306,6 +314,9 @@ hg_status run_separate(hg_batch* b, const hg_shade_desc* d) {
         view.filtered_depth = b->filtered_depth + po;
         view.color = b->color + po;
         view.depth = b->depth + po;
+        view.tile_depth = b->tile_depth;
+        view.hair_list = b->hair_list;
+        view.hair_count = b->hair_count;
         hg_frame_desc f;
         std::memset(&f, 0, sizeof(f));
         f.camera = &b->cam[i];
@@ -417,6 +428,14 @@ hg_status hg_batch_create(hg_ctx* ctx, const hg_batch_item* items, uint32_t coun
     alloc(b->filtered_depth, px * 4);
     alloc(b->color, px * 16);
     alloc(b->depth, px * 4);
+    size_t max_px = 0, max_tiles = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        max_px = std::max(max_px, (size_t)b->w[i] * b->h[i]);
+        max_tiles = std::max(max_tiles, (size_t)((b->w[i] + 7) / 8) * ((b->h[i] + 7) / 8));
+    }
+    alloc(b->tile_depth, max_tiles * 4);
+    alloc(b->hair_list, max_px * 4);
+    alloc(b->hair_count, 16);
     alloc(b->d_views, sizeof(hg::BatchView) * n_views);
     alloc(b->d_tab, sizeof(uint32_t) * to.total);
     alloc(b->d_lights, sizeof(hg_light) * HG_MAX_LIGHTS);

@@ -70,6 +70,10 @@ struct hg_ctx {
     float* depth = nullptr;
     uint32_t* hair_list = nullptr;  // pixels with hair (shade model 1), W*H
     uint32_t* hair_count = nullptr;
+    // Camera raster: per 8x8 pixel tile, the largest quantised depth held by
+    // any of its G-buffer words (an upper bound once built, since the words
+    // only decrease during the pass).
+    uint32_t* tile_depth = nullptr;
     uint32_t* err = nullptr;       // device error word
     hg_light* lights = nullptr;    // device copy, HG_MAX_LIGHTS
     // Pinned staging ring for the light list; slot k is reused only after

@@ -323,7 +323,13 @@ __global__ void scan_expand_sorted_kernel(const hg_lod_record* __restrict__ lod,
 
 constexpr int kRasterWarps = 4;
 constexpr int kRasterThreads = kRasterWarps * 32;
-constexpr int kRasterMinBlocks = 7;  // 28 warps per SM: registers <= 73, shared memory 7 x 26.8 KB
+// Resident blocks per SM.  The camera pass keeps its sample loop in 80
+// registers without a spill in it at 6 (24 warps); at 7 (72 registers) the
+// spilled values sit in the loop and reach L2 on every round (L1 is small
+// next to 7 x 28 KB of shared memory), which costs more than the extra warps
+// give.  The deep-opacity passes fit 71 registers and take 7.
+template <int MODE>
+constexpr int raster_min_blocks() { return MODE == 0 ? 6 : 7; }
 
 // Per-warp shared memory, 6.7 KB.  The layer samples are needed only while
 // control points are generated, so they share storage with the sample offsets.
@@ -336,9 +342,27 @@ struct alignas(16) StrandSmem {
             float4 lp[16];  // layer sample: position, ao
             float4 lt[16];  // layer tangent
         } gen;
-        int32_t off[132];  // camera: exclusive sample offset per segment
+        struct {
+            int32_t off[128];  // camera: first sample of each non-empty segment, in order
+            int32_t seg[128];  // camera: that segment's index | its DDA step count n << 8
+        } run;
     } u;
 };
+
+// Segments are cut into at most this many DDA steps.
+constexpr int kMaxSteps = 96;
+
+// t = i / n, correctly rounded, for integers 0 <= i <= n <= kMaxSteps, from
+// rcp = RN(1/n): q0 = RN(i * rcp), the exact remainder i - q0 * n by FMA, and
+// one correction step q0 + rem * rcp (Markstein's refinement).  An exhaustive
+// check over all (i, n) in that range against the exact quotient rounded to
+// nearest finds no difference, so this equals __fdiv_rn(i, n) there.
+__device__ __forceinline__ float step_t(int32_t i, int32_t n, float rcp) {
+    const float fi = __int2float_rn(i), fn = __int2float_rn(n);
+    const float q0 = __fmul_rn(fi, rcp);
+    const float rem = __fmaf_rn(-q0, fn, fi);
+    return __fmaf_rn(rem, rcp, q0);
+}
 
 struct RasterArgs {
     hg_hair_params p;
@@ -358,6 +382,12 @@ struct RasterArgs {
     const float* scene;
     uint32_t* err;
     uint32_t bundle_count;
+    // Camera pass: the refs (in draw order) this launch covers, in 1/256ths
+    // of the ref count, and the tile depths built from the refs before them
+    // (nullptr: no tile test).
+    uint32_t part_lo, part_hi;
+    const uint32_t* tile_depth;
+    uint32_t tiles_x;
 };
 
 // sample_style (raster.wgsl:34-60)
@@ -572,8 +602,83 @@ __device__ __forceinline__ float sqrt_bound(float r) {
     return x;
 }
 
+// High 32 bits of a G-buffer word, read through L2 (little endian: the second u32).
+__device__ __forceinline__ uint32_t hi_word(const unsigned long long* w) {
+    return __ldcg(reinterpret_cast<const unsigned int*>(w) + 1);
+}
+
 __device__ __forceinline__ bool on_screen(int32_t x, int32_t y, int32_t w, int32_t h) {
     return x >= 0 && y >= 0 && x < w && y < h;
+}
+
+// Pixels per side of a tile of the camera pass's tile-depth buffer.
+constexpr int kTileShift = 3;
+// Stage boundaries of the camera pass over the refs in draw order, in 1/256ths.
+constexpr uint32_t kCameraStages[] = {0, 64, 256};
+constexpr int kCameraStageCount = sizeof(kCameraStages) / sizeof(kCameraStages[0]);
+
+// True when no sample of segment (pa, pb) (world, in sm.cp) / (A, B) (screen)
+// can change a G-buffer word: every pixel it can reach is off screen, or
+// (given tile depths) lies in tiles whose words all hold a nearer depth than
+// the segment's nearest possible sample.  Conservative by construction:
+//  - pixels: a sample sits at floor(mix(A, B, t)), and mix stays within
+//    3 ulp of [min, max]; with |coordinates| < 2^20 that is < 0.2 px, so the
+//    box floor(min) - 1 .. floor(max) + 1 holds every sample and both
+//    diagonal side pixels (each a coordinate of a neighbouring sample);
+//  - depth: a sample's computed view distance differs from the exact linear
+//    one by < 21 u (M + C) (M, C: largest endpoint and camera coordinate,
+//    u = 2^-24), an endpoint's by < 12 u (M + C); the bound below subtracts
+//    1e-5 (M + C), about 5x their sum, and quantize_depth is monotone;
+//  - a word with depth D < the sample's depth d rejects the sample's
+//    payload (depth in the high bits) and its beta word (d << 8 | beta) alike.
+// Non-finite or very large coordinates are never rejected.
+__device__ __forceinline__ bool hidden_segment(const hg_hair_params& p, const uint32_t* tile_depth, uint32_t tiles_x,
+                                               int32_t width, int32_t height, float4 pa, float4 pb, float4 A, float4 B,
+                                               f3 cam, f3 fwd) {
+    const float lim = 1048576.0f;
+    if (!(fabsf(A.x) < lim && fabsf(A.y) < lim && fabsf(B.x) < lim && fabsf(B.y) < lim)) return false;
+    const int32_t x0 = max(f2i(floorf(fminf(A.x, B.x))) - 1, 0), x1 = min(f2i(floorf(fmaxf(A.x, B.x))) + 1, width - 1);
+    const int32_t y0 = max(f2i(floorf(fminf(A.y, B.y))) - 1, 0), y1 = min(f2i(floorf(fmaxf(A.y, B.y))) + 1, height - 1);
+    if (x0 > x1 || y0 > y1) return true;  // nothing on screen
+    if (!tile_depth) return false;
+    const int32_t tx0 = x0 >> kTileShift, tx1 = x1 >> kTileShift, ty0 = y0 >> kTileShift, ty1 = y1 >> kTileShift;
+    if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > 6) return false;
+    const float d0 = dot3(sub3(xyz(pa), cam), fwd), d1 = dot3(sub3(xyz(pb), cam), fwd);
+    const float m = fmaxf(fmaxf(fmaxf(fabsf(pa.x), fabsf(pa.y)), fmaxf(fabsf(pa.z), fabsf(pb.x))),
+                          fmaxf(fabsf(pb.y), fabsf(pb.z)));
+    const float c = fmaxf(fmaxf(fabsf(cam.x), fabsf(cam.y)), fabsf(cam.z));
+    if (!(fabsf(d0) < 1e30f && fabsf(d1) < 1e30f && m < 1e30f)) return false;
+    const uint32_t lower = quantize_depth(fminf(d0, d1) - 1e-5f * (m + c), p.screen[2], p.screen[3]);
+    uint32_t held = 0;
+    for (int32_t ty = ty0; ty <= ty1; ++ty)
+        for (int32_t tx = tx0; tx <= tx1; ++tx) held = max(held, __ldg(&tile_depth[(uint32_t)ty * tiles_x + tx]));
+    return lower > held;
+}
+
+// One warp per 8x8 tile: the largest quantised depth among the tile's
+// conservative, centre and beta words (empty words count as the far value
+// 0xffffff, which rejects nothing; pixels beyond the screen edge are never
+// written and count as 0).
+__global__ void __launch_bounds__(256) tile_depth_kernel(const unsigned long long* __restrict__ center,
+                                                         const unsigned long long* __restrict__ cons,
+                                                         const uint32_t* __restrict__ beta, uint32_t width,
+                                                         uint32_t height, uint32_t tiles_x, uint32_t tiles,
+                                                         uint32_t* __restrict__ tile_depth) {
+    const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (tile >= tiles) return;
+    const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
+    uint32_t held = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < 2; ++k) {
+        const uint32_t x = (tx << kTileShift) + (lane & 7u), y = (ty << kTileShift) + (lane >> 3) + 4u * k;
+        if (x < width && y < height) {
+            const size_t i = (size_t)y * width + x;
+            held = max(held, max(hi_word(&cons[i]) >> 8, hi_word(&center[i]) >> 8));
+            held = max(held, __ldcg(&beta[i]) >> 8);
+        }
+    }
+    held = __reduce_max_sync(0xffffffffu, held);
+    if (lane == 0) tile_depth[tile] = held;
 }
 
 // Camera raster of one generated strand.  The DDA of every segment
@@ -586,10 +691,17 @@ __device__ __forceinline__ bool on_screen(int32_t x, int32_t y, int32_t w, int32
 // diagonal step, the two side pixels.
 template <class Args>
 __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uint32_t ncp, float2 uv,
-                                              float beta, uint32_t lane) {
+                                              float beta, uint32_t lane, const uint32_t* tile_depth = nullptr,
+                                              uint32_t tiles_x = 0) {
     const hg_hair_params& p = a.p;
     const int32_t nseg = (int32_t)ncp - 1;
-    int32_t carry = 0;
+    const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
+    const f3 cam = mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2]);
+    const f3 fwd = mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]);
+    // Sample offsets: a segment with both ends behind the camera, or hidden
+    // behind the tile depths, has no samples, every other one n + 1 >= 2; the
+    // non-empty segments are listed in order with their first sample.
+    int32_t carry = 0, runs = 0;
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         int32_t j = (int32_t)lane + 32 * k;
@@ -601,10 +713,11 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
                 float4 A = sm.cs[j], B = sm.cs[j + 1];
                 float dx = B.x - A.x, dy = B.y - A.y;
                 int32_t steps = f2i(ceilf(fmaxf(fabsf(dx), fabsf(dy))));
-                n = min(max(steps, 1), 96);
+                n = min(max(steps, 1), kMaxSteps);
                 cnt = n + 1;
+                if (hidden_segment(p, tile_depth, tiles_x, width, height, pa, pb, A, B, cam, fwd)) cnt = 0;
             }
-            sm.cs[j].w = __int_as_float(n);
+            sm.cs[j].w = n > 0 ? __frcp_rn(__int2float_rn(n)) : 0.0f;
         }
         int32_t incl = cnt;
 #pragma unroll
@@ -612,34 +725,41 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
             int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
             if ((int32_t)lane >= o) incl += y;
         }
-        if (j < nseg) sm.u.off[j] = carry + incl - cnt;
+        const uint32_t live = __ballot_sync(0xffffffffu, cnt > 0);
+        if (cnt > 0) {
+            const int32_t r = runs + __popc(live & ((1u << lane) - 1u));
+            sm.u.run.off[r] = carry + incl - cnt;
+            sm.u.run.seg[r] = j | (cnt - 1) << 8;
+        }
         carry += __shfl_sync(0xffffffffu, incl, 31);
+        runs += __popc(live);
     }
-    if (lane == 0) sm.u.off[nseg] = carry;
     __syncwarp();
 
     const int32_t total = carry;
-    const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
     const float r2_max = sqrt_bound(fmaxf(p.appearance[3], 0.05f) * 0.5f);
-    const f3 cam = mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2]);
-    const f3 fwd = mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]);
     const uint32_t beta_q = f2u(clampf(beta, 0.0f, 1.0f) * 255.0f + 0.5f);
     const bool ao_on = p.flags[2] != 0u;
+    const uint32_t quv = quant63(uv.x) | quant63(uv.y) << 6u;
     int32_t carry_px = 0, carry_py = 0;
+    int32_t rw = 0;  // the run holding sample `base`
     for (int32_t base = 0; base < total; base += 32) {
         const int32_t s = min(base + (int32_t)lane, total - 1);
         const bool active = base + (int32_t)lane < total;
-        // segment j with off[j] <= s < off[j+1]
-        int32_t lo = 0, hi = nseg - 1;
-        while (lo < hi) {
-            int32_t mid = (lo + hi + 1) >> 1;
-            if (sm.u.off[mid] <= s) lo = mid; else hi = mid - 1;
-        }
-        const int32_t j = lo;
-        const int32_t i = s - sm.u.off[j];
+        // Runs starting inside this window of 32 samples: at most 16, since a
+        // run has two samples or more.  Lane k holds the start of run rw+1+k;
+        // bit q of `starts` marks a run starting at base + q.  Sample s lies in
+        // run rw + (starts in (base, s]), the run with the last start <= s.
+        const int32_t rk = rw + 1 + (int32_t)lane;
+        const int32_t ok = rk < runs ? sm.u.run.off[rk] : 0x7fffffff;
+        const int32_t rel = ok - base;
+        const uint32_t starts = __reduce_or_sync(0xffffffffu, rel > 0 && rel < 32 ? 1u << rel : 0u);
+        const int32_t r = rw + __popc(starts & (0xffffffffu >> (31u - lane)));
+        rw += __popc(__ballot_sync(0xffffffffu, ok <= base + 32));
+        const int32_t jn = sm.u.run.seg[r];
+        const int32_t j = jn & 0xff, i = s - sm.u.run.off[r];
         const float4 A = sm.cs[j], B = sm.cs[j + 1];
-        const int32_t n = __float_as_int(A.w);
-        const float t = __fdiv_rn(__int2float_rn(i), __int2float_rn(n));
+        const float t = step_t(i, jn >> 8, A.w);
         const float sx = mixf(A.x, B.x, t), sy = mixf(A.y, B.y, t);
         const int32_t px = f2i(floorf(sx)), py = f2i(floorf(sy));
         int32_t qx = __shfl_up_sync(0xffffffffu, px, 1), qy = __shfl_up_sync(0xffffffffu, py, 1);
@@ -658,13 +778,15 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
         const uint32_t pix0 = (uint32_t)py * (uint32_t)width + (uint32_t)px;
         const uint32_t pix1 = (uint32_t)py * (uint32_t)width + (uint32_t)qx;
         const uint32_t pix2 = (uint32_t)qy * (uint32_t)width + (uint32_t)px;
-        // Current words, read from L2 before the payload is known.  Buffers only
-        // decrease during the pass, so a stale read is an upper bound: an atomicMin
-        // is skipped only when it cannot change the word.
-        const unsigned long long cur_c0 = on0 ? __ldcg(&a.cons[pix0]) : 0ull;
-        const unsigned long long cur_m0 = on0 ? __ldcg(&a.center[pix0]) : 0ull;
-        const unsigned long long cur_c1 = on1 ? __ldcg(&a.cons[pix1]) : 0ull;
-        const unsigned long long cur_c2 = on2 ? __ldcg(&a.cons[pix2]) : 0ull;
+        // High words (depth, tangent x) of the current payloads, read from L2
+        // before the payload is known.  Buffers only decrease during the pass,
+        // so a stale read is an upper bound, and a payload whose high word is
+        // above it cannot lower the word: its atomicMin is skipped.  Equal high
+        // words go to the atomic, which decides.
+        const uint32_t cur_c0 = on0 ? hi_word(&a.cons[pix0]) : 0u;
+        const uint32_t cur_m0 = on0 ? hi_word(&a.center[pix0]) : 0u;
+        const uint32_t cur_c1 = on1 ? hi_word(&a.cons[pix1]) : 0u;
+        const uint32_t cur_c2 = on2 ? hi_word(&a.cons[pix2]) : 0u;
 
         // write_pixel (raster.wgsl:83-115): depth first; the rest of the payload
         // only when some word can still take it.
@@ -673,11 +795,11 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
         const float dist = dot3(sub3(world, cam), fwd);
         if (dist <= p.screen[2]) continue;
         const uint32_t depth = quantize_depth(dist, p.screen[2], p.screen[3]);
-        const unsigned long long lower = (unsigned long long)depth << 40;  // smallest payload with this depth
-        bool w0 = on0 && lower < cur_c0;
-        bool wm = on0 && depth <= (uint32_t)(cur_m0 >> 40);
-        bool w1 = on1 && lower < cur_c1;
-        bool w2 = on2 && lower < cur_c2;
+        const uint32_t lower = depth << 8u;  // high word of the smallest payload with this depth
+        bool w0 = on0 && lower <= cur_c0;
+        bool wm = on0 && depth <= cur_m0 >> 8u;
+        bool w1 = on1 && lower <= cur_c1;
+        bool w2 = on2 && lower <= cur_c2;
         if (wm) {
             // centre-disk test (raster.wgsl:206-212); length(o) <= r is
             // sqrt_rn(|o|^2) <= r, i.e. |o|^2 <= r2_max
@@ -706,15 +828,17 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
         const f3 tangent = safe_normalize(mix3(xyz(t0), xyz(t1), t));
         const uint32_t oct = oct_encode(tangent);
         const uint32_t ao_q = ao_on ? f2u(clampf(mixf(A.z, B.z, t), 0.0f, 1.0f) * 63.0f + 0.5f) : 63u;
-        const unsigned long long payload = pack_gb(depth, oct & 0xffu, oct >> 8u, quant63(mixf(uv.x, uv.x, t)),
-                                                   quant63(mixf(uv.y, uv.y, t)), quant63(mixf(t0.w, t1.w, t)), ao_q);
-        if (w0 && payload < cur_c0) atomicMin(&a.cons[pix0], payload);
+        // mix(uv, uv, t) is uv, so its quantised value is the strand's own
+        const unsigned long long payload = pack_gb(depth, oct & 0xffu, oct >> 8u, quv & 0x3fu, quv >> 6u,
+                                                   quant63(mixf(t0.w, t1.w, t)), ao_q);
+        const uint32_t high = (uint32_t)(payload >> 32u);
+        if (w0 && high <= cur_c0) atomicMin(&a.cons[pix0], payload);
         if (wm) {
-            if (payload < cur_m0) atomicMin(&a.center[pix0], payload);
+            if (high <= cur_m0) atomicMin(&a.center[pix0], payload);
             atomicMin(&a.beta[pix0], (depth << 8u) | beta_q);
         }
-        if (w1 && payload < cur_c1) atomicMin(&a.cons[pix1], payload);
-        if (w2 && payload < cur_c2) atomicMin(&a.cons[pix2], payload);
+        if (w1 && high <= cur_c1) atomicMin(&a.cons[pix1], payload);
+        if (w2 && high <= cur_c2) atomicMin(&a.cons[pix2], payload);
     }
 }
 
@@ -843,14 +967,15 @@ __global__ void __launch_bounds__(kRasterThreads) generate_kernel(const GenArgs 
 
 // raster.wgsl:225-337: one warp per strand ref, persistent over the refs.
 template <int MODE>
-__global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) raster_kernel(const RasterArgs a) {
+__global__ void __launch_bounds__(kRasterThreads, raster_min_blocks<MODE>()) raster_kernel(const RasterArgs a) {
     __shared__ StrandSmem smem[kRasterWarps];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     StrandSmem& sm = smem[warp];
-    const uint32_t total = a.indirect[0];
+    const unsigned long long total = a.indirect[0];
+    const uint32_t r0 = (uint32_t)((total * a.part_lo) >> 8), r1 = (uint32_t)((total * a.part_hi) >> 8);
     const uint32_t* order = a.draw_order && a.order_meta[1] ? a.draw_order : nullptr;
     const uint32_t nwarps = gridDim.x * kRasterWarps;
-    for (uint32_t r = blockIdx.x * kRasterWarps + warp; r < total; r += nwarps) {
+    for (uint32_t r = r0 + blockIdx.x * kRasterWarps + warp; r < r1; r += nwarps) {
         const hg_strand_ref ref = a.refs[order ? order[r] : r];
         if (ref.bundle >= a.bundle_count) {
             if (lane == 0) atomicOr(a.err, kErrBadRef);
@@ -861,7 +986,7 @@ __global__ void __launch_bounds__(kRasterThreads, kRasterMinBlocks) raster_kerne
         const uint32_t ncp = generate_strand<MODE>(a, sm, ref, bundle, uv, lane);
         if (MODE == 0) {
             float beta = __fdiv_rn(__uint2float_rn(ref.n_lod), __uint2float_rn(max(bundle.strand_count, 1u)));
-            raster_camera(a, sm, ncp, uv, beta, lane);
+            raster_camera(a, sm, ncp, uv, beta, lane, a.tile_depth, a.tiles_x);
         } else {
             raster_dom<MODE>(a, sm, ncp, lane);
         }
@@ -1131,12 +1256,38 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
     a.scene = scene;
     a.err = ctx->err;
     a.bundle_count = g->bundle_count;
+    a.part_lo = 0;
+    a.part_hi = 256;
+    a.tile_depth = nullptr;
+    a.tiles_x = 0;
     uint32_t mode = p.pass_mode[0];
     // One warp per ref slot, no persistence: raster launches on different
     // streams then share the SMs through the block scheduler.
     int blocks = (int)std::max<size_t>((g->ref_capacity + kRasterWarps - 1) / kRasterWarps, 1);
     if (mode == 0) {
-        raster_kernel<0><<<blocks, kRasterThreads, 0, ctx->stream>>>(a);
+        // Refs in draw order (near bundles first), in stages; before each
+        // stage after the first, the tile depths are rebuilt from the words
+        // the earlier stages left, and segments behind them are skipped.
+        const uint32_t tiles_x = (ctx->width + (1u << kTileShift) - 1) >> kTileShift;
+        const uint32_t tiles = tiles_x * ((ctx->height + (1u << kTileShift) - 1) >> kTileShift);
+        for (int k = 0; k + 1 < kCameraStageCount; ++k) {
+            a.part_lo = kCameraStages[k];
+            a.part_hi = kCameraStages[k + 1];
+            if (k > 0 && tiles && ctx->tile_depth) {
+                tile_depth_kernel<<<(tiles + 7) / 8, 256, 0, ctx->stream>>>(ctx->center, ctx->cons, ctx->beta,
+                                                                           ctx->width, ctx->height, tiles_x, tiles,
+                                                                           ctx->tile_depth);
+                cudaError_t e = cudaGetLastError();
+                if (e != cudaSuccess) return e;
+                a.tile_depth = ctx->tile_depth;
+                a.tiles_x = tiles_x;
+            }
+            const size_t part = (g->ref_capacity * (a.part_hi - a.part_lo) + 255) / 256 + 1;
+            const int stage_blocks = (int)std::max<size_t>((part + kRasterWarps - 1) / kRasterWarps, 1);
+            raster_kernel<0><<<stage_blocks, kRasterThreads, 0, ctx->stream>>>(a);
+            cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+        }
     } else if (mode == 1) {
         raster_kernel<1><<<blocks, kRasterThreads, 0, ctx->stream>>>(a);
     } else {

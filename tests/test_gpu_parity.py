@@ -164,6 +164,50 @@ def test_strand_cache_gives_the_same_visibility(renderer, name):
     g.close()
 
 
+def test_dense_groom_with_tile_depth_rejection(renderer):
+    """A dense groom at low resolution (deep overdraw): the camera pass's later
+    stages skip most segments behind the tile depths, and the buffers must not
+    change."""
+    sc = configs.config2(scale=0.25)
+    sc.view = configs._camera(384, 216, 900.0)
+    cam, dom = sc.params()
+    got = _visibility(renderer, sc, cam, None)
+    want = _oracle_visibility(sc, cam, None)
+    _check_visibility(got, want, with_dom=False)
+    covered = int((want["center"] != EMPTY).sum())
+    assert covered > 5000 and want["counts"]["samples"] > 50 * covered
+
+
+def test_two_grooms_into_one_g_buffer(renderer):
+    """A second groom rastered over the first without a clear: the tile depths
+    of its later stages start from the first groom's words."""
+    a = configs.config2(scale=0.05)
+    b = configs.config3(scale=0.02)
+    a.view = configs._camera(480, 270, 900.0)
+    cam_a, _ = a.params()
+    b.view = a.view
+    cam_b, _ = b.params()
+    renderer.ensure_targets(480, 270, *a.dom_size)
+    ga, gb = renderer.upload(a.mesh), renderer.upload(b.mesh)
+    renderer.clear()
+    for g, cam in ((ga, cam_a), (gb, cam_b)):
+        renderer.lod(g, cam, abi.SLOT_CAMERA)
+        renderer.scan(g, cam, abi.SLOT_CAMERA)
+        renderer.raster(g, cam, abi.SLOT_CAMERA)
+    assert renderer.synchronize() == 0
+    center, cons, beta = oracle.clear_targets(480, 270)
+    for sc, cam in ((a, cam_a), (b, cam_b)):
+        lod = oracle.lod(cam, sc.mesh)
+        refs, total = oracle.scan(cam, lod, max(sc.mesh.strand_count(), 1))
+        oracle.raster(cam, sc.mesh, refs, total, center, cons, beta, None)
+    _assert_equal("center", renderer.read(abi.BUF_CENTER), center)
+    _assert_equal("conservative", renderer.read(abi.BUF_CONSERVATIVE), cons)
+    _assert_equal("beta", renderer.read(abi.BUF_BETA), beta)
+    assert (center != EMPTY).sum() > 1000
+    ga.close()
+    gb.close()
+
+
 @pytest.mark.parametrize("diameter", [0.01, 0.3, 0.7, 1.0, 1.41421356, 2.5])
 def test_center_disk_diameters(renderer, diameter):
     """The centre-sample acceptance disk (raster.wgsl:201,212) at several
