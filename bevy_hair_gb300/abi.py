@@ -117,6 +117,38 @@ class EnvDesc(C.Structure):
     ]
 
 
+class ViewDesc(C.Structure):
+    _fields_ = [
+        ("world_from_view", C.c_float * 16),
+        ("clip_from_view", C.c_float * 16),
+        ("clip_from_world", C.c_float * 16),
+        ("has_clip_from_world", C.c_uint32),
+        ("width", C.c_uint32),
+        ("height", C.c_uint32),
+    ]
+
+
+class GroomDesc(C.Structure):
+    _fields_ = [
+        ("world_from_model", C.c_float * 16),
+        ("bounds_min", C.c_float * 3),
+        ("bounds_max", C.c_float * 3),
+        ("bundle_count", C.c_uint32),
+        ("roughness", C.c_float),
+        ("tilt", C.c_float),
+        ("lambda_", C.c_float),
+        ("center_diameter", C.c_float),
+        ("albedo", C.c_float * 4),
+        ("lod", C.c_uint32),
+        ("filter", C.c_uint32),
+        ("ambient_occlusion", C.c_uint32),
+        ("deep_opacity", C.c_uint32),
+    ]
+
+
+DIRECTIONAL = np.dtype([("direction_to_light", "<f4", 3), ("casts_shadows", "<u4")])
+
+
 class BatchItem(C.Structure):
     _fields_ = [
         ("groom", C.c_void_p),
@@ -179,6 +211,9 @@ _SIGNATURES = {
     "hg_groom_frame": (_I32, [_VP, _VP, C.POINTER(FrameDesc)]),
     "hg_scan_noalloc": (_I32, [_VP, _U32, _U32, _VP, _VP, _VP]),
     "hg_shadow_light_from": (_I32, [_VP, _VP]),
+    "hg_groom_params": (_I32, [_VP, _VP, _VP, _U32, _U32, _U32, _VP, _VP]),
+    "hg_copy_out_async": (_I32, [_VP, _I32, _VP, _SZ]),
+    "hg_copy_wait": (_I32, [_VP]),
     "hg_hair_visibility": (_I32, [_VP, _VP, _VP, _U32, _VP]),
     "hg_mlp_create": (_I32, [_VP, C.POINTER(_VP)]),
     "hg_mlp_destroy": (None, [_VP]),

@@ -36,6 +36,10 @@ EXACT_UNITS = {"raster.cu", "filter.cu"}
 # intrinsics, which -use_fast_math does not change.
 FAST_UNITS = {"shade.cu"}
 CUDA_UNITS = ["api.cu", "raster.cu", "shade.cu", "filter.cu", "receiver.cu", "surrogate.cu", "batch.cu"]
+# Host-only C++ linked into libhairgb.so.  -ffp-contract=off keeps f32 results
+# the same on x86-64 and AArch64 (GCC would otherwise fuse into FMAs on Arm).
+HOST_UNITS = ["host_params.cpp"]
+HOST_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
 
 
 def nvcc() -> str:
@@ -82,6 +86,13 @@ def build_cuda(verbose_ptxas: bool = False, force: bool = False) -> Path:
         if verbose_ptxas:
             flags.append("-Xptxas=-v")
         jobs.append([nv, *flags, "-c", str(src), "-o", str(obj)])
+    cxx = os.environ.get("CXX", "g++")
+    for unit in HOST_UNITS:
+        src = CSRC / unit
+        obj = BUILD_DIR / (unit + ".o")
+        objs.append(obj)
+        if force or _stale(obj, [src, ROOT / "include" / "hairgb.h"]):
+            jobs.append([cxx, *HOST_FLAGS, f"-I{ROOT / 'include'}", "-c", str(src), "-o", str(obj)])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=len(jobs)) as ex:
             list(ex.map(_run, jobs))

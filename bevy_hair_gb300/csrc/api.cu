@@ -40,6 +40,18 @@ void free_dev(T*& p) {
     p = nullptr;
 }
 
+constexpr uint32_t kGbufferBits = 1u << HG_BUF_CENTER | 1u << HG_BUF_CONSERVATIVE | 1u << HG_BUF_BETA;
+constexpr uint32_t kColorBits = 1u << HG_BUF_COLOR | 1u << HG_BUF_DEPTH;
+
+// Order work about to write `bits` (enqueued next on the context's current
+// stream) after every asynchronous readback of those buffers.
+cudaError_t guard_writes(hg_ctx* ctx, uint32_t bits) {
+    if (!(ctx->pending_reads & bits)) return cudaSuccess;
+    cudaError_t e = cudaStreamWaitEvent(ctx->stream, ctx->ev_copy_done, 0);
+    if (e == cudaSuccess) ctx->pending_reads &= ~bits;
+    return e;
+}
+
 void free_targets(hg_ctx* ctx) {
     free_dev(ctx->center);
     free_dev(ctx->cons);
@@ -144,7 +156,8 @@ hg_status hg_create(int device, void* stream, hg_ctx** out) {
         }
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
-    for (cudaEvent_t* ev : {&ctx->ev_fork, &ctx->ev_gen, &ctx->ev_join})
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+    for (cudaEvent_t* ev : {&ctx->ev_fork, &ctx->ev_gen, &ctx->ev_join, &ctx->ev_copy_src, &ctx->ev_copy_done})
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->err, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->err, 0, sizeof(uint32_t), ctx->stream);
@@ -164,6 +177,7 @@ hg_status hg_destroy(hg_ctx* ctx) {
     if (!ctx) return HG_INVALID_ARG;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
     free_targets(ctx);
     free_dev(ctx->env_spec);
     free_dev(ctx->env_diff);
@@ -176,7 +190,11 @@ hg_status hg_destroy(hg_ctx* ctx) {
         cudaStreamSynchronize(ctx->side);
         cudaStreamDestroy(ctx->side);
     }
-    for (cudaEvent_t ev : {ctx->ev_fork, ctx->ev_gen, ctx->ev_join})
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+    }
+    for (cudaEvent_t ev : {ctx->ev_fork, ctx->ev_gen, ctx->ev_join, ctx->ev_copy_src, ctx->ev_copy_done})
         if (ev) cudaEventDestroy(ev);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -259,6 +277,8 @@ hg_status hg_ensure_targets(hg_ctx* ctx, uint32_t width, uint32_t height, uint32
         return HG_OK;
     cudaSetDevice(ctx->device);
     HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    HG_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+    ctx->pending_reads = 0;
     free_targets(ctx);
     size_t px = (size_t)width * height;
     size_t texels = (size_t)dom_w * dom_h;
@@ -309,11 +329,31 @@ hg_status hg_copy_out(hg_ctx* ctx, hg_buffer_id id, void* host, size_t bytes) {
     return HG_OK;
 }
 
+hg_status hg_copy_out_async(hg_ctx* ctx, hg_buffer_id id, void* host, size_t bytes) {
+    if (!ctx || !host) return HG_INVALID_ARG;
+    if ((unsigned)id > (unsigned)HG_BUF_DEPTH) return fail(ctx, HG_INVALID_ARG, "unknown buffer id");
+    BufInfo b = buffer_info(ctx, id);
+    if (!b.ptr || bytes != b.bytes) return fail(ctx, HG_INVALID_ARG, "size differs from the buffer size");
+    HG_CUDA(ctx, cudaEventRecord(ctx->ev_copy_src, ctx->stream));
+    HG_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_copy_src, 0));
+    HG_CUDA(ctx, cudaMemcpyAsync(host, b.ptr, bytes, cudaMemcpyDeviceToHost, ctx->copy_stream));
+    HG_CUDA(ctx, cudaEventRecord(ctx->ev_copy_done, ctx->copy_stream));
+    ctx->pending_reads |= 1u << (unsigned)id;
+    return HG_OK;
+}
+
+hg_status hg_copy_wait(hg_ctx* ctx) {
+    if (!ctx) return HG_INVALID_ARG;
+    HG_CUDA(ctx, cudaStreamSynchronize(ctx->copy_stream));
+    return HG_OK;
+}
+
 hg_status hg_copy_in(hg_ctx* ctx, hg_buffer_id id, const void* host, size_t bytes) {
     if (!ctx || !host) return HG_INVALID_ARG;
     if ((unsigned)id > (unsigned)HG_BUF_DEPTH) return fail(ctx, HG_INVALID_ARG, "unknown buffer id");
     BufInfo b = buffer_info(ctx, id);
     if (!b.ptr || bytes != b.bytes) return fail(ctx, HG_INVALID_ARG, "size differs from the buffer size");
+    HG_CUDA(ctx, guard_writes(ctx, 1u << (unsigned)id));
     HG_CUDA(ctx, cudaMemcpyAsync(b.ptr, host, bytes, cudaMemcpyHostToDevice, ctx->stream));
     HG_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return HG_OK;
@@ -453,6 +493,7 @@ hg_status hg_clear(hg_ctx* ctx) {
     if (!ctx) return HG_INVALID_ARG;
     hg_status s = check_targets(ctx, false);
     if (s != HG_OK) return s;
+    HG_CUDA(ctx, guard_writes(ctx, kGbufferBits));
     HG_CUDA(ctx, hg::launch_clear(ctx));
     return HG_OK;
 }
@@ -461,6 +502,7 @@ hg_status hg_clear_dom(hg_ctx* ctx) {
     if (!ctx) return HG_INVALID_ARG;
     hg_status s = check_targets(ctx, true);
     if (s != HG_OK) return s;
+    HG_CUDA(ctx, guard_writes(ctx, 1u << HG_BUF_DOM));
     HG_CUDA(ctx, hg::launch_clear_dom(ctx));
     return HG_OK;
 }
@@ -495,6 +537,7 @@ hg_status hg_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params* p, hg_view_s
     if (!ctx || !g || !p || (slot != HG_SLOT_CAMERA && slot != HG_SLOT_DOM)) return HG_INVALID_ARG;
     hg_status s = check_screen(ctx, p);
     if (s != HG_OK) return s;
+    HG_CUDA(ctx, guard_writes(ctx, p->pass_mode[0] == 0u ? kGbufferBits : 1u << HG_BUF_DOM));
     HG_CUDA(ctx, hg::launch_raster(ctx, g, *p, slot, p->pass_mode[0] == 0u ? scene_depth : nullptr));
     return HG_OK;
 }
@@ -527,6 +570,7 @@ hg_status hg_shade(hg_ctx* ctx, const hg_hair_params* p, const hg_shade_desc* d)
         HG_CUDA(ctx, cudaMemcpyAsync(ctx->lights, staging, n * sizeof(hg_light), cudaMemcpyHostToDevice, ctx->stream));
         HG_CUDA(ctx, cudaEventRecord(ctx->light_events[slot], ctx->stream));
     }
+    HG_CUDA(ctx, guard_writes(ctx, 1u << HG_BUF_SHADED | 1u << HG_BUF_SHADED_DEPTH));
     HG_CUDA(ctx, hg::launch_shade(ctx, *p, n, d->ortho, d->exposure, d->shade_model));
     return HG_OK;
 }
@@ -535,6 +579,7 @@ hg_status hg_filter(hg_ctx* ctx, const hg_hair_params* p) {
     if (!ctx || !p) return HG_INVALID_ARG;
     hg_status s = check_screen(ctx, p);
     if (s != HG_OK) return s;
+    HG_CUDA(ctx, guard_writes(ctx, 1u << HG_BUF_FILTERED | 1u << HG_BUF_FILTERED_DEPTH));
     HG_CUDA(ctx, hg::launch_filter(ctx, *p));
     return HG_OK;
 }
@@ -543,6 +588,7 @@ hg_status hg_composite(hg_ctx* ctx, const hg_hair_params* p, uint32_t source_fil
     if (!ctx || !p) return HG_INVALID_ARG;
     hg_status s = check_screen(ctx, p);
     if (s != HG_OK) return s;
+    HG_CUDA(ctx, guard_writes(ctx, kColorBits));
     HG_CUDA(ctx, hg::launch_composite(ctx, *p, source_filtered));
     return HG_OK;
 }
@@ -551,6 +597,7 @@ hg_status hg_clear_color(hg_ctx* ctx, float depth_clear) {
     if (!ctx) return HG_INVALID_ARG;
     hg_status s = check_targets(ctx, false);
     if (s != HG_OK) return s;
+    HG_CUDA(ctx, guard_writes(ctx, kColorBits));
     HG_CUDA(ctx, hg::launch_clear_color(ctx, depth_clear));
     return HG_OK;
 }

@@ -317,6 +317,7 @@ hg_status run_separate(hg_batch* b, const hg_shade_desc* d) {
         view.tile_depth = b->tile_depth;
         view.hair_list = b->hair_list;
         view.hair_count = b->hair_count;
+        view.pending_reads = 0;  // the batch's arenas are never read back asynchronously
         hg_frame_desc f;
         std::memset(&f, 0, sizeof(f));
         f.camera = &b->cam[i];

@@ -74,6 +74,13 @@ struct hg_ctx {
     // any of its G-buffer words (an upper bound once built, since the words
     // only decrease during the pass).
     uint32_t* tile_depth = nullptr;
+    // Asynchronous readback (hg_copy_out_async): copies run on copy_stream
+    // behind ev_copy_src; ev_copy_done follows the last one.  pending_reads
+    // has bit (1 << hg_buffer_id) set for buffers whose copy a later writer
+    // has not yet been ordered after.
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t ev_copy_src = nullptr, ev_copy_done = nullptr;
+    uint32_t pending_reads = 0;
     uint32_t* err = nullptr;       // device error word
     hg_light* lights = nullptr;    // device copy, HG_MAX_LIGHTS
     // Pinned staging ring for the light list; slot k is reused only after

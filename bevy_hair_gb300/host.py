@@ -10,6 +10,7 @@ Mirrors the parts of ``src/render/pass.rs`` that run on the CPU each frame:
 """
 from __future__ import annotations
 
+import ctypes as C
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -230,8 +231,45 @@ class View:
 def groom_params(view: View, groom: HairGroom, bounds_min, bounds_max, bundle_count: int,
                  directionals: list[Directional], dom_size: tuple[int, int]) -> tuple[np.ndarray, np.ndarray]:
     """Camera (pass_mode 0) and DOM depth (pass_mode 1) params of one groom;
-    src/render/pass.rs:342-453.  The DOM layers params are the DOM params with
+    src/render/pass.rs:342-453, computed by the library's native host code
+    (``hg_groom_params``).  The DOM layers params are the DOM params with
     pass_mode.x = 2."""
+    from . import abi
+
+    v = abi.ViewDesc()
+    C.memmove(v.world_from_view, cols(view.world_from_view).ctypes.data, 64)
+    C.memmove(v.clip_from_view, cols(view.clip_from_view).ctypes.data, 64)
+    v.width, v.height = int(view.width), int(view.height)
+    g = abi.GroomDesc()
+    C.memmove(g.world_from_model, cols(groom.world_from_model).ctypes.data, 64)
+    for i in range(3):
+        g.bounds_min[i] = float(bounds_min[i])
+        g.bounds_max[i] = float(bounds_max[i])
+    g.bundle_count = int(bundle_count)
+    g.roughness, g.tilt, g.lambda_, g.center_diameter = (float(groom.roughness), float(groom.tilt),
+                                                         float(groom.lam), float(groom.center_diameter))
+    for i, a in enumerate((*groom.albedo, 1.0)):
+        g.albedo[i] = float(a)
+    g.lod, g.filter = int(groom.lod), int(groom.filter)
+    g.ambient_occlusion, g.deep_opacity = int(groom.ambient_occlusion), int(groom.deep_opacity)
+    lights = np.zeros(len(directionals), dtype=abi.DIRECTIONAL)
+    for i, d in enumerate(directionals):
+        lights[i]["direction_to_light"] = np.asarray(d.direction_to_light, dtype=F)
+        lights[i]["casts_shadows"] = int(d.casts_shadows)
+    camera = np.zeros((), dtype=HAIR_PARAMS)
+    dom = np.zeros((), dtype=HAIR_PARAMS)
+    st = abi.load().hg_groom_params(C.byref(v), C.byref(g), lights.ctypes.data if len(lights) else None,
+                                    len(lights), int(dom_size[0]), int(dom_size[1]), camera.ctypes.data,
+                                    dom.ctypes.data)
+    if st != 0:
+        raise ValueError(f"hg_groom_params rejected the view or groom (status {st})")
+    return camera, dom
+
+
+def groom_params_numpy(view: View, groom: HairGroom, bounds_min, bounds_max, bundle_count: int,
+                       directionals: list[Directional], dom_size: tuple[int, int]) -> tuple[np.ndarray, np.ndarray]:
+    """The same parameters restated with NumPy (a cross-check of the native
+    host code; slower by two orders of magnitude)."""
     wfv = view.world_from_view.astype(F)
     camera_pos = transform_point(wfv, (0, 0, 0))
     forward = normalize_or(-transform_vector(wfv, (0, 0, 1)), (0, 0, -1))

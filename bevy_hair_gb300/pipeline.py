@@ -224,6 +224,15 @@ class HairRenderer:
         _check(self.lib, self.ctx, self.lib.hg_copy_out(self.ctx, which, abi.ptr(out), out.nbytes))
         return out
 
+    def read_async(self, which: int, host_ptr: int, nbytes: int) -> None:
+        """hg_copy_out_async: enqueue a copy of buffer `which` into host memory at
+        `host_ptr` (page-locked for overlap) and return; the data is final after
+        copy_wait()."""
+        _check(self.lib, self.ctx, self.lib.hg_copy_out_async(self.ctx, which, host_ptr, nbytes))
+
+    def copy_wait(self) -> None:
+        _check(self.lib, self.ctx, self.lib.hg_copy_wait(self.ctx))
+
     def write(self, which: int, host: np.ndarray) -> None:
         host = np.ascontiguousarray(host)
         _check(self.lib, self.ctx, self.lib.hg_copy_in(self.ctx, which, abi.ptr(host), host.nbytes))

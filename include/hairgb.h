@@ -213,6 +213,15 @@ hg_status hg_ensure_targets(hg_ctx* ctx, uint32_t width, uint32_t height,
 hg_status hg_buffer(hg_ctx* ctx, hg_buffer_id id, void** device_ptr, size_t* bytes);
 /* Copies a context buffer to host memory (bytes must equal its size). */
 hg_status hg_copy_out(hg_ctx* ctx, hg_buffer_id id, void* host, size_t bytes);
+/* Enqueues the same copy on the context's copy stream, behind the work
+ * enqueued so far, and returns at once.  host should be page-locked for the
+ * copy to overlap later work; it must stay valid, and its contents are not
+ * final, until hg_copy_wait returns.  Later passes that write the buffer wait
+ * for the copy on the device, so the next frame can be enqueued right away.
+ * (No reference counterpart: the reference never reads its targets back.) */
+hg_status hg_copy_out_async(hg_ctx* ctx, hg_buffer_id id, void* host, size_t bytes);
+/* Blocks until every hg_copy_out_async of the context has landed. */
+hg_status hg_copy_wait(hg_ctx* ctx);
 /* Copies host memory into a context buffer (used to feed a pass its inputs). */
 hg_status hg_copy_in(hg_ctx* ctx, hg_buffer_id id, const void* host, size_t bytes);
 
@@ -289,6 +298,48 @@ typedef struct hg_shadow_light {
 /* The ShadowLight the reference publishes after the DOM passes
  * (src/render/pass.rs:574-579), from the DOM params (pass_mode.x == 1). */
 hg_status hg_shadow_light_from(const hg_hair_params* dom_params, hg_shadow_light* out);
+
+/* ---- Host-side per-view uniforms (no device work, no context) ----------- */
+
+/* The camera of one view (ExtractedView: world_from_view, clip_from_view and
+ * the optional clip_from_world override, src/render/pass.rs:342-348) and its
+ * target size.  Matrices are column-major (glam to_cols_array). */
+typedef struct hg_view_desc {
+    float world_from_view[16];
+    float clip_from_view[16];
+    float clip_from_world[16]; /* used when has_clip_from_world != 0 */
+    uint32_t has_clip_from_world;
+    uint32_t width, height;
+} hg_view_desc;
+
+/* One groom's settings (HairGroom, src/lib.rs:32-63; albedo linear RGB + 1)
+ * and its GPU asset's bounds and bundle count (GpuGroom). */
+typedef struct hg_groom_desc {
+    float world_from_model[16];
+    float bounds_min[3];
+    float bounds_max[3];
+    uint32_t bundle_count;
+    float roughness, tilt, lambda, center_diameter;
+    float albedo[4];
+    uint32_t lod, filter, ambient_occlusion, deep_opacity;
+} hg_groom_desc;
+
+/* A directional light as extract_hair records it (src/render/mod.rs:104-107). */
+typedef struct hg_directional {
+    float direction_to_light[3];
+    uint32_t casts_shadows;
+} hg_directional;
+
+/* The camera (pass_mode.x = 0) and DOM depth (pass_mode.x = 1) HairParams of
+ * one groom, as hair_pass builds them each frame (src/render/pass.rs:342-453:
+ * camera position and forward, clip_from_world and its inverse, reverse-Z
+ * detection :778-787, key_direction :711-719, world_extent :721-745,
+ * light_fit :747-776, make_params :676-709).  The DOM layers params are the
+ * DOM params with pass_mode.x = 2.  The DOM size is a parameter (the
+ * reference fixes 512).  Pure host arithmetic in f32 (inverses in f64). */
+hg_status hg_groom_params(const hg_view_desc* view, const hg_groom_desc* groom, const hg_directional* lights,
+                          uint32_t light_count, uint32_t dom_w, uint32_t dom_h, hg_hair_params* camera,
+                          hg_hair_params* dom);
 
 /* hair_visibility (src/render/shaders/hair_shadow.wesl:30-75) for n world
  * points against the context's deep opacity map: the fraction of the key

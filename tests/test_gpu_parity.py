@@ -457,3 +457,34 @@ def test_hair_visibility_for_receivers(renderer):
     np.testing.assert_allclose(got, want, rtol=1e-5, atol=1e-6)
     assert (want < 0.99).sum() > 100 and (want == 1.0).sum() > 100  # shadowed and unshadowed points
     g.close()
+
+
+def test_async_readback_lands_before_the_next_frame_writes(renderer):
+    """hg_copy_out_async: a frame's colour and depth copied on the copy stream
+    while the next frame (another camera) is already enqueued; the next
+    frame's writes wait for the copies on the device."""
+    torch = pytest.importorskip("torch")
+    sc = configs.config2(scale=0.02)
+    cam_a, dom_a = sc.params()
+    lights = sc.light_array()
+    renderer.ensure_targets(sc.view.width, sc.view.height, *sc.dom_size)
+    g = renderer.upload(sc.mesh)
+    renderer.render_groom(g, cam_a, dom_a, lights)
+    want_color, want_depth = renderer.read(abi.BUF_COLOR).copy(), renderer.read(abi.BUF_DEPTH).copy()
+    sc.view = configs._camera(sc.view.width, sc.view.height, 700.0, azimuth=1.1)
+    cam_b, dom_b = sc.params()
+    color = torch.empty(want_color.size, dtype=torch.float32, pin_memory=True)
+    depth = torch.empty(want_depth.size, dtype=torch.float32, pin_memory=True)
+    renderer.render_groom(g, cam_a, dom_a, lights)
+    renderer.read_async(abi.BUF_COLOR, color.data_ptr(), color.numel() * 4)
+    renderer.read_async(abi.BUF_DEPTH, depth.data_ptr(), depth.numel() * 4)
+    renderer.render_groom(g, cam_b, dom_b, lights)
+    renderer.copy_wait()
+    assert renderer.synchronize() == 0
+    np.testing.assert_array_equal(color.numpy(), want_color)
+    np.testing.assert_array_equal(depth.numpy(), want_depth)
+    other = renderer.read(abi.BUF_COLOR)
+    assert np.abs(other - want_color).max() > 1e-3  # frame B did overwrite the target
+    with pytest.raises(abi.HairGbError):
+        renderer.read_async(abi.BUF_COLOR, color.data_ptr(), 16)
+    g.close()

@@ -71,3 +71,55 @@ def test_shadow_light_published_from_the_dom_params():
     assert np.array_equal(light["light_eye"][:3], dom["light_eye"][:3])
     assert light["depth"].tolist() == pytest.approx([dom["dom_info"][2], dom["dom_info"][3], 0.05, 1.0])
     assert abi.load().hg_shadow_light_from(cam.ctypes.data, light.ctypes.data) == abi.HG_INVALID_ARG
+
+
+def _numpy_params(sc):
+    return host.groom_params_numpy(sc.view, sc.groom, sc.mesh.bounds_min, sc.mesh.bounds_max, sc.mesh.bundle_count,
+                                   sc.directionals, sc.dom_size)
+
+
+@pytest.mark.parametrize("name", ["config1", "config2", "config3", "forward_z", "rotated_groom", "no_lights"])
+def test_native_params_match_the_numpy_restatement(name):
+    """hg_groom_params (native, the product path) against the NumPy restatement
+    of the same host math: integer fields equal, float fields within 1e-6 of the
+    largest magnitude of their vector or matrix."""
+    if name == "config1":
+        sc = configs.config1(scale=0.01)
+    elif name == "config3":
+        sc = configs.config3(scale=0.01)
+    else:
+        sc = configs.config2(scale=0.01)
+    if name == "forward_z":
+        v = sc.view
+        sc.view = host.View(v.world_from_view, host.perspective_rh(math.pi / 3, v.width / v.height, 0.5, 3000.0),
+                            v.width, v.height)
+    if name == "rotated_groom":
+        c, s = math.cos(0.7), math.sin(0.7)
+        m = np.eye(4, dtype=np.float32)
+        m[:3, :3] = [[c, 0, s], [0, 1, 0], [-s, 0, c]]
+        m[:3, 3] = [12.0, -30.0, 5.0]
+        sc.groom.world_from_model = m
+    if name == "no_lights":
+        sc.directionals = []
+    got = sc.params()
+    want = _numpy_params(sc)
+    for g, w in zip(got, want):
+        for f in w.dtype.names:
+            a, b = np.asarray(g[f]), np.asarray(w[f])
+            if a.dtype.kind == "u":
+                assert np.array_equal(a, b), f
+            else:
+                tol = 1e-6 * max(float(np.abs(b).max()), 1e-30)
+                assert np.abs(a.astype(np.float64) - b).max() <= tol, (f, a, b)
+    if name == "forward_z":
+        assert got[0]["pass_mode"][2] == 0
+    if name == "no_lights":
+        d = np.array([0.35, 0.82, 0.45]) / np.linalg.norm([0.35, 0.82, 0.45])
+        assert np.allclose(-got[1]["camera_forward"][:3], d, atol=1e-6)
+
+
+def test_native_params_reject_an_empty_target():
+    sc = configs.config1(scale=0.01)
+    sc.view = host.View(sc.view.world_from_view, sc.view.clip_from_view, 0, sc.view.height)
+    with pytest.raises(ValueError):
+        sc.params()
