@@ -341,6 +341,7 @@ struct alignas(16) StrandSmem {
         struct {
             float4 lp[16];  // layer sample: position, ao
             float4 lt[16];  // layer tangent
+            float4 ls[16];  // style residual of each w layer at the strand's (u, v)
         } gen;
         struct {
             int32_t off[128];  // camera: first sample of each non-empty segment, in order
@@ -390,22 +391,39 @@ struct RasterArgs {
     uint32_t tiles_x;
 };
 
-// sample_style (raster.wgsl:34-60)
-__device__ __forceinline__ f3 sample_style(const float4* __restrict__ style, uint32_t offset, float2 uv, float w) {
-    float u = clampf(uv.x, 0.0f, 1.0f) * (float)(kStyleU - 1u);
-    float v = clampf(uv.y, 0.0f, 1.0f) * (float)(kStyleV - 1u);
+// sample_style (raster.wgsl:34-60), the trilinear style residual, is
+// mix3(B(w0), B(w1), tw) with B(l) = mix3(mix3(c(u0,v0,l), c(u1,v0,l), tu),
+// mix3(c(u0,v1,l), c(u1,v1,l), tu), tv), the bilinear lookup at the strand's
+// (u, v) in layer l.  (u, v) is the same for every control point of a strand,
+// so lanes 16..31 (idle while lanes 0..15 sample the layer cage) compute B
+// for one layer each, and style_at finishes each control point with the same
+// operations in the same order.
+__device__ __forceinline__ void style_layers(const float4* __restrict__ style, uint32_t offset, float2 uv,
+                                             float4* ls, uint32_t lane) {
+    static_assert(kStyleW == 16, "one style layer per lane of the upper half-warp");
+    if (lane >= 16u) {
+        const uint32_t layer = lane - 16u;
+        float u = clampf(uv.x, 0.0f, 1.0f) * (float)(kStyleU - 1u);
+        float v = clampf(uv.y, 0.0f, 1.0f) * (float)(kStyleV - 1u);
+        uint32_t u0 = f2u(floorf(u)), v0 = f2u(floorf(v));
+        uint32_t u1 = min(u0 + 1u, kStyleU - 1u), v1 = min(v0 + 1u, kStyleV - 1u);
+        float tu = u - __uint2float_rn(u0), tv = v - __uint2float_rn(v0);
+        auto at = [&](uint32_t iu, uint32_t iv) {
+            return xyz(__ldg(&style[offset + (layer * kStyleV + iv) * kStyleU + iu]));
+        };
+        const f3 c0 = mix3(at(u0, v0), at(u1, v0), tu);
+        const f3 c1 = mix3(at(u0, v1), at(u1, v1), tu);
+        const f3 r = mix3(c0, c1, tv);
+        ls[layer] = make_float4(r.x, r.y, r.z, 0.0f);
+    }
+}
+
+__device__ __forceinline__ f3 style_at(const float4* ls, float w) {
     float ww = clampf(w, 0.0f, 1.0f) * (float)(kStyleW - 1u);
-    uint32_t u0 = f2u(floorf(u)), v0 = f2u(floorf(v)), w0 = f2u(floorf(ww));
-    uint32_t u1 = min(u0 + 1u, kStyleU - 1u), v1 = min(v0 + 1u, kStyleV - 1u), w1 = min(w0 + 1u, kStyleW - 1u);
-    float tu = u - __uint2float_rn(u0), tv = v - __uint2float_rn(v0), tw = ww - __uint2float_rn(w0);
-    auto at = [&](uint32_t iu, uint32_t iv, uint32_t iw) {
-        return xyz(__ldg(&style[offset + (iw * kStyleV + iv) * kStyleU + iu]));
-    };
-    f3 c00 = mix3(at(u0, v0, w0), at(u1, v0, w0), tu);
-    f3 c01 = mix3(at(u0, v1, w0), at(u1, v1, w0), tu);
-    f3 c10 = mix3(at(u0, v0, w1), at(u1, v0, w1), tu);
-    f3 c11 = mix3(at(u0, v1, w1), at(u1, v1, w1), tu);
-    return mix3(mix3(c00, c01, tv), mix3(c10, c11, tv), tw);
+    uint32_t w0 = f2u(floorf(ww));
+    uint32_t w1 = min(w0 + 1u, kStyleW - 1u);
+    float tw = ww - __uint2float_rn(w0);
+    return mix3(xyz(ls[w0]), xyz(ls[w1]), tw);
 }
 
 __device__ __forceinline__ f3 hermite(f3 p0, f3 p1, f3 m0, f3 m1, float t) {
@@ -460,7 +478,7 @@ constexpr uint32_t kCacheCps = 65;
 // tangents into lp/lt, then eval_cp for control point j on lane j % 32, slot
 // j / 32.
 __device__ __forceinline__ void model_cps(const float4* __restrict__ layers, const float4* __restrict__ style,
-                                          float4* lp, float4* lt, const hg_gpu_bundle& bundle, float2 uv,
+                                          float4* lp, float4* lt, float4* ls, const hg_gpu_bundle& bundle, float2 uv,
                                           uint32_t ncp, uint32_t lane, f3 mp[4], float wk[4], float aok[4]) {
     float4 loaded = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     if (lane < kLayerCount) {
@@ -477,6 +495,7 @@ __device__ __forceinline__ void model_cps(const float4* __restrict__ layers, con
         lp[lane] = loaded;
         lt[lane] = make_float4(t.x, t.y, t.z, 0.0f);
     }
+    style_layers(style, bundle.style_offset, uv, ls, lane);
     __syncwarp();
     const float den = __uint2float_rn(max(ncp - 1u, 1u));
 #pragma unroll
@@ -492,7 +511,7 @@ __device__ __forceinline__ void model_cps(const float4* __restrict__ layers, con
             float t = layers_f - __uint2float_rn(i0);
             float4 la = lp[i0], lb = lp[i1];
             f3 base = hermite(xyz(la), xyz(lb), xyz(lt[i0]), xyz(lt[i1]), t);
-            f3 res = sample_style(style, bundle.style_offset, uv, w);
+            f3 res = style_at(ls, w);
             mp[k] = add3(base, res);
             wk[k] = w;
             aok[k] = mixf(la.w, lb.w, t);
@@ -579,7 +598,7 @@ __device__ __forceinline__ uint32_t generate_strand(const Args& a, StrandSmem& s
     }
     f3 mp[4];
     float wk[4], aok[4];
-    model_cps(a.layers, a.style, sm.u.gen.lp, sm.u.gen.lt, bundle, uv, ncp, lane, mp, wk, aok);
+    model_cps(a.layers, a.style, sm.u.gen.lp, sm.u.gen.lt, sm.u.gen.ls, bundle, uv, ncp, lane, mp, wk, aok);
     generate_slot<0, MODE>(p, sm, mp, wk, aok, ncp, lane);
     generate_slot<1, MODE>(p, sm, mp, wk, aok, ncp, lane);
     generate_slot<2, MODE>(p, sm, mp, wk, aok, ncp, lane);
@@ -851,10 +870,11 @@ __device__ __forceinline__ void dom_write(const Args& a, int32_t px, int32_t py,
     if (px < 0 || py < 0 || px >= width || py >= height) return;
     const uint32_t dom_w = f2u(p.dom_info[0]);
     const uint32_t pix = (uint32_t)py * dom_w + (uint32_t)px;
-    // Mode 2 needs the texel's front depth (final after mode 1); mode 1's
-    // atomicMin is fire-and-forget, which beats reading the word first in this
-    // sequential per-lane loop.
-    const uint32_t cur = MODE == 2 ? __ldcg(&a.dom[pix]) : 0u;
+    // Mode 2 needs the texel's front depth (final after mode 1, and no word of
+    // the front plane is written during mode 2, so the read-only path may
+    // cache it); mode 1's atomicMin is fire-and-forget, which beats reading
+    // the word first in this sequential per-lane loop.
+    const uint32_t cur = MODE == 2 ? __ldg(&a.dom[pix]) : 0u;
     if (MODE == 2 && cur == kDomEmpty) return;
     const float2 ctr = make_float2(__int2float_rn(px) + 0.5f, __int2float_rn(py) + 0.5f);
     const float t = clampf(__fdiv_rn(dot2(sub2(ctr, A), seg), seg_len2), 0.0f, 1.0f);
@@ -929,14 +949,15 @@ struct GenArgs {
 
 // Strand g of a groom into its cache slot (one warp).
 template <class Args>
-__device__ __forceinline__ void generate_one(const Args& a, uint32_t g, float4* lp, float4* lt, uint32_t lane) {
+__device__ __forceinline__ void generate_one(const Args& a, uint32_t g, float4* lp, float4* lt, float4* ls,
+                                             uint32_t lane) {
     const uint32_t b = a.strand_bundle[g];
     const uint32_t s = g - a.strand_base[b];
     const hg_gpu_bundle bundle = a.bundles[b];
     const float2 uv = pcg_uv(s ^ (b * 0x85ebca6bu));
     f3 mp[4];
     float wk[4], aok[4];
-    model_cps(a.layers, a.style, lp, lt, bundle, uv, kCacheCps, lane, mp, wk, aok);
+    model_cps(a.layers, a.style, lp, lt, ls, bundle, uv, kCacheCps, lane, mp, wk, aok);
     float4* pos = a.cache + (size_t)g * (2u * kCacheCps);
     float4* tan = pos + kCacheCps;
 #pragma unroll
@@ -959,10 +980,11 @@ __device__ __forceinline__ void generate_one(const Args& a, uint32_t g, float4* 
 __global__ void __launch_bounds__(kRasterThreads) generate_kernel(const GenArgs a) {
     __shared__ float4 lp[kRasterWarps][16];
     __shared__ float4 lt[kRasterWarps][16];
+    __shared__ float4 ls[kRasterWarps][16];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t nwarps = gridDim.x * kRasterWarps;
     for (uint32_t g = blockIdx.x * kRasterWarps + warp; g < a.strands; g += nwarps)
-        generate_one(a, g, lp[warp], lt[warp], lane);
+        generate_one(a, g, lp[warp], lt[warp], ls[warp], lane);
 }
 
 // raster.wgsl:225-337: one warp per strand ref, persistent over the refs.
@@ -1056,11 +1078,12 @@ __global__ void __launch_bounds__(kRasterThreads) batch_generate_kernel(const Ba
                                                                         uint32_t n_cam, uint32_t total) {
     __shared__ float4 lp[kRasterWarps][16];
     __shared__ float4 lt[kRasterWarps][16];
+    __shared__ float4 ls[kRasterWarps][16];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t nwarps = gridDim.x * kRasterWarps;
     for (uint32_t g = blockIdx.x * kRasterWarps + warp; g < total; g += nwarps) {
         const uint32_t v = find_view(prefix, n_cam, g);
-        generate_one(views[v], g - prefix[v], lp[warp], lt[warp], lane);
+        generate_one(views[v], g - prefix[v], lp[warp], lt[warp], ls[warp], lane);
     }
 }
 
