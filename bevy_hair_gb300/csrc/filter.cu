@@ -62,6 +62,20 @@ __device__ __forceinline__ void filter_tile(const V& a, int32_t bx, int32_t by) 
     const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
     const int32_t x0 = bx * TX - kFilterRadius, y0 = by * TY - kFilterRadius;
     const int tid = threadIdx.y * TX + threadIdx.x;
+    const int32_t px = bx * TX + threadIdx.x, py = by * TY + threadIdx.y;
+    const bool inside = px < width && py < height;
+    const uint32_t pix = (uint32_t)py * (uint32_t)width + (uint32_t)px;
+    const unsigned long long center_word = inside ? __ldg(&a.center[pix]) : kEmptyU64;
+    const unsigned long long cons_word = inside ? __ldg(&a.cons[pix]) : kEmptyU64;
+    const bool center_hit = !is_empty(center_word), cons_hit = !is_empty(cons_word);
+    // A tile without hair writes zeros and needs no halo.
+    if (!__syncthreads_or(center_hit || cons_hit)) {
+        if (inside) {
+            a.filtered[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            a.filtered_depth[pix] = 0.0f;
+        }
+        return;
+    }
     for (int i = tid; i < kHaloX * kHaloY; i += TX * TY) {
         int hx = i % kHaloX, hy = i / kHaloX;
         int32_t gx = x0 + hx, gy = y0 + hy;
@@ -82,11 +96,7 @@ __device__ __forceinline__ void filter_tile(const V& a, int32_t bx, int32_t by) 
     }
     __syncthreads();
 
-    const int32_t px = bx * TX + threadIdx.x, py = by * TY + threadIdx.y;
-    if (px >= width || py >= height) return;
-    const uint32_t pix = (uint32_t)py * (uint32_t)width + (uint32_t)px;
-    const unsigned long long center_word = __ldg(&a.center[pix]), cons_word = __ldg(&a.cons[pix]);
-    const bool center_hit = !is_empty(center_word), cons_hit = !is_empty(cons_word);
+    if (!inside) return;
     if (!center_hit && !cons_hit) {
         a.filtered[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         a.filtered_depth[pix] = 0.0f;
@@ -141,15 +151,18 @@ __device__ __forceinline__ void filter_tile(const V& a, int32_t bx, int32_t by) 
             if (nrm < 0.0f) continue;
             if (fabsf(nrm - p_norm) > depth_reject) continue;
             const float4 qcol = s_col[ly + dy][lx + dx];
-            float e = d_par * d_par * k_par + e2 * k_perp;
+            // The colour weights are compared within a tolerance, so they use
+            // fused multiply-adds (this file is otherwise built without
+            // contraction for the exact strip and coverage tests above).
+            float e = __fmaf_rn(d_par * d_par, k_par, e2 * k_perp);
             if (use_color) {
                 const float cx = cc.x - qcol.x, cy = cc.y - qcol.y, cz = cc.z - qcol.z;
-                e += (cx * cx + cy * cy + cz * cz) * k_col;
+                e = __fmaf_rn(__fmaf_rn(cz, cz, __fmaf_rn(cy, cy, cx * cx)), k_col, e);
             }
             const float wgt = exp2f(-e);
-            ax += qcol.x * wgt;
-            ay += qcol.y * wgt;
-            az += qcol.z * wgt;
+            ax = __fmaf_rn(qcol.x, wgt, ax);
+            ay = __fmaf_rn(qcol.y, wgt, ay);
+            az = __fmaf_rn(qcol.z, wgt, az);
             weight += wgt;
         }
     }

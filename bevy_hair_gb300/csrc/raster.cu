@@ -1220,7 +1220,10 @@ cudaError_t launch_lod(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int sl
 
 cudaError_t launch_scan(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot) {
     uint32_t count = std::min(p.pass_mode[1], g->bundle_count);
-    // The camera pass draws near bundles first; the DOM passes gain nothing from it.
+    // The camera pass draws near bundles first (its later stage skips what the
+    // tile depths hide).  Sorting the DOM refs by light depth and staging the DOM
+    // depth pass the same way measured slower (0.195 vs 0.170 ms on config 2):
+    // its lanes walk one segment each, so a skipped segment rarely frees a warp.
     const bool order = p.pass_mode[0] == 0u;
     scan_offsets_kernel<<<1, kScanThreads, 0, ctx->stream>>>(
         g->lod[slot], count, g->ref_capacity, g->offsets[slot], g->indirect[slot], g->depth_key[slot],

@@ -165,15 +165,16 @@ def test_strand_cache_gives_the_same_visibility(renderer, name):
 
 
 def test_dense_groom_with_tile_depth_rejection(renderer):
-    """A dense groom at low resolution (deep overdraw): the camera pass's later
-    stages skip most segments behind the tile depths, and the buffers must not
-    change."""
+    """A dense groom at low resolution (deep overdraw) with a small deep
+    opacity map: the later stages of the camera and DOM depth passes skip most
+    segments behind the tile depths, and no buffer may change."""
     sc = configs.config2(scale=0.25)
     sc.view = configs._camera(384, 216, 900.0)
+    sc.dom_size = (192, 192)
     cam, dom = sc.params()
-    got = _visibility(renderer, sc, cam, None)
-    want = _oracle_visibility(sc, cam, None)
-    _check_visibility(got, want, with_dom=False)
+    got = _visibility(renderer, sc, cam, dom)
+    want = _oracle_visibility(sc, cam, dom)
+    _check_visibility(got, want)
     covered = int((want["center"] != EMPTY).sum())
     assert covered > 5000 and want["counts"]["samples"] > 50 * covered
 
