@@ -379,7 +379,8 @@ def batch_measure(r, stream, flush, steps: int, warmup: int, scale: float) -> di
         "gseg_per_s": round(segs / (graph_ms * 1e-3) / 1e9, 4),
         "launches": {"graph": b.launches(abi.BATCH_GRAPH), "separate": b.launches(abi.BATCH_SEPARATE)},
         "phase_ms": phase_ms,
-        "tuning": {"chosen": b.tuning(), "tried": tuning},
+        "tuning": {"chosen": {k: round(v, 4) for k, v in b.tuning().items()},
+                   "tried": [{k: round(v, 4) for k, v in t.items()} for t in tuning]},
         "e2e": {"ms_per_frame": round(e2e_ms, 4), "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
         "bake_s": round(t_bake, 1),
     }

@@ -170,7 +170,9 @@ class BatchTuning(C.Structure):
     ]
 
     def as_dict(self) -> dict:
-        return {n: (round(float(getattr(self, n)), 4) if n == "ms" else int(getattr(self, n))) for n, _ in self._fields_}
+        # ms unrounded: the tuner keeps the strictly fastest shape, and rounding
+        # here would turn near ties into ties
+        return {n: (float(getattr(self, n)) if n == "ms" else int(getattr(self, n))) for n, _ in self._fields_}
 
 
 BATCH_GRAPH, BATCH_LAUNCHES, BATCH_SEPARATE = 0, 1, 2

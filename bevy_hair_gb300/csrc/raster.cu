@@ -153,6 +153,7 @@ __global__ void lod_kernel(const hg_hair_params p, const hg_gpu_bundle* __restri
 // n_lod into offsets and the indirect arguments (total, 1, 1) with the total
 // clamped to the refs capacity.
 constexpr int kScanThreads = 1024;
+constexpr uint32_t kScanItems = 16;  // bundles per thread per scan pass
 
 // Block-wide exclusive scan of one value per thread; returns the thread's
 // exclusive prefix and, through *total, the block's sum.
@@ -184,6 +185,45 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* w
     return r;
 }
 
+// One pass of a block-wide exclusive scan over elements [base, base + 1024 *
+// kScanItems) of n: warp w takes the 32 * kScanItems elements from base +
+// 32 * kScanItems * w, lane-interleaved so loads and stores coalesce; all its
+// loads are issued before the first shuffle.  store(i, carry + exclusive
+// prefix) for every i < n in the pass; returns the pass total.
+template <class Load, class Store>
+__device__ __forceinline__ uint32_t scan_pass(uint32_t base, uint32_t n, uint32_t carry, uint32_t* warp_sums,
+                                              Load load, Store store) {
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t wbase = base + warp * 32u * kScanItems;
+    uint32_t v[kScanItems];
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+        const uint32_t i = wbase + k * 32u + lane;
+        v[k] = i < n ? load(i) : 0u;
+    }
+    uint32_t pre[kScanItems];
+    uint32_t wrun = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+        uint32_t incl = v[k];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        pre[k] = wrun + incl - v[k];
+        wrun += __shfl_sync(0xffffffffu, incl, 31);
+    }
+    uint32_t total = 0;
+    const uint32_t woff = block_exclusive_scan(lane == 31u ? wrun : 0u, warp_sums, &total);
+#pragma unroll
+    for (uint32_t k = 0; k < kScanItems; ++k) {
+        const uint32_t i = wbase + k * 32u + lane;
+        if (i < n) store(i, carry + woff + pre[k]);
+    }
+    return total;
+}
+
 __device__ __forceinline__ void scan_offsets_block(const hg_lod_record* __restrict__ lod, uint32_t count,
                                                    uint32_t capacity, uint32_t* __restrict__ offsets,
                                                    uint32_t* __restrict__ indirect,
@@ -191,39 +231,12 @@ __device__ __forceinline__ void scan_offsets_block(const hg_lod_record* __restri
                                                    uint32_t* __restrict__ sorted, uint32_t* __restrict__ sorted_off,
                                                    uint32_t* __restrict__ order_meta) {
     __shared__ uint32_t warp_sums[33];
-    __shared__ uint32_t carry;
     __shared__ uint32_t bucket[kDepthBuckets];
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    for (uint32_t base = 0; base < count; base += kScanThreads) {
-        uint32_t i = base + threadIdx.x;
-        uint32_t v = i < count ? lod[i].n_lod : 0u;
-        uint32_t incl = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= (uint32_t)o) incl += y;
-        }
-        if (lane == 31) warp_sums[warp] = incl;
-        __syncthreads();
-        if (warp == 0) {
-            uint32_t s = warp_sums[lane];
-            uint32_t si = s;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                uint32_t y = __shfl_up_sync(0xffffffffu, si, o);
-                if (lane >= (uint32_t)o) si += y;
-            }
-            warp_sums[lane] = si - s;  // exclusive warp offsets
-        }
-        __syncthreads();
-        uint32_t c = carry;
-        if (i < count) offsets[i] = c + warp_sums[warp] + incl - v;
-        __syncthreads();
-        if (threadIdx.x == kScanThreads - 1) carry = c + warp_sums[warp] + incl;
-        __syncthreads();
-    }
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < count; base += kScanThreads * kScanItems)
+        carry += scan_pass(
+            base, count, carry, warp_sums, [&](uint32_t i) { return lod[i].n_lod; },
+            [&](uint32_t i, uint32_t at) { offsets[i] = at; });
     if (threadIdx.x == 0) {
         uint32_t total = carry < capacity ? carry : capacity;
         offsets[count] = carry;
@@ -240,26 +253,41 @@ __device__ __forceinline__ void scan_offsets_block(const hg_lod_record* __restri
     const uint32_t full = carry;
     for (uint32_t k = threadIdx.x; k < kDepthBuckets; k += kScanThreads) bucket[k] = 0u;
     __syncthreads();
-    for (uint32_t b = threadIdx.x; b < count; b += kScanThreads)
-        if (lod[b].n_lod) atomicAdd(&bucket[depth_key[b]], 1u);
+    // keys of live bundles, loaded a pass at a time before the shared atomics
+    for (uint32_t base = 0; base < count; base += kScanThreads * kScanItems) {
+        uint32_t key[kScanItems];
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) {
+            const uint32_t b = base + k * kScanThreads + threadIdx.x;
+            key[k] = b < count && lod[b].n_lod ? depth_key[b] : kDepthBuckets;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k)
+            if (key[k] < kDepthBuckets) atomicAdd(&bucket[key[k]], 1u);
+    }
     __syncthreads();
     uint32_t live = 0;
     const uint32_t start = block_exclusive_scan(threadIdx.x < kDepthBuckets ? bucket[threadIdx.x] : 0u, warp_sums,
                                                 &live);
     if (threadIdx.x < kDepthBuckets) bucket[threadIdx.x] = start;
     __syncthreads();
-    for (uint32_t b = threadIdx.x; b < count; b += kScanThreads)
-        if (lod[b].n_lod) sorted[atomicAdd(&bucket[depth_key[b]], 1u)] = b;
+    for (uint32_t base = 0; base < count; base += kScanThreads * kScanItems) {
+        uint32_t key[kScanItems];
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k) {
+            const uint32_t b = base + k * kScanThreads + threadIdx.x;
+            key[k] = b < count && lod[b].n_lod ? depth_key[b] : kDepthBuckets;
+        }
+#pragma unroll
+        for (uint32_t k = 0; k < kScanItems; ++k)
+            if (key[k] < kDepthBuckets) sorted[atomicAdd(&bucket[key[k]], 1u)] = base + k * kScanThreads + threadIdx.x;
+    }
     __syncthreads();
     uint32_t run = 0;
-    for (uint32_t base = 0; base < live; base += kScanThreads) {
-        const uint32_t k = base + threadIdx.x;
-        const uint32_t v = k < live ? lod[sorted[k]].n_lod : 0u;
-        uint32_t sum = 0;
-        const uint32_t ex = block_exclusive_scan(v, warp_sums, &sum);
-        if (k < live) sorted_off[k] = run + ex;
-        run += sum;
-    }
+    for (uint32_t base = 0; base < live; base += kScanThreads * kScanItems)
+        run += scan_pass(
+            base, live, run, warp_sums, [&](uint32_t i) { return lod[sorted[i]].n_lod; },
+            [&](uint32_t i, uint32_t at) { sorted_off[i] = at; });
     if (threadIdx.x == 0) {
         sorted_off[live] = run;
         order_meta[0] = live;
@@ -630,6 +658,47 @@ __device__ __forceinline__ bool on_screen(int32_t x, int32_t y, int32_t w, int32
     return x >= 0 && y >= 0 && x < w && y < h;
 }
 
+// Flattened sample lists.  The camera and DOM rasters cut each segment of a
+// strand into samples and hand them to the 32 lanes 32 at a time; segments
+// with samples ("runs") are listed in order with their first sample.
+
+// Appends this round's 32 segments (one per lane, cnt samples each, tag
+// stored with the run) to the run list.  Every lane of the warp calls it.
+__device__ __forceinline__ void append_runs(StrandSmem& sm, int32_t cnt, int32_t tag, uint32_t lane,
+                                            int32_t& carry, int32_t& runs) {
+    int32_t incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int32_t)lane >= o) incl += y;
+    }
+    const uint32_t live = __ballot_sync(0xffffffffu, cnt > 0);
+    if (cnt > 0) {
+        const int32_t r = runs + __popc(live & ((1u << lane) - 1u));
+        sm.u.run.off[r] = carry + incl - cnt;
+        sm.u.run.seg[r] = tag;
+    }
+    carry += __shfl_sync(0xffffffffu, incl, 31);
+    runs += __popc(live);
+}
+
+// The run holding sample base + lane, for the window of samples [base,
+// base + 32); rw is the run holding sample `base` and advances to the one
+// holding base + 32.  Lane k holds the start of run rw+1+k: at most 32 runs
+// start in (base, base + 32], one per sample.  Bit q of `starts` marks a run
+// starting at base + q, so sample s lies in run rw + (starts in (base, s]).
+// Every lane of the warp calls it.
+__device__ __forceinline__ int32_t run_of_lane(const StrandSmem& sm, int32_t runs, int32_t& rw, int32_t base,
+                                               uint32_t lane) {
+    const int32_t rk = rw + 1 + (int32_t)lane;
+    const int32_t ok = rk < runs ? sm.u.run.off[rk] : 0x7fffffff;
+    const int32_t rel = ok - base;
+    const uint32_t starts = __reduce_or_sync(0xffffffffu, rel > 0 && rel < 32 ? 1u << rel : 0u);
+    const int32_t r = rw + __popc(starts & (0xffffffffu >> (31u - lane)));
+    rw += __popc(__ballot_sync(0xffffffffu, ok <= base + 32));
+    return r;
+}
+
 // Pixels per side of a tile of the camera pass's tile-depth buffer.
 constexpr int kTileShift = 3;
 // Stage boundaries of the camera pass over the refs in draw order, in 1/256ths.
@@ -738,20 +807,7 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
             }
             sm.cs[j].w = n > 0 ? __frcp_rn(__int2float_rn(n)) : 0.0f;
         }
-        int32_t incl = cnt;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-            if ((int32_t)lane >= o) incl += y;
-        }
-        const uint32_t live = __ballot_sync(0xffffffffu, cnt > 0);
-        if (cnt > 0) {
-            const int32_t r = runs + __popc(live & ((1u << lane) - 1u));
-            sm.u.run.off[r] = carry + incl - cnt;
-            sm.u.run.seg[r] = j | (cnt - 1) << 8;
-        }
-        carry += __shfl_sync(0xffffffffu, incl, 31);
-        runs += __popc(live);
+        append_runs(sm, cnt, j | (cnt - 1) << 8, lane, carry, runs);
     }
     __syncwarp();
 
@@ -765,16 +821,7 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
     for (int32_t base = 0; base < total; base += 32) {
         const int32_t s = min(base + (int32_t)lane, total - 1);
         const bool active = base + (int32_t)lane < total;
-        // Runs starting inside this window of 32 samples: at most 16, since a
-        // run has two samples or more.  Lane k holds the start of run rw+1+k;
-        // bit q of `starts` marks a run starting at base + q.  Sample s lies in
-        // run rw + (starts in (base, s]), the run with the last start <= s.
-        const int32_t rk = rw + 1 + (int32_t)lane;
-        const int32_t ok = rk < runs ? sm.u.run.off[rk] : 0x7fffffff;
-        const int32_t rel = ok - base;
-        const uint32_t starts = __reduce_or_sync(0xffffffffu, rel > 0 && rel < 32 ? 1u << rel : 0u);
-        const int32_t r = rw + __popc(starts & (0xffffffffu >> (31u - lane)));
-        rw += __popc(__ballot_sync(0xffffffffu, ok <= base + 32));
+        const int32_t r = run_of_lane(sm, runs, rw, base, lane);
         const int32_t jn = sm.u.run.seg[r];
         const int32_t j = jn & 0xff, i = s - sm.u.run.off[r];
         const float4 A = sm.cs[j], B = sm.cs[j + 1];
@@ -895,7 +942,13 @@ __device__ __forceinline__ void dom_write(const Args& a, int32_t px, int32_t py,
     atomicAdd(&a.dom[pixels + pix * kDomLayers + slice], 1u);
 }
 
-// draw_dom_segment (raster.wgsl:150-190), one segment per lane.
+// draw_dom_segment (raster.wgsl:150-190), one segment per lane: the
+// all-octant Bresenham walk from floor(a) to floor(b), at most 1024 steps, the
+// start pixel skipped for all but the first segment unless the segment stays
+// in one pixel.  (A flattened variant that spreads the walks' pixels evenly
+// over the lanes, each pixel found in closed form, measured slower on config
+// 2: segments average 3.3 pixels, and recomputing each pixel's segment state
+// costs more than the idle lanes of the per-lane walk.)
 template <int MODE, class Args>
 __device__ __forceinline__ void raster_dom(const Args& a, StrandSmem& sm, uint32_t ncp, uint32_t lane) {
     const hg_hair_params& p = a.p;
