@@ -654,6 +654,15 @@ __device__ __forceinline__ uint32_t hi_word(const unsigned long long* w) {
     return __ldcg(reinterpret_cast<const unsigned int*>(w) + 1);
 }
 
+// The same through L1 (ld.global.ca).  L1 is not coherent with other SMs'
+// atomics, so the value may be one the word held earlier in the pass; words
+// only decrease, so it is still an upper bound of the current word.
+__device__ __forceinline__ uint32_t hi_word_l1(const unsigned long long* w) {
+    uint32_t r;
+    asm("ld.global.ca.u32 %0, [%1];" : "=r"(r) : "l"(reinterpret_cast<const unsigned int*>(w) + 1));
+    return r;
+}
+
 __device__ __forceinline__ bool on_screen(int32_t x, int32_t y, int32_t w, int32_t h) {
     return x >= 0 && y >= 0 && x < w && y < h;
 }
@@ -844,15 +853,15 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
         const uint32_t pix0 = (uint32_t)py * (uint32_t)width + (uint32_t)px;
         const uint32_t pix1 = (uint32_t)py * (uint32_t)width + (uint32_t)qx;
         const uint32_t pix2 = (uint32_t)qy * (uint32_t)width + (uint32_t)px;
-        // High words (depth, tangent x) of the current payloads, read from L2
+        // High words (depth, tangent x) of the current payloads, read through L1
         // before the payload is known.  Buffers only decrease during the pass,
         // so a stale read is an upper bound, and a payload whose high word is
         // above it cannot lower the word: its atomicMin is skipped.  Equal high
         // words go to the atomic, which decides.
-        const uint32_t cur_c0 = on0 ? hi_word(&a.cons[pix0]) : 0u;
-        const uint32_t cur_m0 = on0 ? hi_word(&a.center[pix0]) : 0u;
-        const uint32_t cur_c1 = on1 ? hi_word(&a.cons[pix1]) : 0u;
-        const uint32_t cur_c2 = on2 ? hi_word(&a.cons[pix2]) : 0u;
+        const uint32_t cur_c0 = on0 ? hi_word_l1(&a.cons[pix0]) : 0u;
+        const uint32_t cur_m0 = on0 ? hi_word_l1(&a.center[pix0]) : 0u;
+        const uint32_t cur_c1 = on1 ? hi_word_l1(&a.cons[pix1]) : 0u;
+        const uint32_t cur_c2 = on2 ? hi_word_l1(&a.cons[pix2]) : 0u;
 
         // write_pixel (raster.wgsl:83-115): depth first; the rest of the payload
         // only when some word can still take it.
