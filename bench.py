@@ -533,9 +533,9 @@ def run_ours(args, rank, world, local):
     peak, peak_kind = peaks()
     achieved = nbytes[dominant] / (acc[dominant] * 1e-3) / 1e9
     traffic, traffic_src = None, None
-    try:  # DRAM bytes per launch from the committed ncu capture of this workload
+    try:  # DRAM bytes of the pass (its launches summed) from the committed ncu capture of this workload
         tj = json.loads((ROOT / "profiles" / "traffic.json").read_text())
-        traffic, traffic_src = tj["per_launch"][dominant]["dram_bytes"], tj["profile"]
+        traffic, traffic_src = tj["per_pass"][dominant]["dram_bytes"], tj["profile"]
     except (OSError, KeyError, ValueError):
         pass
     per_pass_roofline = {
