@@ -156,6 +156,7 @@ hg_status hg_create(int device, void* stream, hg_ctx** out) {
         }
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = hg::ensure_shade_setup(device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
     for (cudaEvent_t* ev : {&ctx->ev_fork, &ctx->ev_gen, &ctx->ev_join, &ctx->ev_copy_src, &ctx->ev_copy_done})
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);

@@ -172,6 +172,8 @@ struct BatchDev {
 };
 
 // raster.cu
+// Once per device before the first shade launch: the dual-scattering angle table.
+cudaError_t ensure_shade_setup(int device);
 cudaError_t launch_clear(hg_ctx* ctx);
 cudaError_t launch_clear_dom(hg_ctx* ctx);
 cudaError_t launch_lod(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot);

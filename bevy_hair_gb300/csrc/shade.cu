@@ -4,6 +4,8 @@
 // file compiles with FMA contraction on.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
 #include <mutex>
 
 #include "hg_device.cuh"
@@ -102,14 +104,59 @@ __device__ __forceinline__ f3 lobe_mean(const Lobes& l, f3 total, f3 q) {
     return vdiv(num, vmaxs(total, 1e-5f));
 }
 
+// The azimuthal angles dual_scatter integrates over are fixed: per step i,
+// cos phi at u = (i + 0.5) / kScatterSteps for the back half (phi = u pi/2)
+// and the front half (phi = (1 + u) pi/2), with the factors of azimuthal()
+// that depend on phi alone: cos(phi/2), exp(-3.65 cos phi - 3.98) and
+// exp(17 cos phi - 16.78).  Filled from double precision on the host.
+struct ScatterAngle {
+    float cos_phi, cos_half_phi, k_tt, k_trt;
+};
+__constant__ ScatterAngle c_scatter[2 * kScatterSteps];  // [0, steps): back, [steps, 2 steps): front
+
+// azimuthal() at one of those angles, with the terms that depend only on the
+// pixel (cos theta_d, sigma_a) computed once by the caller.
+struct AzimuthPixel {
+    float cos_theta_d, inv_ctd, a;
+    f3 sigma_a;
+    f3 trt;  // exp(-sigma_a 3.2 / cos theta_d) (1 - F)^2 F with F = fresnel(cos theta_d / 2)
+};
+
+__device__ __forceinline__ AzimuthPixel azimuth_pixel(float cos_theta_d, f3 sigma_a) {
+    AzimuthPixel q;
+    q.cos_theta_d = cos_theta_d;
+    q.inv_ctd = 1.0f / cos_theta_d;
+    const float eta = 1.19f * q.inv_ctd + 0.36f * cos_theta_d;
+    q.a = 1.0f / eta;
+    q.sigma_a = sigma_a;
+    const float f_trt = fresnel(cos_theta_d * 0.5f);
+    const float trt_path = 3.2f * q.inv_ctd;
+    const float k = (1.0f - f_trt) * (1.0f - f_trt) * f_trt;
+    q.trt = {expf(-sigma_a.x * trt_path) * k, expf(-sigma_a.y * trt_path) * k, expf(-sigma_a.z * trt_path) * k};
+    return q;
+}
+
+__device__ __forceinline__ Lobes azimuthal_at(const AzimuthPixel& q, const ScatterAngle& g) {
+    const float n_r = 0.25f * g.cos_half_phi * fresnel(q.cos_theta_d * g.cos_half_phi);
+    const float h = g.cos_half_phi * (1.0f + q.a * (0.6f - 0.8f * g.cos_phi));
+    const float f_tt = fresnel(q.cos_theta_d * sqrtf(clampf(1.0f - h * h, 0.0f, 1.0f)));
+    const float path = 2.0f * sqrtf(clampf(1.0f - h * h * q.a * q.a, 0.0f, 1.0f)) * q.inv_ctd;
+    const float k_tt = g.k_tt * (1.0f - f_tt) * (1.0f - f_tt);
+    Lobes r;
+    r.r = spl(n_r);
+    r.tt = {expf(-q.sigma_a.x * path) * k_tt, expf(-q.sigma_a.y * path) * k_tt, expf(-q.sigma_a.z * path) * k_tt};
+    r.trt = mul3s(q.trt, g.k_trt);
+    return r;
+}
+
 // dual_scatter (shade.wesl:153-190)
 __device__ Dual dual_scatter(float cos_theta_d, f3 sigma_a, const Shape& shape) {
     Lobes fwd = {spl(0.0f), spl(0.0f), spl(0.0f)}, back = fwd;
+    const AzimuthPixel q = azimuth_pixel(cos_theta_d, sigma_a);
 #pragma unroll 2
     for (int i = 0; i < kScatterSteps; ++i) {
-        float u = ((float)i + 0.5f) / (float)kScatterSteps;
-        Lobes b = azimuthal(cos_theta_d, cosf(u * 0.5f * kPi), sigma_a);
-        Lobes f = azimuthal(cos_theta_d, cosf((1.0f + u) * 0.5f * kPi), sigma_a);
+        Lobes b = azimuthal_at(q, c_scatter[i]);
+        Lobes f = azimuthal_at(q, c_scatter[kScatterSteps + i]);
         back.r = add3(back.r, b.r);
         back.tt = add3(back.tt, b.tt);
         back.trt = add3(back.trt, b.trt);
@@ -158,9 +205,8 @@ struct Geometry {
     float sin_i, sin_o, theta_h, cos_theta_d, cos_phi;
 };
 
-__device__ __forceinline__ Geometry light_geometry(f3 tangent, f3 view, f3 light) {
-    f3 t = safe_normalize(tangent);
-    f3 v = safe_normalize(view);
+// t and v arrive normalized (once per pixel); the light direction per light.
+__device__ __forceinline__ Geometry light_geometry(f3 t, f3 v, f3 light) {
     f3 l = safe_normalize(light);
     Geometry g;
     g.sin_i = clampf(dot3(t, l), -1.0f, 1.0f);
@@ -193,9 +239,10 @@ __device__ f3 spread_term(const Shape& shape, const Dual& ds, float theta_h, flo
     return vmul(mul3s(transmit, (1.0f - direct) * kDensityFront), inner);
 }
 
-// hair_bsdf (shade.wesl:193-244)
-__device__ f3 hair_bsdf(f3 tangent, f3 view, f3 light, f3 sigma_a, const Shape& shape, const Dual& ds, float depth) {
-    const Geometry gm = light_geometry(tangent, view, light);
+// hair_bsdf (shade.wesl:193-244); t_n and v_n are the normalized tangent and view.
+__device__ __forceinline__ f3 hair_bsdf(f3 t_n, f3 v_n, f3 light, f3 sigma_a, const Shape& shape, const Dual& ds,
+                                        float depth) {
+    const Geometry gm = light_geometry(t_n, v_n, light);
     Lobes n = azimuthal(gm.cos_theta_d, gm.cos_phi, sigma_a);
     f3 x = spl(gm.theta_h);
     f3 m = gaussian3(shape.beta, sub3(x, shape.alpha));
@@ -444,45 +491,45 @@ __device__ __forceinline__ void shade_pixel(const V& a, const hg_light* __restri
     const Dual ds = dual_scatter(cos_theta_o, sigma_a, shape);
     f3 color = spl(0.0f);
     bool dom_left = true;
+    const f3 t_n = safe_normalize(tangent), v_n = safe_normalize(view);
     for (uint32_t i = 0; i < n_lights; ++i) {
         const hg_light& L = lights[i];
         const uint32_t kind = L.kind;
+        // each kind gives the incident direction, a weight and the DOM depth;
+        // one BSDF evaluation serves them all
+        f3 incident = spl(0.0f);
+        float weight = 0.0f, depth = 0.0f;
         if (kind == HG_LIGHT_POINT || kind == HG_LIGHT_SPOT) {
             f3 to_l = sub3(ld3(L.position), world);
             float dist2 = dot3(to_l, to_l);
-            f3 incident = safe_normalize(to_l);
+            incident = safe_normalize(to_l);
             float inv_r2 = 1.0f / fmaxf(L.range * L.range, 1e-8f);
-            float att = range_window(dist2, inv_r2) / fmaxf(dist2, 1e-4f);
+            weight = range_window(dist2, inv_r2) / fmaxf(dist2, 1e-4f);
             if (kind == HG_LIGHT_SPOT) {
                 float cd = dot3(mul3s(ld3(L.direction), -1.0f), incident);
                 float sm = clampf(cd * L.spot[0] + L.spot[1], 0.0f, 1.0f);
-                att *= sm * sm;
-            }
-            if (att > 0.0f) {
-                f3 lobe = hair_bsdf(tangent, view, incident, sigma_a, shape, ds, 0.0f);
-                color = add3(color, mul3s(vmul(lobe, ld3(L.color)), att));
+                weight *= sm * sm;
             }
         } else if (kind == HG_LIGHT_DIRECTIONAL) {
-            float depth = 0.0f;
             if (dom_left && (L.flags & HG_LIGHT_CASTS_SHADOWS)) {
                 depth = -logf(fmaxf(dom_visibility(p, a.dom, world, beta), 1e-6f));
                 dom_left = false;
             }
-            f3 lobe = hair_bsdf(tangent, view, ld3(L.direction), sigma_a, shape, ds, depth);
-            color = add3(color, vmul(lobe, ld3(L.color)));
+            incident = ld3(L.direction);
+            weight = 1.0f;
         } else if (kind == HG_LIGHT_RECT) {
             f3 to_c = sub3(ld3(L.position), world);
             float dist2 = fmaxf(dot3(to_c, to_c), 1e-4f);
-            f3 incident = mul3s(to_c, rsqrtf(dist2));
+            incident = mul3s(to_c, rsqrtf(dist2));
             f3 normal = safe_normalize(cross3(ld3(L.up), ld3(L.right)));
             float facing = fmaxf(dot3(normal, incident), 0.0f);
             float solid = L.spot[0] * L.spot[1] * facing / dist2;
             float range2 = fmaxf(L.range * L.range, 1e-4f);
-            float falloff = range_window(dist2, 1.0f / range2);
-            if (solid * falloff > 0.0f) {
-                f3 lobe = hair_bsdf(tangent, view, incident, sigma_a, shape, ds, 0.0f);
-                color = add3(color, mul3s(vmul(lobe, ld3(L.color)), solid * falloff));
-            }
+            weight = solid * range_window(dist2, 1.0f / range2);
+        }
+        if (weight > 0.0f) {
+            f3 lobe = hair_bsdf(t_n, v_n, incident, sigma_a, shape, ds, depth);
+            color = add3(color, mul3s(vmul(lobe, ld3(L.color)), weight));
         }
     }
     if (env.spec) {
@@ -632,7 +679,7 @@ __global__ void __launch_bounds__(kSurrogateWarps * 32, 2)
             if (depth > 1e-3f) {
                 const float tv = dot3(tangent, view);
                 const Dual ds = dual_scatter(sqrtf(fmaxf(1.0f - tv * tv, 1e-6f)), sigma_a, shape);
-                const Geometry gm = light_geometry(tangent, view, ld3(L.direction));
+                const Geometry gm = light_geometry(t_n, v_n, ld3(L.direction));
                 color = vmul(spread_term(shape, ds, gm.theta_h, depth, dom_direct), ld3(L.color));
             }
         }
@@ -807,7 +854,7 @@ __global__ void __launch_bounds__(mlp::tc::kThreads, 1)
             if (depth > 1e-3f) {
                 const float tv = dot3(tangent, view);
                 const Dual ds = dual_scatter(sqrtf(fmaxf(1.0f - tv * tv, 1e-6f)), sigma_a, shape);
-                const Geometry gm = light_geometry(tangent, view, ld3(L.direction));
+                const Geometry gm = light_geometry(t_n, v_n, ld3(L.direction));
                 color = vmul(spread_term(shape, ds, gm.theta_h, depth, dom_direct), ld3(L.color));
             }
         }
@@ -882,6 +929,29 @@ EnvArgs env_args(const hg_ctx* ctx) {
     for (int i = 0; i < 4; ++i) e.rot[i] = ctx->env_rot[i];
     e.intensity = ctx->env_intensity;
     if (!e.diff) e.spec = nullptr;
+    return e;
+}
+
+cudaError_t ensure_shade_setup(int device) {
+    static std::mutex mutex;
+    static bool ready[64] = {};
+    std::lock_guard<std::mutex> lock(mutex);
+    if (device < 0 || device >= 64) return cudaErrorInvalidDevice;
+    if (ready[device]) return cudaSuccess;
+    ScatterAngle t[2 * kScatterSteps];
+    const double pi = 3.14159265358979323846;
+    for (int half = 0; half < 2; ++half)
+        for (int i = 0; i < kScatterSteps; ++i) {
+            const double u = (i + 0.5) / kScatterSteps;
+            const double c = std::cos((half + u) * 0.5 * pi);
+            ScatterAngle& g = t[half * kScatterSteps + i];
+            g.cos_phi = (float)c;
+            g.cos_half_phi = (float)std::sqrt(std::min(std::max(0.5 + 0.5 * c, 0.0), 1.0));
+            g.k_tt = (float)std::exp(-3.65 * c - 3.98);
+            g.k_trt = (float)std::exp(17.0 * c - 16.78);
+        }
+    cudaError_t e = cudaMemcpyToSymbol(c_scatter, t, sizeof(t));
+    if (e == cudaSuccess) ready[device] = true;
     return e;
 }
 
