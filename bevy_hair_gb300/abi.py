@@ -216,6 +216,7 @@ _SIGNATURES = {
     "hg_groom_params": (_I32, [_VP, _VP, _VP, _U32, _U32, _U32, _VP, _VP]),
     "hg_copy_out_async": (_I32, [_VP, _I32, _VP, _SZ]),
     "hg_copy_wait": (_I32, [_VP]),
+    "hg_batch_copy_out_async": (_I32, [_VP, _U32, _I32, _VP, _SZ]),
     "hg_hair_visibility": (_I32, [_VP, _VP, _VP, _U32, _VP]),
     "hg_mlp_create": (_I32, [_VP, C.POINTER(_VP)]),
     "hg_mlp_destroy": (None, [_VP]),

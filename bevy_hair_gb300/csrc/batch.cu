@@ -52,9 +52,13 @@ struct hg_batch {
     uint32_t raster_per_sm_max = 1, gen_per_sm = 1;
     hg_batch_tuning tuning{4u, 0u, 32u, 8u, 0u, 0.0f};
     // graph
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
+    // The frame is two graphs: the passes up to shading, then filter + colour
+    // clear + composite, so a wait for the previous frame's asynchronous
+    // readback of the colour/depth arenas can sit between them.
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
     bool graph_valid = false;
+    bool pending_reads = false;  // an hg_batch_copy_out_async not yet waited for by a frame
     uint32_t g_lights = 0, g_ortho = 0;
     float g_exposure = 0.0f;
     cudaEvent_t done = nullptr;
@@ -105,8 +109,11 @@ TabOffsets tab_offsets(uint32_t n, uint32_t n_views) {
 }
 
 void free_batch(hg_batch* b) {
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->ctx && b->ctx->copy_stream) cudaStreamSynchronize(b->ctx->copy_stream);
+    for (int k = 0; k < 2; ++k) {
+        if (b->exec[k]) cudaGraphExecDestroy(b->exec[k]);
+        if (b->graph[k]) cudaGraphDestroy(b->graph[k]);
+    }
     free_dev(b->center);
     free_dev(b->cons);
     free_dev(b->beta);
@@ -226,8 +233,11 @@ void build_tables(hg_batch* b) {
 }
 
 // Uploads and the batched passes, on ctx->stream (captured or direct).
-cudaError_t enqueue_frame(hg_batch* b) {
+// Part 0 of a frame: table uploads, setup, raster, shade.  Part 1: filter,
+// colour clear, composite (the only writers of the colour/depth arenas).
+cudaError_t enqueue_part(hg_batch* b, int part) {
     hg_ctx* ctx = b->ctx;
+    if (part == 1) return hg::launch_batch_filter_composite(ctx, b->dev);
     const uint32_t n_views = b->n + b->n_dom;
     cudaError_t e = cudaMemcpyAsync(b->d_views, b->h_views, sizeof(hg::BatchView) * n_views, cudaMemcpyHostToDevice,
                                     ctx->stream);
@@ -240,33 +250,58 @@ cudaError_t enqueue_frame(hg_batch* b) {
     if (e == cudaSuccess) e = hg::launch_batch_setup(ctx, b->dev);
     if (e == cudaSuccess) e = hg::launch_batch_raster(ctx, b->dev);
     if (e == cudaSuccess) e = hg::launch_batch_shade(ctx, b->dev);
-    if (e == cudaSuccess) e = hg::launch_batch_filter_composite(ctx, b->dev);
+    return e;
+}
+
+// Orders part 1 after any pending asynchronous readback of the arenas.
+cudaError_t guard_readback(hg_batch* b) {
+    if (!b->pending_reads) return cudaSuccess;
+    cudaError_t e = cudaStreamWaitEvent(b->ctx->stream, b->ctx->ev_copy_done, 0);
+    if (e == cudaSuccess) b->pending_reads = false;
+    return e;
+}
+
+cudaError_t enqueue_frame(hg_batch* b) {
+    cudaError_t e = enqueue_part(b, 0);
+    if (e == cudaSuccess) e = guard_readback(b);
+    if (e == cudaSuccess) e = enqueue_part(b, 1);
     return e;
 }
 
 hg_status capture(hg_batch* b) {
     hg_ctx* ctx = b->ctx;
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    if (b->graph) cudaGraphDestroy(b->graph);
-    b->exec = nullptr;
-    b->graph = nullptr;
     b->graph_valid = false;
-    BATCH_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    cudaError_t e = enqueue_frame(b);
-    cudaGraph_t g = nullptr;
-    cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
-    if (e != cudaSuccess) {
-        if (g) cudaGraphDestroy(g);
-        return cuda_fail(ctx, e, "capturing the batched frame");
+    for (int k = 0; k < 2; ++k) {
+        if (b->exec[k]) cudaGraphExecDestroy(b->exec[k]);
+        if (b->graph[k]) cudaGraphDestroy(b->graph[k]);
+        b->exec[k] = nullptr;
+        b->graph[k] = nullptr;
     }
-    if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "ending the capture");
-    b->graph = g;
-    BATCH_CUDA(ctx, cudaGraphInstantiate(&b->exec, g, 0));
+    for (int k = 0; k < 2; ++k) {
+        BATCH_CUDA(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        cudaError_t e = enqueue_part(b, k);
+        cudaGraph_t g = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(ctx->stream, &g);
+        if (e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_fail(ctx, e, "capturing the batched frame");
+        }
+        if (e2 != cudaSuccess) return cuda_fail(ctx, e2, "ending the capture");
+        b->graph[k] = g;
+        BATCH_CUDA(ctx, cudaGraphInstantiate(&b->exec[k], g, 0));
+    }
     b->graph_valid = true;
     b->g_lights = b->dev.n_lights;
     b->g_ortho = b->dev.ortho;
     b->g_exposure = b->dev.exposure;
     return HG_OK;
+}
+
+cudaError_t launch_graphs(hg_batch* b) {
+    cudaError_t e = cudaGraphLaunch(b->exec[0], b->ctx->stream);
+    if (e == cudaSuccess) e = guard_readback(b);
+    if (e == cudaSuccess) e = cudaGraphLaunch(b->exec[1], b->ctx->stream);
+    return e;
 }
 
 // Lights sorted by kind into the pinned staging copy (what hg_shade does).
@@ -352,9 +387,9 @@ float time_graph(hg_batch* b, int warm, int reps, cudaError_t* err) {
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     *err = cudaEventCreate(&e0);
     if (*err == cudaSuccess) *err = cudaEventCreate(&e1);
-    for (int i = 0; i < warm && *err == cudaSuccess; ++i) *err = cudaGraphLaunch(b->exec, ctx->stream);
+    for (int i = 0; i < warm && *err == cudaSuccess; ++i) *err = launch_graphs(b);
     if (*err == cudaSuccess) *err = cudaEventRecord(e0, ctx->stream);
-    for (int i = 0; i < reps && *err == cudaSuccess; ++i) *err = cudaGraphLaunch(b->exec, ctx->stream);
+    for (int i = 0; i < reps && *err == cudaSuccess; ++i) *err = launch_graphs(b);
     if (*err == cudaSuccess) *err = cudaEventRecord(e1, ctx->stream);
     if (*err == cudaSuccess) *err = cudaEventSynchronize(e1);
     float ms = 0.0f;
@@ -512,6 +547,7 @@ hg_status hg_batch_frame(hg_batch* b, const hg_shade_desc* shade, hg_batch_mode 
     cudaSetDevice(ctx->device);
     if (mode == HG_BATCH_SEPARATE) {
         if (shade->shade_model != 0u) return fail(ctx, HG_INVALID_ARG, "batched frames shade with model 0");
+        BATCH_CUDA(ctx, guard_readback(b));
         hg_status s = run_separate(b, shade);
         if (s == HG_OK) BATCH_CUDA(ctx, cudaEventRecord(b->done, ctx->stream));
         return s;
@@ -527,7 +563,7 @@ hg_status hg_batch_frame(hg_batch* b, const hg_shade_desc* shade, hg_batch_mode 
             b->g_exposure != b->dev.exposure) {
             if ((s = capture(b)) != HG_OK) return s;
         }
-        BATCH_CUDA(ctx, cudaGraphLaunch(b->exec, ctx->stream));
+        BATCH_CUDA(ctx, launch_graphs(b));
     }
     BATCH_CUDA(ctx, cudaEventRecord(b->done, ctx->stream));
     return HG_OK;
@@ -538,10 +574,10 @@ hg_status hg_batch_launches(hg_batch* b, hg_batch_mode mode, uint32_t* launches)
     if (!ready(b)) return fail(b->ctx, HG_NOT_READY, "set every item's params first");
     if (mode == HG_BATCH_SEPARATE) {
         // hg_groom_frame: clear, lod, scan (2 kernels), [generate, clear_dom, lod, scan (2), raster x2],
-        // clear colour, raster, shade, [filter], composite
+        // clear colour, camera raster (2 stages + tile depths), shade, [filter], composite
         uint32_t total = 0;
         for (uint32_t i = 0; i < b->n; ++i)
-            total += 1 + 1 + 2 + (b->dw[i] ? 7u : 0u) + 1 + 1 + 1 + (b->cam[i].flags[1] ? 1u : 0u) + 1;
+            total += 1 + 1 + 2 + (b->dw[i] ? 7u : 0u) + 1 + 3 + 1 + (b->cam[i].flags[1] ? 1u : 0u) + 1;
         *launches = total;
         return HG_OK;
     }
@@ -700,6 +736,23 @@ hg_status hg_batch_buffer(hg_batch* b, uint32_t item, hg_buffer_id which, void**
         case HG_BUF_DEPTH: *ptr = b->depth + po, *bytes = px * 4; break;
         default: return fail(b->ctx, HG_INVALID_ARG, "unknown buffer id");
     }
+    return HG_OK;
+}
+
+hg_status hg_batch_copy_out_async(hg_batch* b, uint32_t item, hg_buffer_id which, void* host, size_t bytes) {
+    if (!b || !host) return HG_INVALID_ARG;
+    void* p = nullptr;
+    size_t n = 0;
+    hg_status s = hg_batch_buffer(b, item, which, &p, &n);
+    if (s != HG_OK) return s;
+    if (bytes != n) return fail(b->ctx, HG_INVALID_ARG, "size differs from the item's buffer");
+    if (!n) return HG_OK;
+    hg_ctx* ctx = b->ctx;
+    BATCH_CUDA(ctx, cudaEventRecord(ctx->ev_copy_src, ctx->stream));
+    BATCH_CUDA(ctx, cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_copy_src, 0));
+    BATCH_CUDA(ctx, cudaMemcpyAsync(host, p, n, cudaMemcpyDeviceToHost, ctx->copy_stream));
+    BATCH_CUDA(ctx, cudaEventRecord(ctx->ev_copy_done, ctx->copy_stream));
+    b->pending_reads = true;
     return HG_OK;
 }
 

@@ -484,6 +484,11 @@ hg_status hg_batch_get_tuning(hg_batch* batch, hg_batch_tuning* tuning);
 hg_status hg_batch_buffer(hg_batch* batch, uint32_t item, hg_buffer_id which, void** ptr, size_t* bytes);
 /* Copy an item's target to host memory (bytes must equal its size); synchronous. */
 hg_status hg_batch_copy_out(hg_batch* batch, uint32_t item, hg_buffer_id which, void* host, size_t bytes);
+/* The same copy on the context's copy stream, returning at once (see
+ * hg_copy_out_async; hg_copy_wait waits for it).  The next batched frame runs
+ * its passes up to shading at once and waits for the copies only before it
+ * writes the colour and depth targets. */
+hg_status hg_batch_copy_out_async(hg_batch* batch, uint32_t item, hg_buffer_id which, void* host, size_t bytes);
 
 /* ---------------------------------------------------------------- learned shading surrogate */
 

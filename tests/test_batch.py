@@ -81,7 +81,7 @@ def test_batched_graph_frame_matches_per_groom_frames(renderer, batch_scene):
     for k, g in enumerate(graph):
         assert (g[abi.BUF_CENTER] != np.uint64(0xFFFFFFFFFFFFFFFF)).any(), k
     assert b.launches(abi.BATCH_GRAPH) <= 14
-    assert b.launches(abi.BATCH_SEPARATE) == 16 * len(grooms)
+    assert b.launches(abi.BATCH_SEPARATE) == 18 * len(grooms)  # hg_groom_frame per item (camera raster: 3)
     _close(b, grooms)
 
 
@@ -120,6 +120,42 @@ def test_graph_replays_new_uniforms(renderer, batch_scene):
     b.frame(lights, abi.BATCH_SEPARATE)
     renderer.synchronize()
     _compare(graph, _read_all(b, len(grooms)))
+    _close(b, grooms)
+
+
+@pytest.mark.parametrize("mode", [abi.BATCH_GRAPH, abi.BATCH_LAUNCHES, abi.BATCH_SEPARATE])
+def test_async_readback_lands_before_the_next_frame_composites(renderer, batch_scene, mode):
+    """hg_batch_copy_out_async: every item's colour and depth copied on the
+    copy stream while the next frame (moved cameras) is already enqueued; that
+    frame waits for the copies before it writes the colour and depth targets."""
+    torch = pytest.importorskip("torch")
+    bs = batch_scene
+    b, grooms, params = _make(renderer, bs)
+    lights = bs.light_array()
+    b.frame(lights, mode)
+    renderer.synchronize()
+    want = [(b.read(k, abi.BUF_COLOR).copy(), b.read(k, abi.BUF_DEPTH).copy()) for k in range(len(grooms))]
+    b.frame(lights, mode)
+    hosts = []
+    for k, (c, d) in enumerate(want):
+        hc = torch.empty(c.size, dtype=torch.float32, pin_memory=True)
+        hd = torch.empty(d.size, dtype=torch.float32, pin_memory=True)
+        assert renderer.lib.hg_batch_copy_out_async(b.handle, k, abi.BUF_COLOR, hc.data_ptr(), c.nbytes) == 0
+        assert renderer.lib.hg_batch_copy_out_async(b.handle, k, abi.BUF_DEPTH, hd.data_ptr(), d.nbytes) == 0
+        hosts.append((hc, hd))
+    for k, s in enumerate(bs.scenes):
+        view = configs._camera(s.view.width, s.view.height, 700.0 + 15.0 * k, azimuth=1.0 + 0.3 * k)
+        moved = configs.Scene(s.name, s.mesh, s.groom, view, s.dom_size, s.lights, s.directionals)
+        b.set_params(k, *moved.params())
+    b.frame(lights, mode)
+    renderer.copy_wait()
+    assert renderer.synchronize() == 0
+    changed = 0
+    for k, ((c, d), (hc, hd)) in enumerate(zip(want, hosts)):
+        np.testing.assert_array_equal(hc.numpy(), c, err_msg=f"item {k} colour")
+        np.testing.assert_array_equal(hd.numpy(), d, err_msg=f"item {k} depth")
+        changed += int(np.abs(b.read(k, abi.BUF_COLOR) - c).max() > 1e-3)
+    assert changed >= len(grooms) // 2  # the moved frame did overwrite the targets
     _close(b, grooms)
 
 
