@@ -605,8 +605,20 @@ def run_ours(args, rank, world, local):
             "t_bound_ms": round(t_bound_ms, 4) if t_bound_ms else None,
             "frac": round(t_bound_ms / acc["raster_camera"], 4) if t_bound_ms else None,
             "probe": {k: round(v / 1e9, 2) for k, v in apeak.items()}, "probe_unit": "G ops/s"}
-    elif cpu:
+        # The DOM passes: one u32 atomic per sample (min, then add) at scattered
+        # texels, against the measured rate of random u32 reductions.
+        dom_rate = apeak.get("u32_add_random")
+        for name, key, field in (("raster_dom_depth", "dom_depth", "dom_min"),
+                                 ("raster_dom_layers", "dom_layers", "dom_add")):
+            cd = cpu.get("counts_dom", {}).get(key)
+            if cd and dom_rate and acc.get(name):
+                t_b = cd[field] / dom_rate * 1e3
+                roofline["atomics"].setdefault("dom_passes", {})[name] = {
+                    "algorithmic_ops": int(cd[field]), "peak_source": "measured (libhairprobe: u32 atomicAdd, random)",
+                    "t_bound_ms": round(t_b, 4), "frac": round(t_b / acc[name], 4)}
+    if cpu:
         cpu.pop("counts_camera", None)
+        cpu.pop("counts_dom", None)
     g.close()
     r.close()
     dist.close()
@@ -661,7 +673,8 @@ def cpu_baseline(args, sample: bool) -> dict:
     dt = time.perf_counter() - t
     segs = r["camera_segments"]
     return {"value": r["gseg_per_s"], "unit": "Gseg/s", "cores": threads, "kind": "port",
-            "counts_camera": r["counts_camera"], "per_pass_ms": r["per_pass_ms"], "ms_per_frame": r["frame_ms"],
+            "counts_camera": r["counts_camera"], "counts_dom": r["counts_dom"], "per_pass_ms": r["per_pass_ms"],
+            "ms_per_frame": r["frame_ms"],
             "sample": (f"config{args.config} at scale {scale}: {sc.mesh.strand_count()} strands, "
                        f"{sc.view.width}x{sc.view.height}, DOM {sc.dom_size[0]}^2, {segs} camera segments; "
                        f"1 warm-up + median of 3 frames, {dt:.1f} s in all"),

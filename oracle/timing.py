@@ -67,4 +67,5 @@ def per_pass(mesh, camera, dom_params, lights, env=None, runs: int = 5, threads:
     segs = int(counts["camera"]["segments"])
     return {"per_pass_ms": med, "frame_ms": round(frame * 1e3, 3), "camera_segments": segs,
             "gseg_per_s": round(segs / frame / 1e9, 6), "threads": threads, "runs": runs,
-            "counts_camera": counts["camera"]}
+            "counts_camera": counts["camera"], "counts_dom": {k: counts[k] for k in ("dom_depth", "dom_layers")
+                                                               if k in counts}}
