@@ -359,12 +359,12 @@ constexpr int kRasterThreads = kRasterWarps * 32;
 template <int MODE>
 constexpr int raster_min_blocks() { return MODE == 0 ? 6 : 7; }
 
-// Per-warp shared memory, 6.7 KB.  The layer samples are needed only while
-// control points are generated, so they share storage with the sample offsets.
+// Per-warp shared memory, 7 KB.  The layer samples are needed only while
+// control points are generated, so they share storage with the run list.
 struct alignas(16) StrandSmem {
     float4 cp[128];  // control point: model position, then world position + in_front flag
     float4 ct[128];  // camera: world tangent xyz + w (uvw.z)
-    float4 cs[128];  // screen xy, ao, DDA step count n of the segment starting here (int bits)
+    float4 cs[128];  // screen xy, ao; camera: RN(1/n) for the segment's DDA step count n
     union {
         struct {
             float4 lp[16];  // layer sample: position, ao
