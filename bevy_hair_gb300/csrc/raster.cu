@@ -355,7 +355,8 @@ constexpr int kRasterThreads = kRasterWarps * 32;
 // registers without a spill in it at 6 (24 warps); at 7 (72 registers) the
 // spilled values sit in the loop and reach L2 on every round (L1 is small
 // next to 7 x 28 KB of shared memory), which costs more than the extra warps
-// give.  The deep-opacity passes fit 71 registers and take 7.
+// give.  The deep-opacity passes fit 60 registers and take 7 (shared memory
+// allows no eighth).
 template <int MODE>
 constexpr int raster_min_blocks() { return MODE == 0 ? 6 : 7; }
 
