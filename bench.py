@@ -369,7 +369,7 @@ def batch_measure(r, stream, flush, steps: int, warmup: int, scale: float) -> di
 
     e2e_step()
     r.copy_wait()
-    n_e2e = max(3, steps // 4)
+    n_e2e = max(5, steps)
     t = time.perf_counter()
     for _ in range(n_e2e):
         e2e_step()

@@ -59,6 +59,11 @@ struct hg_batch {
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     bool graph_valid = false;
     bool pending_reads = false;  // an hg_batch_copy_out_async not yet waited for by a frame
+    // The pinned tables are rebuilt at frame time (set_params only marks them
+    // dirty) and uploaded ahead of the frame's kernels; `uploaded` follows the
+    // last upload, so the host may rewrite them while that frame still runs.
+    bool tables_dirty = true;
+    cudaEvent_t uploaded = nullptr;
     uint32_t g_lights = 0, g_ortho = 0;
     float g_exposure = 0.0f;
     cudaEvent_t done = nullptr;
@@ -135,6 +140,7 @@ void free_batch(hg_batch* b) {
     if (b->h_tab) cudaFreeHost(b->h_tab);
     if (b->h_lights) cudaFreeHost(b->h_lights);
     if (b->done) cudaEventDestroy(b->done);
+    if (b->uploaded) cudaEventDestroy(b->uploaded);
     delete b;
 }
 
@@ -233,11 +239,10 @@ void build_tables(hg_batch* b) {
 }
 
 // Uploads and the batched passes, on ctx->stream (captured or direct).
-// Part 0 of a frame: table uploads, setup, raster, shade.  Part 1: filter,
-// colour clear, composite (the only writers of the colour/depth arenas).
-cudaError_t enqueue_part(hg_batch* b, int part) {
+// The view table, prefix tables and light list, pinned host -> device, on the
+// work stream ahead of the frame's kernels.
+cudaError_t upload_tables(hg_batch* b) {
     hg_ctx* ctx = b->ctx;
-    if (part == 1) return hg::launch_batch_filter_composite(ctx, b->dev);
     const uint32_t n_views = b->n + b->n_dom;
     cudaError_t e = cudaMemcpyAsync(b->d_views, b->h_views, sizeof(hg::BatchView) * n_views, cudaMemcpyHostToDevice,
                                     ctx->stream);
@@ -247,10 +252,32 @@ cudaError_t enqueue_part(hg_batch* b, int part) {
     if (e == cudaSuccess && b->dev.n_lights)
         e = cudaMemcpyAsync(b->d_lights, b->h_lights, sizeof(hg_light) * b->dev.n_lights, cudaMemcpyHostToDevice,
                             ctx->stream);
-    if (e == cudaSuccess) e = hg::launch_batch_setup(ctx, b->dev);
+    if (e == cudaSuccess) e = cudaEventRecord(b->uploaded, ctx->stream);
+    return e;
+}
+
+// Part 0 of a frame: setup, raster, shade.  Part 1: filter, colour clear,
+// composite (the only writers of the colour/depth arenas).
+cudaError_t enqueue_part(hg_batch* b, int part) {
+    hg_ctx* ctx = b->ctx;
+    if (part == 1) return hg::launch_batch_filter_composite(ctx, b->dev);
+    cudaError_t e = hg::launch_batch_setup(ctx, b->dev);
     if (e == cudaSuccess) e = hg::launch_batch_raster(ctx, b->dev);
     if (e == cudaSuccess) e = hg::launch_batch_shade(ctx, b->dev);
     return e;
+}
+
+// Rebuilds the pinned tables after set_params; the caller has waited for the
+// last upload.  The graphs hold the launch sizes, so a change of them (bundle
+// totals, filter flag, depth convention) forces a new capture.
+void refresh_tables(hg_batch* b) {
+    if (!b->tables_dirty) return;
+    const hg::BatchDev before = b->dev;
+    build_tables(b);
+    const hg::BatchDev& d = b->dev;
+    if (d.total_bundles != before.total_bundles || d.filter != before.filter || d.depth_clear != before.depth_clear)
+        b->graph_valid = false;
+    b->tables_dirty = false;
 }
 
 // Orders part 1 after any pending asynchronous readback of the arenas.
@@ -262,7 +289,8 @@ cudaError_t guard_readback(hg_batch* b) {
 }
 
 cudaError_t enqueue_frame(hg_batch* b) {
-    cudaError_t e = enqueue_part(b, 0);
+    cudaError_t e = upload_tables(b);
+    if (e == cudaSuccess) e = enqueue_part(b, 0);
     if (e == cudaSuccess) e = guard_readback(b);
     if (e == cudaSuccess) e = enqueue_part(b, 1);
     return e;
@@ -480,6 +508,7 @@ hg_status hg_batch_create(hg_ctx* ctx, const hg_batch_item* items, uint32_t coun
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_tab, sizeof(uint32_t) * to.total);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_lights, sizeof(hg_light) * HG_MAX_LIGHTS);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->uploaded, cudaEventDisableTiming);
     // every groom's strand cache (the batched camera and DOM rasters read it)
     for (uint32_t i = 0; i < count && e == cudaSuccess; ++i) {
         hg_groom* g = items[i].groom;
@@ -524,19 +553,11 @@ hg_status hg_batch_set_params(hg_batch* b, uint32_t item, const hg_hair_params* 
         if (j != item && b->have[j] &&
             (b->cam[j].flags[1] != c.flags[1] || b->cam[j].pass_mode[2] != c.pass_mode[2]))
             return fail(ctx, HG_INVALID_ARG, "items must agree on the filter flag and the depth convention");
-    BATCH_CUDA(ctx, cudaEventSynchronize(b->done));
+    // host copies only: the pinned tables are rebuilt at the next frame
     b->cam[item] = c;
     if (has_dom) b->dom[item] = *dom;
     b->have[item] = 1;
-    if (ready(b)) {
-        // The graph holds the launch sizes; the tables it uploads are read at replay.
-        const hg::BatchDev before = b->dev;
-        build_tables(b);
-        const hg::BatchDev& d = b->dev;
-        if (d.total_bundles != before.total_bundles || d.filter != before.filter ||
-            d.depth_clear != before.depth_clear)
-            b->graph_valid = false;
-    }
+    b->tables_dirty = true;
     return HG_OK;
 }
 
@@ -553,7 +574,10 @@ hg_status hg_batch_frame(hg_batch* b, const hg_shade_desc* shade, hg_batch_mode 
         return s;
     }
     if (mode != HG_BATCH_GRAPH && mode != HG_BATCH_LAUNCHES) return fail(ctx, HG_INVALID_ARG, "unknown batch mode");
-    BATCH_CUDA(ctx, cudaEventSynchronize(b->done));
+    // The previous frame's upload has read the pinned tables; its kernels may
+    // still run while this frame's tables are written.
+    BATCH_CUDA(ctx, cudaEventSynchronize(b->uploaded));
+    refresh_tables(b);
     hg_status s = stage_lights(b, shade);
     if (s != HG_OK) return s;
     if (mode == HG_BATCH_LAUNCHES) {
@@ -563,6 +587,7 @@ hg_status hg_batch_frame(hg_batch* b, const hg_shade_desc* shade, hg_batch_mode 
             b->g_exposure != b->dev.exposure) {
             if ((s = capture(b)) != HG_OK) return s;
         }
+        BATCH_CUDA(ctx, upload_tables(b));
         BATCH_CUDA(ctx, launch_graphs(b));
     }
     BATCH_CUDA(ctx, cudaEventRecord(b->done, ctx->stream));
@@ -572,6 +597,8 @@ hg_status hg_batch_frame(hg_batch* b, const hg_shade_desc* shade, hg_batch_mode 
 hg_status hg_batch_launches(hg_batch* b, hg_batch_mode mode, uint32_t* launches) {
     if (!b || !launches) return HG_INVALID_ARG;
     if (!ready(b)) return fail(b->ctx, HG_NOT_READY, "set every item's params first");
+    BATCH_CUDA(b->ctx, cudaEventSynchronize(b->uploaded));
+    refresh_tables(b);
     if (mode == HG_BATCH_SEPARATE) {
         // hg_groom_frame: clear, lod, scan (2 kernels), [generate, clear_dom, lod, scan (2), raster x2],
         // clear colour, camera raster (2 stages + tile depths), shade, [filter], composite
@@ -601,6 +628,7 @@ hg_status hg_batch_profile(hg_batch* b, const hg_shade_desc* shade, float* ms) {
     if (!ready(b)) return fail(ctx, HG_NOT_READY, "set every item's params before a frame");
     cudaSetDevice(ctx->device);
     BATCH_CUDA(ctx, cudaEventSynchronize(b->done));
+    refresh_tables(b);
     hg_status s = stage_lights(b, shade);
     if (s != HG_OK) return s;
     cudaEvent_t ev[5] = {};
@@ -641,7 +669,10 @@ hg_status hg_batch_set_tuning(hg_batch* b, const hg_batch_tuning* t) {
     BATCH_CUDA(b->ctx, cudaEventSynchronize(b->done));
     b->tuning = *t;
     b->graph_valid = false;
-    if (ready(b)) build_tables(b);
+    if (ready(b)) {
+        build_tables(b);
+        b->tables_dirty = false;
+    }
     return HG_OK;
 }
 
@@ -669,9 +700,11 @@ hg_status hg_batch_tune(hg_batch* b, const hg_shade_desc* shade, hg_batch_tuning
     auto trial = [&](hg_batch_tuning t) -> hg_status {
         b->tuning = t;
         build_tables(b);
+        b->tables_dirty = false;
         hg_status st = capture(b);
         if (st != HG_OK) return st;
-        cudaError_t e = cudaSuccess;
+        cudaError_t e = upload_tables(b);  // time_graph ends with a stream sync before the next rebuild
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "uploading a tuning candidate's tables");
         const float ms = time_graph(b, 2, 5, &e);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "timing a tuning candidate");
         t.ms = ms;
@@ -711,6 +744,7 @@ hg_status hg_batch_tune(hg_batch* b, const hg_shade_desc* shade, hg_batch_tuning
     }
     b->tuning = best;
     build_tables(b);
+    b->tables_dirty = false;
     b->graph_valid = false;
     BATCH_CUDA(ctx, cudaEventRecord(b->done, ctx->stream));
     return HG_OK;
