@@ -220,6 +220,7 @@ def tensor_peak() -> tuple[float, str]:
 
 
 MLP_FLOP_PER_EVAL = 27392  # 2 * (10*64 + 3*64*64 + 64*12)
+COMPACT_FLOP_PER_EVAL = 3456  # 2 * (10*32 + 32*32 + 32*12)
 
 
 def surrogate_section(r, cam, lights, flush, stream, reps: int, karis_ms: float, hair_px: int) -> dict | None:
@@ -258,6 +259,27 @@ def surrogate_section(r, cam, lights, flush, stream, reps: int, karis_ms: float,
     evals = hair_px * len(lights)
     tflops = evals * MLP_FLOP_PER_EVAL / (ms * 1e-3) / 1e12
     peak, src = tensor_peak()
+    compact = None
+    try:
+        cparams = S.load_params(abi.MLP_ARCH_COMPACT)
+    except (OSError, ValueError):
+        cparams = None
+    if cparams is not None:
+        c = S.Surrogate(r, cparams, abi.MLP_ARCH_COMPACT)
+        r.bind_surrogate(c)
+        ms_c = timed(abi.SHADE_SURROGATE_COMPACT)
+        ev_c = S.evaluate(r, c, n=1 << 16)
+        r.bind_surrogate(None)
+        c.close()
+        compact = {
+            "network": "10 -> 32 -> 32 -> 12 (shade model 3, mma.sync m16n8k16, FP16 weights, FP32 accumulation)",
+            "shade_ms": round(ms_c, 4), "ratio_vs_karis": round(ms_c / karis_ms, 3),
+            "flop_per_eval": COMPACT_FLOP_PER_EVAL,
+            "achieved_tflops": round(evals * COMPACT_FLOP_PER_EVAL / (ms_c * 1e-3) / 1e12, 2),
+            "error": {"surrogate": round(ev_c["surrogate_bsdf"], 5), "karis": round(ev_c["karis_bsdf"], 5),
+                      "per_lobe": {k: round(v, 5) for k, v in ev_c.items() if k.startswith("surrogate_")
+                                   and not k.endswith("bsdf")}},
+        }
     return {
         "shade_ms": round(ms, 4), "karis_shade_ms": round(karis_ms, 4), "ratio_vs_karis": round(ms / karis_ms, 3),
         "kernel": "tcgen05 (shade model 1: 128-row MMAs, TMEM accumulators, compacted hair pixels)",
@@ -270,6 +292,7 @@ def surrogate_section(r, cam, lights, flush, stream, reps: int, karis_ms: float,
                   "surrogate": round(ev["surrogate_bsdf"], 5), "karis": round(ev["karis_bsdf"], 5),
                   "per_lobe": {k: round(v, 5) for k, v in ev.items() if k.startswith(("surrogate_", "karis_"))
                                and not k.endswith("bsdf")}},
+        "compact": compact,
     }
 
 

@@ -20,9 +20,11 @@ DOM_LAYERS = 16
 MAX_LIGHTS = 256
 SCAN_NOALLOC_MAX_BUNDLES = 65536
 MLP_PARAMS = 14608
+MLP_COMPACT_PARAMS = 2128
 MLP_INPUTS = 10
 MLP_OUTPUTS = 12
-SHADE_KARIS, SHADE_SURROGATE, SHADE_SURROGATE_MMA = 0, 1, 2
+MLP_ARCH_DEEP, MLP_ARCH_COMPACT = 0, 1
+SHADE_KARIS, SHADE_SURROGATE, SHADE_SURROGATE_MMA, SHADE_SURROGATE_COMPACT = 0, 1, 2, 3
 
 # --------------------------------------------------------------------- dtypes
 
@@ -219,6 +221,8 @@ _SIGNATURES = {
     "hg_batch_copy_out_async": (_I32, [_VP, _U32, _I32, _VP, _SZ]),
     "hg_hair_visibility": (_I32, [_VP, _VP, _VP, _U32, _VP]),
     "hg_mlp_create": (_I32, [_VP, C.POINTER(_VP)]),
+    "hg_mlp_create_arch": (_I32, [_VP, _U32, C.POINTER(_VP)]),
+    "hg_mlp_param_count": (_U32, [_VP]),
     "hg_mlp_destroy": (None, [_VP]),
     "hg_mlp_set_params": (_I32, [_VP, _VP, _U32]),
     "hg_mlp_get_params": (_I32, [_VP, _VP, _U32]),

@@ -547,9 +547,12 @@ hg_status hg_shade(hg_ctx* ctx, const hg_hair_params* p, const hg_shade_desc* d)
     if (!ctx || !p || !d) return HG_INVALID_ARG;
     if (d->light_count > HG_MAX_LIGHTS) return fail(ctx, HG_CAPACITY_EXCEEDED, "more than HG_MAX_LIGHTS lights");
     if (d->light_count && !d->lights) return fail(ctx, HG_INVALID_ARG, "null light array");
-    if (d->shade_model > 2u) return fail(ctx, HG_INVALID_ARG, "unknown shade model");
+    if (d->shade_model > 3u) return fail(ctx, HG_INVALID_ARG, "unknown shade model");
     if (d->shade_model != 0u && !ctx->surrogate)
-        return fail(ctx, HG_NOT_READY, "shade models 1 and 2 need a surrogate bound with hg_mlp_bind");
+        return fail(ctx, HG_NOT_READY, "shade models 1 to 3 need a surrogate bound with hg_mlp_bind");
+    if (d->shade_model != 0u &&
+        ctx->surrogate->arch != (d->shade_model == 3u ? HG_MLP_ARCH_COMPACT : HG_MLP_ARCH_DEEP))
+        return fail(ctx, HG_INVALID_ARG, "shade models 1 and 2 take the 4 x 64 surrogate, model 3 the compact one");
     hg_status s = check_screen(ctx, p);
     if (s != HG_OK) return s;
     if (p->pass_mode[0] != 0u) return fail(ctx, HG_INVALID_ARG, "shade takes the camera params (pass_mode.x == 0)");

@@ -41,12 +41,14 @@ struct hg_groom {
 // state, FP16 forward and transposed copies, training scratch.
 struct hg_mlp {
     hg_ctx* ctx = nullptr;
-    float* params = nullptr;   // HG_MLP_PARAMS
+    uint32_t arch = 0;         // HG_MLP_ARCH_*
+    uint32_t n_params = 0;     // HG_MLP_PARAMS or HG_MLP_COMPACT_PARAMS
+    float* params = nullptr;   // n_params floats
     float* grad = nullptr;
     float* adam_m = nullptr;
     float* adam_v = nullptr;
-    void* w16 = nullptr;       // __half[HG_MLP_PARAMS], parameter layout
-    void* wt16 = nullptr;      // __half[13312], W2^T W3^T W4^T W5^T
+    void* w16 = nullptr;       // __half[n_params], parameter layout
+    void* wt16 = nullptr;      // __half[13312], W2^T W3^T W4^T W5^T (4 x 64 network only)
     float* loss = nullptr;     // device scalar
     void* scratch = nullptr;   // transposed activations and gradients, (16 + 4*64 + 4*64 + 16) x ld halves
     uint32_t ld_capacity = 0;

@@ -11,6 +11,7 @@
 #include "hg_device.cuh"
 #include "hg_internal.h"
 #include "hg_mlp.cuh"
+#include "hg_mlp_small.cuh"
 #include "hg_mlp_tc.cuh"
 
 namespace hg {
@@ -912,6 +913,269 @@ __global__ void __launch_bounds__(mlp::tc::kThreads, 1)
     mlp::tc::teardown(smem_tc, c, failed);
 }
 
+// ---------------------------------------------------------------- compact surrogate
+// Shade model 3: the compact 2 x 32 network (hg_mlp_small.cuh) on mma.sync.
+// The hair-pixel list of shade model 1 fills every lane: a warp shades 32
+// listed pixels and evaluates the network for all of them once per light.
+//
+// Layout choices that keep the light loop short:
+// * Lane L = 4g + t puts its pixel in network row g + 8t.  That is the row
+//   whose outputs a reduce-scatter over the lane's quad leaves in lane L, so
+//   the outputs are decoded and summed in the C-fragment layout without a
+//   trip through shared memory.
+// * The output layer's rows are permuted in shared memory so that lane t's
+//   C-fragment columns 2t, 2t+1 and 8+2t are the red, green and blue of lobe
+//   t (R, TT, TRT, B) and column 9+2t is padding: every lane decodes 12
+//   values and weighs them with one factor.
+// * Each pixel's inputs sit in shared row L (row stride 13 words: stores
+//   and the permuted fragment loads are both free of bank conflicts); the
+//   per-pixel inputs (sin theta_o, absorption, roughnesses, IOR) are written
+//   once per pixel, per light only sin theta_i, cos phi and sin phi.
+// * Biases are stored as the accumulator quads {b(2t), b(2t+1), b(2t),
+//   b(2t+1)} and enter the first MMA of a layer as its C operand.
+constexpr int kCompactWarps = 8;
+constexpr int kXPad = 26;  // halves per input row
+
+struct CompactSmem {
+    __half w1[mlps::kHid][mlps::kPadIn];
+    __half w2[mlps::kHid][mlps::kPadHid];
+    __half w3[mlps::kOut][mlps::kPadHid];  // rows permuted, see above
+    float4 bq1[4][4], bq2[4][4], bq3[2][4];  // [n-tile][t]
+    __half x[kCompactWarps][32][kXPad];
+    hg_light lights[HG_MAX_LIGHTS];
+};
+
+// Output row of the network in physical column pc of the permuted layer.
+__device__ __forceinline__ int compact_out_row(int pc) {
+    if (pc < 8) return 3 * (pc >> 1) + (pc & 1);
+    const int t = (pc - 8) >> 1;
+    return (pc & 1) ? 12 + t : 3 * t + 2;  // 12..15: zero padding rows
+}
+
+__device__ __forceinline__ void st_h2(__half* p, float lo, float hi) {
+    *reinterpret_cast<uint32_t*>(p) = mlp::pack_h2(lo, hi);
+}
+
+// D = A * B + C with a separate C (the bias quad).
+__device__ __forceinline__ void mma_c(float d[4], const uint32_t a[4], uint32_t b0, uint32_t b1, const float4& c) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%10,%11,%12,%13};\n"
+        : "=f"(d[0]), "=f"(d[1]), "=f"(d[2]), "=f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1), "f"(c.x), "f"(c.y), "f"(c.z), "f"(c.w));
+}
+
+// One layer: acc[mt][nt] = bias + A[mt] * W^T, N = 8 NT outputs, K = 16 KT inputs.
+template <int NT, int KT, int PAD>
+__device__ __forceinline__ void compact_layer(float acc[2][NT][4], const uint32_t a[2][KT][4],
+                                              const __half (*w)[PAD], const float4 (*bq)[4], int lane) {
+    const int t = lane & 3, mat = lane >> 3, r = lane & 7;
+#pragma unroll
+    for (int kt = 0; kt < KT; ++kt) {
+#pragma unroll
+        for (int nt = 0; nt < NT; nt += 2) {
+            uint32_t b[4];
+            mlp::ldsm_x4(b, &w[(nt + (mat >> 1)) * 8 + r][kt * 16 + (mat & 1) * 8]);
+            if (kt == 0) {
+                const float4 c0 = bq[nt][t], c1 = bq[nt + 1][t];
+                mma_c(acc[0][nt], a[0][0], b[0], b[1], c0);
+                mma_c(acc[1][nt], a[1][0], b[0], b[1], c0);
+                mma_c(acc[0][nt + 1], a[0][0], b[2], b[3], c1);
+                mma_c(acc[1][nt + 1], a[1][0], b[2], b[3], c1);
+            } else {
+                mlp::mma(acc[0][nt], a[0][kt], b[0], b[1]);
+                mlp::mma(acc[1][nt], a[1][kt], b[0], b[1]);
+                mlp::mma(acc[0][nt + 1], a[0][kt], b[2], b[3]);
+                mlp::mma(acc[1][nt + 1], a[1][kt], b[2], b[3]);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ float4 bias_quad(const float* b, int nt, int t) {
+    const float lo = b[nt * 8 + 2 * t], hi = b[nt * 8 + 2 * t + 1];
+    return make_float4(lo, hi, lo, hi);
+}
+
+__global__ void __launch_bounds__(kCompactWarps * 32, 2)
+    shade_compact_kernel(const ShadeArgs a, const __half* __restrict__ w16, const float* __restrict__ mparams,
+                         const EnvArgs env, const uint32_t* __restrict__ list, const uint32_t* __restrict__ count) {
+    __shared__ __align__(16) CompactSmem sm;
+    {
+        const int tid = threadIdx.x, nth = blockDim.x;
+        mlp::copy_rows<mlps::kPadIn>(sm.w1, w16 + mlps::kW1, mlps::kHid, mlps::kIn, tid, nth);
+        mlp::copy_rows<mlps::kPadHid>(sm.w2, w16 + mlps::kW2, mlps::kHid, mlps::kHid, tid, nth);
+        for (int i = tid; i < mlps::kOut * (mlps::kHid / 8); i += nth) {
+            const int pc = i / (mlps::kHid / 8), c = (i % (mlps::kHid / 8)) * 8;
+            *reinterpret_cast<uint4*>(&sm.w3[pc][c]) =
+                __ldg(reinterpret_cast<const uint4*>(w16 + mlps::kW3 + compact_out_row(pc) * mlps::kHid + c));
+        }
+        for (int i = tid; i < 16; i += nth) {
+            const int nt = i >> 2, tt = i & 3;
+            sm.bq1[nt][tt] = bias_quad(mparams + mlps::kB1, nt, tt);
+            sm.bq2[nt][tt] = bias_quad(mparams + mlps::kB2, nt, tt);
+            if (nt < 2) {
+                const float lo = mparams[mlps::kB3 + compact_out_row(nt * 8 + 2 * tt)];
+                const float hi = mparams[mlps::kB3 + compact_out_row(nt * 8 + 2 * tt + 1)];
+                sm.bq3[nt][tt] = make_float4(lo, hi, lo, hi);
+            }
+        }
+        const uint32_t words = a.n_lights * (uint32_t)(sizeof(hg_light) / 4);
+        for (uint32_t i = tid; i < words; i += nth)
+            reinterpret_cast<uint32_t*>(sm.lights)[i] = __ldg(reinterpret_cast<const uint32_t*>(a.lights) + i);
+    }
+    __syncthreads();
+    const hg_hair_params& p = a.p;
+    const uint32_t width = f2u(p.screen[0]);
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const int g = (int)(lane >> 2), t = (int)(lane & 3u);
+    __half(*xr)[kXPad] = sm.x[warp];
+    // lobe t's factor: the lobe scale, times the back-scattering density for B
+    const float lobe_w = t == 3 ? mlp::kScale * kDensityBack : mlp::kScale;
+    // The light that receives the deep-opacity depth (shade.wesl:486-503).
+    int dom_light = -1;
+    for (uint32_t i = 0; i < a.n_lights; ++i)
+        if (sm.lights[i].kind == HG_LIGHT_DIRECTIONAL && (sm.lights[i].flags & HG_LIGHT_CASTS_SHADOWS)) {
+            dom_light = (int)i;
+            break;
+        }
+    const uint32_t n = *count;
+    const uint32_t chunks = (n + 31u) >> 5;
+    for (uint32_t ch = blockIdx.x * kCompactWarps + warp; ch < chunks; ch += gridDim.x * kCompactWarps) {
+        const uint32_t idx = ch * 32u + lane;
+        const bool active = idx < n;
+        const uint32_t pix = active ? __ldg(&list[idx]) : 0u;
+        const uint32_t x = pix % width, y = pix / width;
+        const unsigned long long word = active ? __ldg(&a.center[pix]) : 0ull;
+        const uint32_t low = (uint32_t)word, high = (uint32_t)(word >> 32);
+        const float view_dist = dequantize_depth(high >> 8u, p.screen[2], p.screen[3]);
+        const f3 world = reconstruct_world(p, (int32_t)x, (int32_t)y, view_dist);
+        const f3 tangent = oct_decode(high & 0xffu, low >> 24u);
+        const float uvw_z = (float)((low >> 6u) & 0x3fu) / 63.0f;
+        const float roughness = fmaxf(p.appearance[0] * (0.65f + 0.7f * uvw_z), 0.04f);
+        const float ascale = 0.65f + 0.35f * uvw_z;
+        const f3 albedo = {p.albedo[0] * ascale, p.albedo[1] * ascale, p.albedo[2] * ascale};
+        f3 view;
+        if (a.ortho) {
+            view = safe_normalize(mk3(p.clip_from_world[2], p.clip_from_world[6], p.clip_from_world[10]));
+        } else {
+            view = safe_normalize(sub3(ld3(p.camera_pos), world));
+        }
+        const Shape shape = lobe_shape(roughness, p.appearance[1]);
+        const f3 sigma_a = absorption_from_color(albedo, roughness);
+        const f3 t_n = safe_normalize(tangent), v_n = safe_normalize(view);
+        const float sin_o = clampf(dot3(t_n, v_n), -1.0f, 1.0f);
+        const f3 t_o = sub3(v_n, mul3s(t_n, sin_o));
+        const float to2 = dot3(t_o, t_o);
+        // this pixel's row: the per-pixel inputs, columns 0, 2, 3 filled per light
+        {
+            const float raw[10] = {0.0f, sin_o, 1.0f, 0.0f, sigma_a.x, sigma_a.y, sigma_a.z, shape.beta.x,
+                                   clampf(roughness, 0.2f, 0.8f), kIor};
+            float xin[10];
+            mlp::normalise(raw, xin);
+            __syncwarp();
+#pragma unroll
+            for (int c = 0; c < 10; c += 2) st_h2(&xr[lane][c], xin[c], xin[c + 1]);
+#pragma unroll
+            for (int c = 10; c < mlps::kIn; c += 2) st_h2(&xr[lane][c], 0.0f, 0.0f);
+            __syncwarp();
+        }
+        // A-fragment registers of columns 8..15, the same for every light;
+        // network row g + 8k holds the pixel of lane 4g + k
+        uint32_t a_hi[2][2];
+#pragma unroll
+        for (int mt = 0; mt < 2; ++mt) {
+            a_hi[mt][0] = mlp::ld32(&xr[4 * g + 2 * mt][8 + 2 * t]);
+            a_hi[mt][1] = mlp::ld32(&xr[4 * g + 2 * mt + 1][8 + 2 * t]);
+        }
+        f3 color = spl(0.0f);
+        float dom_direct = 1.0f;
+        if (dom_light >= 0 && active) {
+            const hg_light& L = sm.lights[dom_light];
+            const float beta = (float)(__ldg(&a.beta[pix]) & 0xffu) / 255.0f;
+            const float depth = -logf(fmaxf(dom_visibility(p, a.dom, world, beta), 1e-6f));
+            dom_direct = expf(-depth);
+            if (depth > 1e-3f) {
+                const float tv = dot3(tangent, view);
+                const Dual ds = dual_scatter(sqrtf(fmaxf(1.0f - tv * tv, 1e-6f)), sigma_a, shape);
+                const Geometry gm = light_geometry(t_n, v_n, ld3(L.direction));
+                color = vmul(spread_term(shape, ds, gm.theta_h, depth, dom_direct), ld3(L.color));
+            }
+        }
+        for (uint32_t i = 0; i < a.n_lights; ++i) {
+            const hg_light& L = sm.lights[i];
+            f3 incident;
+            float weight = light_weight(L, world, incident);
+            if ((int)i == dom_light) weight = dom_direct;
+            const bool use = active && weight > 0.0f;
+            if (!__any_sync(0xffffffffu, use)) continue;
+            // sin theta_i and cos phi as light_geometry computes them
+            const f3 l = safe_normalize(incident);
+            const float sin_i = clampf(dot3(t_n, l), -1.0f, 1.0f);
+            const f3 t_i = sub3(l, mul3s(t_n, sin_i));
+            const float cos_phi = clampf(dot3(t_i, t_o) * rsqrtf(fmaxf(dot3(t_i, t_i) * to2, 1e-8f)), -1.0f, 1.0f);
+            __syncwarp();
+            st_h2(&xr[lane][0], sin_i, sin_o);
+            st_h2(&xr[lane][2], cos_phi, sqrtf(fmaxf(1.0f - cos_phi * cos_phi, 0.0f)));
+            __syncwarp();
+            uint32_t a0[2][1][4];
+#pragma unroll
+            for (int mt = 0; mt < 2; ++mt) {
+                a0[mt][0][0] = mlp::ld32(&xr[4 * g + 2 * mt][2 * t]);
+                a0[mt][0][1] = mlp::ld32(&xr[4 * g + 2 * mt + 1][2 * t]);
+                a0[mt][0][2] = a_hi[mt][0];
+                a0[mt][0][3] = a_hi[mt][1];
+            }
+            float acc[2][4][4];
+            uint32_t ah[2][2][4];
+            compact_layer<4, 1, mlps::kPadIn>(acc, a0, sm.w1, sm.bq1, (int)lane);
+            mlps::relu_to_a(acc, ah);
+            compact_layer<4, 2, mlps::kPadHid>(acc, ah, sm.w2, sm.bq2, (int)lane);
+            mlps::relu_to_a(acc, ah);
+            float out[2][2][4];
+            compact_layer<2, 2, mlps::kPadHid>(out, ah, sm.w3, sm.bq3, (int)lane);
+            // part[k]: lobe t's rgb in network row g + 8k (columns 2t, 2t+1, 8+2t)
+            float part[4][3];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                const int mt = k >> 1, h = k & 1;
+                const float y3[3] = {out[mt][0][2 * h], out[mt][0][2 * h + 1], out[mt][1][2 * h]};
+#pragma unroll
+                for (int c = 0; c < 3; ++c) part[k][c] = fmaf(lobe_w, __expf(fmaxf(y3[c], 0.0f)), -lobe_w);
+            }
+            // reduce-scatter over the quad: lane t keeps row slot t
+            const bool hi = (t >> 1) != 0, lo = (t & 1) != 0;
+            float kept[2][3];
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float mine = hi ? part[2 + j][c] : part[j][c];
+                    const float other = hi ? part[j][c] : part[2 + j][c];
+                    kept[j][c] = mine + __shfl_xor_sync(0xffffffffu, other, 2);
+                }
+            float v[3];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float mine = lo ? kept[1][c] : kept[0][c];
+                const float other = lo ? kept[0][c] : kept[1][c];
+                v[c] = mine + __shfl_xor_sync(0xffffffffu, other, 1);
+            }
+            if (use) color = add3(color, mul3s(vmul(mk3(v[0], v[1], v[2]), ld3(L.color)), weight));
+        }
+        if (active) {
+            if (env.spec) {
+                const f3 fiber_n = safe_normalize(sub3(view, mul3s(tangent, dot3(view, tangent))));
+                const f3 pr = probe_radiance(env, tangent, fiber_n, view, albedo, roughness, p.appearance[1]);
+                color = add3(color, mul3s(pr, pixel_ao(p, low)));
+            }
+            color = mul3s(color, a.exposure);
+            a.shaded[pix] = make_float4(color.x, color.y, color.z, 1.0f);
+            a.shaded_depth[pix] = view_dist;
+        }
+    }
+}
+
 std::mutex g_surrogate_attr_mutex;
 int g_surrogate_per_sm[64] = {};  // resident blocks per SM, 0 until the attribute is set
 bool g_tc_attr[64] = {};
@@ -1014,6 +1278,24 @@ cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights
         if (blocks > tiles) blocks = tiles;
         shade_surrogate_kernel<<<blocks, kSurrogateWarps * 32, kSurrogateSmem, ctx->stream>>>(
             a, reinterpret_cast<const __half*>(ctx->surrogate->w16), ctx->surrogate->params, env);
+        return cudaGetLastError();
+    }
+    if (model == 3u) {
+        const uint32_t pixels = ctx->width * ctx->height;
+        cudaError_t e = cudaMemsetAsync(ctx->hair_count, 0, sizeof(uint32_t), ctx->stream);
+        if (e != cudaSuccess) return e;
+        hair_list_kernel<<<(pixels + 255u) / 256u, 256, 0, ctx->stream>>>(ctx->center, pixels, ctx->hair_list,
+                                                                          ctx->hair_count, ctx->shaded,
+                                                                          ctx->shaded_depth);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        // two resident blocks per SM (the kernel's launch bounds), grid-striding over 32-pixel chunks
+        uint32_t blocks = (uint32_t)ctx->sm_count * 2u;
+        const uint32_t max_chunks = (pixels + 31u) / 32u;
+        const uint32_t needed = (max_chunks + kCompactWarps - 1) / kCompactWarps;
+        if (blocks > needed) blocks = needed;
+        shade_compact_kernel<<<blocks, kCompactWarps * 32, 0, ctx->stream>>>(
+            a, reinterpret_cast<const __half*>(ctx->surrogate->w16), ctx->surrogate->params, env, ctx->hair_list,
+            ctx->hair_count);
         return cudaGetLastError();
     }
     dim3 block(32, 8);

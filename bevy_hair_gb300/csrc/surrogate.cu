@@ -13,6 +13,7 @@
 
 #include "hg_internal.h"
 #include "hg_mlp.cuh"
+#include "hg_mlp_small.cuh"
 #include "hg_mlp_tc.cuh"
 
 namespace hg {
@@ -261,6 +262,149 @@ __global__ void __launch_bounds__(kWarps * 32) infer_kernel(const InferArgs a) {
                 if (a.net) a.net[(size_t)i * 12 + c] = y[c];
             }
         }
+    }
+}
+
+// The compact network (hg_mlp_small.cuh) on mma.sync, 32 samples per warp.
+__global__ void __launch_bounds__(kWarps * 32) infer_small_kernel(const InferArgs a) {
+    __shared__ __align__(16) mlps::Weights w;
+    __shared__ __align__(16) WarpIo io[kWarps];
+    mlps::load(w, a.w16, a.params, threadIdx.x, blockDim.x);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (uint32_t base = (blockIdx.x * kWarps + warp) * 32u; base < a.n; base += gridDim.x * kWarps * 32u) {
+        const uint32_t i = base + lane;
+        const bool valid = i < a.n;
+        float raw[10], x[10], y[12];
+        load_raw(a.inputs, i, valid, raw);
+        normalise(raw, x);
+        mlps::forward(w, io[warp], x, y);
+        if (valid) {
+#pragma unroll
+            for (int c = 0; c < 12; ++c) {
+                if (a.lobes) a.lobes[(size_t)i * 12 + c] = decode(y[c]);
+                if (a.net) a.net[(size_t)i * 12 + c] = y[c];
+            }
+        }
+    }
+}
+
+// Training of the compact network: one thread per sample (32 per block) runs
+// the forward pass with the inference roundings and the backward pass in
+// FP32; the block then sums its samples' weight gradients (each thread a
+// strided set of parameters, over the block's 32 samples) into `grad`.
+struct SmallTrainArgs {
+    const float* inputs;   // [n][10] raw
+    const float* targets;  // [n][12] transformed
+    uint32_t n;
+    const __half* w16;
+    const float* params;
+    float* grad;  // += d(sum of squared errors) / d(params)
+    float* loss;  // += sum of squared errors
+};
+
+constexpr int kSmallTrainThreads = 32;
+
+__global__ void __launch_bounds__(kSmallTrainThreads) small_train_kernel(const SmallTrainArgs a) {
+    __shared__ mlps::TrainWeights w;
+    __shared__ float s_x[kSmallTrainThreads][mlps::kIn], s_a1[kSmallTrainThreads][mlps::kHid], s_a2[kSmallTrainThreads][mlps::kHid];
+    __shared__ float s_d1[kSmallTrainThreads][mlps::kHid], s_d2[kSmallTrainThreads][mlps::kHid], s_dy[kSmallTrainThreads][mlps::kOut];
+    const int tid = threadIdx.x;
+    for (int i = tid; i < mlps::kHid * mlps::kIn; i += kSmallTrainThreads) (&w.w1[0][0])[i] = __half2float(a.w16[mlps::kW1 + i]);
+    for (int i = tid; i < mlps::kHid * mlps::kHid; i += kSmallTrainThreads) (&w.w2[0][0])[i] = __half2float(a.w16[mlps::kW2 + i]);
+    for (int i = tid; i < mlps::kOut * mlps::kHid; i += kSmallTrainThreads) (&w.w3[0][0])[i] = __half2float(a.w16[mlps::kW3 + i]);
+    for (int i = tid; i < mlps::kHid; i += kSmallTrainThreads) {
+        w.b1[i] = a.params[mlps::kB1 + i];
+        w.b2[i] = a.params[mlps::kB2 + i];
+        if (i < mlps::kOut) w.b3[i] = a.params[mlps::kB3 + i];
+    }
+    __syncthreads();
+    const uint32_t k = blockIdx.x * kSmallTrainThreads + tid;
+    const bool valid = k < a.n;
+    float raw[10], xn[10];
+    load_raw(a.inputs, k, valid, raw);
+    normalise(raw, xn);
+    float x[mlps::kIn];
+#pragma unroll
+    for (int i = 0; i < mlps::kIn; ++i) x[i] = i < mlp::kUsedIn ? mlps::round_half(xn[i]) : 0.0f;
+    float a1[mlps::kHid], a2[mlps::kHid];
+#pragma unroll
+    for (int j = 0; j < mlps::kHid; ++j) {
+        float z = w.b1[j];
+#pragma unroll
+        for (int i = 0; i < mlps::kIn; ++i) z += w.w1[j][i] * x[i];
+        a1[j] = mlps::round_half(fmaxf(z, 0.0f));
+    }
+#pragma unroll
+    for (int j = 0; j < mlps::kHid; ++j) {
+        float z = w.b2[j];
+#pragma unroll
+        for (int i = 0; i < mlps::kHid; ++i) z += w.w2[j][i] * a1[i];
+        a2[j] = mlps::round_half(fmaxf(z, 0.0f));
+    }
+    float dy[mlps::kOut];
+    float loss = 0.0f;
+#pragma unroll
+    for (int o = 0; o < mlps::kOut; ++o) {
+        float y = w.b3[o];
+#pragma unroll
+        for (int j = 0; j < mlps::kHid; ++j) y += w.w3[o][j] * a2[j];
+        const float d = valid && o < mlp::kUsedOut ? y - __ldg(&a.targets[(size_t)k * 12 + o]) : 0.0f;
+        loss += d * d;
+        dy[o] = 2.0f * d;
+    }
+    float d2[mlps::kHid], d1[mlps::kHid];
+#pragma unroll
+    for (int j = 0; j < mlps::kHid; ++j) {
+        float s = 0.0f;
+#pragma unroll
+        for (int o = 0; o < mlps::kOut; ++o) s += w.w3[o][j] * dy[o];
+        d2[j] = a2[j] > 0.0f ? s : 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < mlps::kHid; ++i) {
+        float s = 0.0f;
+#pragma unroll
+        for (int j = 0; j < mlps::kHid; ++j) s += w.w2[j][i] * d2[j];
+        d1[i] = a1[i] > 0.0f ? s : 0.0f;
+    }
+#pragma unroll
+    for (int i = 0; i < mlps::kIn; ++i) s_x[tid][i] = x[i];
+#pragma unroll
+    for (int j = 0; j < mlps::kHid; ++j) {
+        s_a1[tid][j] = a1[j];
+        s_a2[tid][j] = a2[j];
+        s_d1[tid][j] = d1[j];
+        s_d2[tid][j] = d2[j];
+    }
+#pragma unroll
+    for (int o = 0; o < mlps::kOut; ++o) s_dy[tid][o] = dy[o];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
+    if (tid == 0) atomicAdd(a.loss, loss);
+    __syncthreads();
+    for (int p = tid; p < mlps::kParams; p += kSmallTrainThreads) {
+        float g = 0.0f;
+        if (p < mlps::kB1) {
+            const int r = p / mlps::kIn, c = p - r * mlps::kIn;
+            for (int s = 0; s < kSmallTrainThreads; ++s) g += s_d1[s][r] * s_x[s][c];
+        } else if (p < mlps::kW2) {
+            const int r = p - mlps::kB1;
+            for (int s = 0; s < kSmallTrainThreads; ++s) g += s_d1[s][r];
+        } else if (p < mlps::kB2) {
+            const int r = (p - mlps::kW2) / mlps::kHid, c = (p - mlps::kW2) - r * mlps::kHid;
+            for (int s = 0; s < kSmallTrainThreads; ++s) g += s_d2[s][r] * s_a1[s][c];
+        } else if (p < mlps::kW3) {
+            const int r = p - mlps::kB2;
+            for (int s = 0; s < kSmallTrainThreads; ++s) g += s_d2[s][r];
+        } else if (p < mlps::kB3) {
+            const int r = (p - mlps::kW3) / mlps::kHid, c = (p - mlps::kW3) - r * mlps::kHid;
+            for (int s = 0; s < kSmallTrainThreads; ++s) g += s_dy[s][r] * s_a2[s][c];
+        } else {
+            const int r = p - mlps::kB3;
+            for (int s = 0; s < kSmallTrainThreads; ++s) g += s_dy[s][r];
+        }
+        if (g != 0.0f) atomicAdd(&a.grad[p], g);
     }
 }
 
@@ -586,6 +730,24 @@ __global__ void adam_kernel(const AdamArgs a) {
     }
 }
 
+// Adam for the compact network (no transposed copies).
+__global__ void adam_small_kernel(const AdamArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= mlps::kParams) return;
+    float p = a.params[i];
+    if (a.update) {
+        const float gr = a.grad[i] * a.gscale;
+        const float m = a.beta1 * a.m[i] + (1.0f - a.beta1) * gr;
+        const float v = a.beta2 * a.v[i] + (1.0f - a.beta2) * gr * gr;
+        a.m[i] = m;
+        a.v[i] = v;
+        p -= a.lr_t * m / (sqrtf(v) + a.eps_t);
+        a.params[i] = p;
+        a.grad[i] = 0.0f;
+    }
+    a.w16[i] = __float2half_rn(p);
+}
+
 // ------------------------------------------------------------ host side
 
 constexpr size_t kFwdSmem = sizeof(FwdWeights) + kWarps * sizeof(WarpIo);
@@ -683,7 +845,10 @@ cudaError_t convert(hg_mlp* m, int update, float lr_t, float eps_t, float gscale
     a.eps_t = eps_t;
     a.gscale = gscale;
     a.update = update;
-    adam_kernel<<<(kParams + 255) / 256, 256, 0, m->ctx->stream>>>(a);
+    if (m->arch == HG_MLP_ARCH_COMPACT)
+        adam_small_kernel<<<(mlps::kParams + 255) / 256, 256, 0, m->ctx->stream>>>(a);
+    else
+        adam_kernel<<<(kParams + 255) / 256, 256, 0, m->ctx->stream>>>(a);
     return cudaGetLastError();
 }
 
@@ -705,6 +870,19 @@ cudaError_t ensure_scratch(hg_mlp* m, uint32_t n) {
 // Forward + backward + weight gradients of n samples into m->grad (sum of
 // squared errors) and m->loss.
 cudaError_t run_gradients(hg_mlp* m, const float* inputs, const float* targets, uint32_t n) {
+    if (m->arch == HG_MLP_ARCH_COMPACT) {
+        SmallTrainArgs s;
+        s.inputs = inputs;
+        s.targets = targets;
+        s.n = n;
+        s.w16 = reinterpret_cast<const __half*>(m->w16);
+        s.params = m->params;
+        s.grad = m->grad;
+        s.loss = m->loss;
+        small_train_kernel<<<(n + kSmallTrainThreads - 1) / kSmallTrainThreads, kSmallTrainThreads, 0,
+                             m->ctx->stream>>>(s);
+        return cudaGetLastError();
+    }
     const uint32_t ld = m->ld_capacity;
     __half* s = reinterpret_cast<__half*>(m->scratch);
     TrainArgs a;
@@ -768,6 +946,12 @@ cudaError_t launch_mlp_infer(hg_mlp* m, const float* inputs, uint32_t n, float* 
     a.net = net;
     const uint32_t warps = (n + 31u) / 32u;
     uint32_t blocks = (warps + kWarps - 1) / kWarps;
+    if (m->arch == HG_MLP_ARCH_COMPACT) {
+        const uint32_t cap = (uint32_t)m->ctx->sm_count * 8u;
+        if (blocks > cap) blocks = cap;
+        infer_small_kernel<<<blocks, kWarps * 32, 0, m->ctx->stream>>>(a);
+        return cudaGetLastError();
+    }
     const uint32_t cap = (uint32_t)m->ctx->sm_count * 3u;
     if (blocks > cap) blocks = cap;
     infer_kernel<<<blocks, kWarps * 32, kFwdSmem, m->ctx->stream>>>(a);
@@ -781,21 +965,28 @@ using hg::fail;
 
 extern "C" {
 
-hg_status hg_mlp_create(hg_ctx* ctx, hg_mlp** out) {
+hg_status hg_mlp_create(hg_ctx* ctx, hg_mlp** out) { return hg_mlp_create_arch(ctx, HG_MLP_ARCH_DEEP, out); }
+
+hg_status hg_mlp_create_arch(hg_ctx* ctx, uint32_t arch, hg_mlp** out) {
     if (!ctx || !out) return HG_INVALID_ARG;
     *out = nullptr;
+    if (arch != HG_MLP_ARCH_DEEP && arch != HG_MLP_ARCH_COMPACT)
+        return fail(ctx, HG_INVALID_ARG, "unknown surrogate architecture");
     cudaSetDevice(ctx->device);
     MLP_CUDA(ctx, hg::ensure_device_setup(ctx->device));
     hg_mlp* m = new (std::nothrow) hg_mlp();
     if (!m) return fail(ctx, HG_OUT_OF_MEMORY, "allocating the surrogate");
     m->ctx = ctx;
-    const size_t pf = sizeof(float) * hg::mlp::kParams;
+    m->arch = arch;
+    m->n_params = arch == HG_MLP_ARCH_COMPACT ? (uint32_t)hg::mlps::kParams : (uint32_t)hg::mlp::kParams;
+    const size_t pf = sizeof(float) * m->n_params;
     cudaError_t e = cudaMalloc(&m->params, pf);
     if (e == cudaSuccess) e = cudaMalloc(&m->grad, pf);
     if (e == cudaSuccess) e = cudaMalloc(&m->adam_m, pf);
     if (e == cudaSuccess) e = cudaMalloc(&m->adam_v, pf);
-    if (e == cudaSuccess) e = cudaMalloc(&m->w16, sizeof(__half) * hg::mlp::kParams);
-    if (e == cudaSuccess) e = cudaMalloc(&m->wt16, sizeof(__half) * hg::mlp::kTransposed);
+    if (e == cudaSuccess) e = cudaMalloc(&m->w16, sizeof(__half) * m->n_params);
+    if (e == cudaSuccess && arch == HG_MLP_ARCH_DEEP)
+        e = cudaMalloc(&m->wt16, sizeof(__half) * hg::mlp::kTransposed);
     if (e == cudaSuccess) e = cudaMalloc(&m->loss, sizeof(float));
     for (void* p : {(void*)m->params, (void*)m->grad, (void*)m->adam_m, (void*)m->adam_v})
         if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, pf, ctx->stream);
@@ -823,10 +1014,12 @@ void hg_mlp_destroy(hg_mlp* m) {
     delete m;
 }
 
+uint32_t hg_mlp_param_count(const hg_mlp* m) { return m ? m->n_params : 0u; }
+
 hg_status hg_mlp_set_params(hg_mlp* m, const float* params, uint32_t count) {
     if (!m || !params) return HG_INVALID_ARG;
     hg_ctx* ctx = m->ctx;
-    if (count != (uint32_t)hg::mlp::kParams) return fail(ctx, HG_INVALID_ARG, "parameter count must be HG_MLP_PARAMS");
+    if (count != m->n_params) return fail(ctx, HG_INVALID_ARG, "parameter count must be hg_mlp_param_count");
     for (uint32_t i = 0; i < count; ++i)
         if (!std::isfinite(params[i])) return fail(ctx, HG_INVALID_ARG, "non-finite parameter");
     const size_t pf = sizeof(float) * count;
@@ -843,7 +1036,7 @@ hg_status hg_mlp_set_params(hg_mlp* m, const float* params, uint32_t count) {
 hg_status hg_mlp_get_params(hg_mlp* m, float* params, uint32_t count) {
     if (!m || !params) return HG_INVALID_ARG;
     hg_ctx* ctx = m->ctx;
-    if (count != (uint32_t)hg::mlp::kParams) return fail(ctx, HG_INVALID_ARG, "parameter count must be HG_MLP_PARAMS");
+    if (count != m->n_params) return fail(ctx, HG_INVALID_ARG, "parameter count must be hg_mlp_param_count");
     MLP_CUDA(ctx, cudaMemcpyAsync(params, m->params, sizeof(float) * count, cudaMemcpyDeviceToHost, ctx->stream));
     MLP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return HG_OK;
@@ -880,6 +1073,7 @@ hg_status hg_mlp_infer(hg_mlp* m, const float* inputs, uint32_t count, float* lo
 
 hg_status hg_mlp_infer_tc(hg_mlp* m, const float* inputs, uint32_t count, float* lobes, float* net) {
     if (!m) return HG_INVALID_ARG;
+    if (m->arch != HG_MLP_ARCH_DEEP) return fail(m->ctx, HG_INVALID_ARG, "tcgen05 inference runs the 4 x 64 network");
     if (count == 0) return HG_OK;
     if (!inputs || (!lobes && !net)) return fail(m->ctx, HG_INVALID_ARG, "null buffer");
     MLP_CUDA(m->ctx, hg::launch_mlp_infer_tc(m, inputs, count, lobes, net));
@@ -891,8 +1085,8 @@ hg_status hg_mlp_gradients(hg_mlp* m, const float* inputs, const float* targets,
     if (!m) return HG_INVALID_ARG;
     hg_ctx* ctx = m->ctx;
     if (count == 0 || !inputs || !targets || !grad) return fail(ctx, HG_INVALID_ARG, "empty batch or null buffer");
-    MLP_CUDA(ctx, hg::ensure_scratch(m, count));
-    const size_t pf = sizeof(float) * hg::mlp::kParams;
+    if (m->arch == HG_MLP_ARCH_DEEP) MLP_CUDA(ctx, hg::ensure_scratch(m, count));
+    const size_t pf = sizeof(float) * m->n_params;
     MLP_CUDA(ctx, cudaMemsetAsync(m->grad, 0, pf, ctx->stream));
     MLP_CUDA(ctx, cudaMemsetAsync(m->loss, 0, sizeof(float), ctx->stream));
     MLP_CUDA(ctx, hg::run_gradients(m, inputs, targets, count));
@@ -911,7 +1105,7 @@ hg_status hg_mlp_train_step(hg_mlp* m, const float* inputs, const float* targets
     hg_ctx* ctx = m->ctx;
     if (count == 0 || !inputs || !targets) return fail(ctx, HG_INVALID_ARG, "empty batch or null buffer");
     if (!(lr >= 0.0f) || !std::isfinite(lr)) return fail(ctx, HG_INVALID_ARG, "learning rate must be finite, >= 0");
-    MLP_CUDA(ctx, hg::ensure_scratch(m, count));
+    if (m->arch == HG_MLP_ARCH_DEEP) MLP_CUDA(ctx, hg::ensure_scratch(m, count));
     MLP_CUDA(ctx, hg::run_gradients(m, inputs, targets, count));
     m->step += 1;
     const double b1t = 1.0 - std::pow(0.9, (double)m->step), b2t = 1.0 - std::pow(0.999, (double)m->step);

@@ -1,8 +1,10 @@
 """The learned shading surrogate: host side of the ``hg_mlp_*`` entry points.
 
-A 10 -> 4 x 64 -> 12 ReLU network (FP16 weights and activations, FP32
-accumulation on the tensor cores) that stands in for the Karis-fit lobes of
-``shade.wesl:94-190``.  It is trained on FP64 samples of the exact lobes
+A ReLU network (FP16 weights and activations, FP32 accumulation on the
+tensor cores) that stands in for the Karis-fit lobes of
+``shade.wesl:94-190``: 10 -> 4 x 64 -> 12 (``MLP_ARCH_DEEP``, shade models 1
+and 2) or the compact 10 -> 2 x 32 -> 12 (``MLP_ARCH_COMPACT``, shade model
+3).  It is trained on FP64 samples of the exact lobes
 (Gauss-Legendre integration of the Marschner/d'Eon azimuthal scattering plus
 the Zinke back-scattering term), generated on the GPU by ``hg_mlp_samples``.
 
@@ -22,48 +24,64 @@ from . import abi
 from .pipeline import HairRenderer, _check
 
 WEIGHTS = Path(__file__).resolve().parent / "surrogate_weights.npy"
+COMPACT_WEIGHTS = Path(__file__).resolve().parent / "surrogate_compact_weights.npy"
 TILT = 0.08                 # longitudinal tilt the network is trained at (all configs use it)
 SAMPLE_SEED = 0x5EED0005    # seed of the training set (16M samples)
 HOLDOUT_FIRST = 1 << 40     # sample index where the held-out set starts
 
-# Parameter layout (hg_mlp.cuh): W1[64][16] b1 W2[64][64] b2 W3 b3 W4 b4 W5[16][64] b5.
+# Parameter layouts: hg_mlp.cuh W1[64][16] b1 W2[64][64] b2 W3 b3 W4 b4 W5[16][64] b5;
+# hg_mlp_small.cuh W1[32][16] b1 W2[32][32] b2 W3[16][32] b3.
 LAYERS = ((64, 16), (64, 64), (64, 64), (64, 64), (16, 64))
+COMPACT_LAYERS = ((32, 16), (32, 32), (16, 32))
 
 
-def split(params: np.ndarray) -> list[tuple[np.ndarray, np.ndarray]]:
+def layers_of(arch: int = abi.MLP_ARCH_DEEP):
+    return COMPACT_LAYERS if arch == abi.MLP_ARCH_COMPACT else LAYERS
+
+
+def param_count(arch: int = abi.MLP_ARCH_DEEP) -> int:
+    return abi.MLP_COMPACT_PARAMS if arch == abi.MLP_ARCH_COMPACT else abi.MLP_PARAMS
+
+
+def split(params: np.ndarray, arch: int = abi.MLP_ARCH_DEEP) -> list[tuple[np.ndarray, np.ndarray]]:
     """Views (W[out][in], b[out]) of each layer of a flat parameter vector."""
     out, o = [], 0
-    for rows, cols in LAYERS:
+    for rows, cols in layers_of(arch):
         w = params[o:o + rows * cols].reshape(rows, cols)
         o += rows * cols
         b = params[o:o + rows]
         o += rows
         out.append((w, b))
-    assert o == abi.MLP_PARAMS
+    assert o == param_count(arch) == len(params)
     return out
 
 
-def init_params(seed: int = 0) -> np.ndarray:
+def init_params(seed: int = 0, arch: int = abi.MLP_ARCH_DEEP) -> np.ndarray:
     """He-normal hidden layers, a small output layer, zero biases and zero padding."""
     rng = np.random.default_rng(seed)
-    p = np.zeros(abi.MLP_PARAMS, dtype=np.float32)
-    fan_in = (abi.MLP_INPUTS, 64, 64, 64, 64)
-    for k, (w, _b) in enumerate(split(p)):
-        std = math.sqrt(2.0 / fan_in[k]) * (0.5 if k == 4 else 1.0)
+    p = np.zeros(param_count(arch), dtype=np.float32)
+    layers = split(p, arch)
+    for k, (w, _b) in enumerate(layers):
+        fan_in = abi.MLP_INPUTS if k == 0 else w.shape[1]
+        std = math.sqrt(2.0 / fan_in) * (0.5 if k == len(layers) - 1 else 1.0)
         w[...] = rng.normal(0.0, std, size=w.shape).astype(np.float32)
-    w1, _ = split(p)[0]
-    w1[:, abi.MLP_INPUTS:] = 0.0
-    w5, b5 = split(p)[4]
-    w5[abi.MLP_OUTPUTS:, :] = 0.0
-    b5[...] = 0.0
+    layers[0][0][:, abi.MLP_INPUTS:] = 0.0
+    w_out, b_out = layers[-1]
+    w_out[abi.MLP_OUTPUTS:, :] = 0.0
+    b_out[...] = 0.0
     return p
 
 
-def load_params() -> np.ndarray:
+def weights_path(arch: int = abi.MLP_ARCH_DEEP) -> Path:
+    return COMPACT_WEIGHTS if arch == abi.MLP_ARCH_COMPACT else WEIGHTS
+
+
+def load_params(arch: int = abi.MLP_ARCH_DEEP) -> np.ndarray:
     """The trained parameters shipped with the package."""
-    p = np.load(WEIGHTS).astype(np.float32)
-    if p.shape != (abi.MLP_PARAMS,):
-        raise ValueError(f"{WEIGHTS} holds {p.shape}, expected ({abi.MLP_PARAMS},)")
+    path = weights_path(arch)
+    p = np.load(path).astype(np.float32)
+    if p.shape != (param_count(arch),):
+        raise ValueError(f"{path} holds {p.shape}, expected ({param_count(arch)},)")
     return p
 
 
@@ -76,12 +94,14 @@ def _ptr(t) -> int | None:
 class Surrogate:
     """One hg_mlp on a renderer's context."""
 
-    def __init__(self, renderer: HairRenderer, params: np.ndarray | None = None):
+    def __init__(self, renderer: HairRenderer, params: np.ndarray | None = None, arch: int = abi.MLP_ARCH_DEEP):
         self.renderer = renderer
         self.lib = renderer.lib
+        self.arch = int(arch)
         h = C.c_void_p()
-        _check(self.lib, renderer.ctx, self.lib.hg_mlp_create(renderer.ctx, C.byref(h)))
+        _check(self.lib, renderer.ctx, self.lib.hg_mlp_create_arch(renderer.ctx, self.arch, C.byref(h)))
         self.handle = h
+        self.n_params = int(self.lib.hg_mlp_param_count(h))
         if not hasattr(renderer, "_surrogates"):
             renderer._surrogates = []
         renderer._surrogates.append(self)
@@ -96,7 +116,7 @@ class Surrogate:
         self._check(self.lib.hg_mlp_set_params(self.handle, p.ctypes.data, p.size))
 
     def get_params(self) -> np.ndarray:
-        p = np.empty(abi.MLP_PARAMS, dtype=np.float32)
+        p = np.empty(self.n_params, dtype=np.float32)
         self._check(self.lib.hg_mlp_get_params(self.handle, p.ctypes.data, p.size))
         return p
 
@@ -105,12 +125,13 @@ class Surrogate:
         self._check(self.lib.hg_mlp_infer(self.handle, _ptr(inputs), n, _ptr(lobes), _ptr(net)))
 
     def infer_tc(self, inputs, n: int, lobes=None, net=None) -> None:
-        """The same evaluation on the tcgen05 tensor cores (128 rows per MMA, TMEM accumulators)."""
+        """The same evaluation on the tcgen05 tensor cores (128 rows per MMA, TMEM accumulators);
+        4 x 64 network only."""
         self._check(self.lib.hg_mlp_infer_tc(self.handle, _ptr(inputs), n, _ptr(lobes), _ptr(net)))
 
     def gradients(self, inputs, targets, n: int) -> tuple[np.ndarray, float]:
         """Gradient of sum((net - target)^2) over one device batch, and that sum."""
-        g = np.empty(abi.MLP_PARAMS, dtype=np.float32)
+        g = np.empty(self.n_params, dtype=np.float32)
         loss = C.c_float()
         self._check(self.lib.hg_mlp_gradients(self.handle, _ptr(inputs), _ptr(targets), n, g.ctypes.data,
                                               C.byref(loss)))
@@ -180,7 +201,7 @@ def evaluate(renderer: HairRenderer, surrogate: Surrogate, n: int = 1 << 16, see
 
 def train(renderer: HairRenderer, n_samples: int = 16 << 20, batch: int = 16384, epochs: int = 150,
           lr_max: float = 3e-3, lr_min: float = 1e-5, warmup: int = 200, seed: int = SAMPLE_SEED,
-          init_seed: int = 0, log=print) -> tuple[np.ndarray, dict]:
+          init_seed: int = 0, log=print, arch: int = abi.MLP_ARCH_DEEP) -> tuple[np.ndarray, dict]:
     """Generate n_samples FP64 samples on the GPU and fit the network with Adam
     (linear warm-up, cosine decay).  Returns the parameters and a history."""
     import torch
@@ -197,7 +218,7 @@ def train(renderer: HairRenderer, n_samples: int = 16 << 20, batch: int = 16384,
     t_gen = time.perf_counter() - t0
     log(f"generated {n_samples} FP64 samples in {t_gen:.1f} s")
 
-    s = Surrogate(renderer, init_params(init_seed))
+    s = Surrogate(renderer, init_params(init_seed, arch), arch)
     n_batches = n_samples // batch
     steps = n_batches * epochs
     losses = torch.zeros(steps, dtype=torch.float32, device=dev)
@@ -221,7 +242,8 @@ def train(renderer: HairRenderer, n_samples: int = 16 << 20, batch: int = 16384,
     renderer.synchronize()
     t_train = time.perf_counter() - t1
     params = s.get_params()
-    hist = {"generate_s": t_gen, "train_s": t_train, "steps": steps, "batch": batch, "epochs": epochs,
+    hist = {"arch": "2x32" if arch == abi.MLP_ARCH_COMPACT else "4x64", "generate_s": t_gen, "train_s": t_train,
+            "steps": steps, "batch": batch, "epochs": epochs,
             "samples": n_samples, "final_mse": losses[-n_batches:].mean().item() / (batch * 12),
             "first_mse": losses[:min(50, steps)].mean().item() / (batch * 12)}
     hist.update(evaluate(renderer, s))
@@ -239,11 +261,15 @@ def main(argv=None) -> int:
     ap.add_argument("--batch", type=int, default=16384)
     ap.add_argument("--epochs", type=int, default=150)
     ap.add_argument("--lr", type=float, default=3e-3)
-    ap.add_argument("--out", type=Path, default=WEIGHTS)
+    ap.add_argument("--arch", choices=("4x64", "2x32"), default="4x64")
+    ap.add_argument("--out", type=Path, default=None)
     ap.add_argument("--history", type=Path, default=None)
     a = ap.parse_args(argv)
+    arch = abi.MLP_ARCH_COMPACT if a.arch == "2x32" else abi.MLP_ARCH_DEEP
+    if a.out is None:
+        a.out = weights_path(arch)
     with HairRenderer(0) as r:
-        params, hist = train(r, n_samples=a.samples, batch=a.batch, epochs=a.epochs, lr_max=a.lr)
+        params, hist = train(r, n_samples=a.samples, batch=a.batch, epochs=a.epochs, lr_max=a.lr, arch=arch)
     a.out.parent.mkdir(parents=True, exist_ok=True)
     np.save(a.out, params)
     text = json.dumps(hist, indent=1)

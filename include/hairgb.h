@@ -151,8 +151,9 @@ typedef struct hg_shade_desc {
     uint32_t light_count;
     uint32_t ortho;           /* 1 when the camera projection is orthographic */
     float exposure;           /* view.exposure */
-    uint32_t shade_model;     /* 0: Karis fit (shade.wesl); 1: learned surrogate on tcgen05;
-                                 2: the surrogate on mma.sync (for comparison) */
+    uint32_t shade_model;     /* 0: Karis fit (shade.wesl); 1: learned 4 x 64 surrogate on tcgen05;
+                                 2: the 4 x 64 surrogate on mma.sync (for comparison);
+                                 3: the compact 2 x 32 surrogate on mma.sync */
 } hg_shade_desc;
 
 /* Buffers a context owns. */
@@ -505,12 +506,23 @@ hg_status hg_batch_copy_out_async(hg_batch* batch, uint32_t item, hg_buffer_id w
 #define HG_MLP_PARAMS 14608u
 #define HG_MLP_INPUTS 10u
 #define HG_MLP_OUTPUTS 12u
+/* The compact network: 10 -> 32 -> 32 -> 12, the same inputs, outputs,
+ * roundings and output transform; HG_MLP_COMPACT_PARAMS floats W1[32][16]
+ * b1[32] W2[32][32] b2[32] W3[16][32] b3[16] (padding columns 10..15 of W1
+ * and rows 12..15 of W3 and b3 stay zero).  Shade model 3 evaluates it. */
+#define HG_MLP_COMPACT_PARAMS 2128u
+#define HG_MLP_ARCH_DEEP 0u     /* 4 x 64, HG_MLP_PARAMS */
+#define HG_MLP_ARCH_COMPACT 1u  /* 2 x 32, HG_MLP_COMPACT_PARAMS */
 
 typedef struct hg_mlp hg_mlp;
 
-hg_status hg_mlp_create(hg_ctx* ctx, hg_mlp** out);   /* parameters start at zero */
+hg_status hg_mlp_create(hg_ctx* ctx, hg_mlp** out);   /* the 4 x 64 network; parameters start at zero */
+/* A surrogate of the given HG_MLP_ARCH_*; parameters start at zero. */
+hg_status hg_mlp_create_arch(hg_ctx* ctx, uint32_t arch, hg_mlp** out);
 void hg_mlp_destroy(hg_mlp* mlp);
-/* Host float[count], count == HG_MLP_PARAMS; resets the optimiser state. */
+/* Number of parameters of the surrogate's architecture (0 for NULL). */
+uint32_t hg_mlp_param_count(const hg_mlp* mlp);
+/* Host float[count], count == hg_mlp_param_count; resets the optimiser state. */
 hg_status hg_mlp_set_params(hg_mlp* mlp, const float* params, uint32_t count);
 hg_status hg_mlp_get_params(hg_mlp* mlp, float* params, uint32_t count);
 /* Training samples with FP64 lobes (Gauss-Legendre integration of the
@@ -526,10 +538,11 @@ hg_status hg_mlp_samples(hg_ctx* ctx, uint64_t seed, uint64_t first, uint32_t co
 hg_status hg_mlp_infer(hg_mlp* mlp, const float* inputs, uint32_t count, float* lobes, float* net);
 /* The same evaluation on the tcgen05 tensor cores: 128 rows per MMA,
  * accumulators in tensor memory, biases as two extra FP16 (high, low)
- * product columns.  Outputs match hg_mlp_infer to FP16 rounding. */
+ * product columns.  Outputs match hg_mlp_infer to FP16 rounding.  4 x 64
+ * network only (HG_INVALID_ARG for the compact one). */
 hg_status hg_mlp_infer_tc(hg_mlp* mlp, const float* inputs, uint32_t count, float* lobes, float* net);
 /* Gradient of the sum over samples and outputs of (net - target)^2 for one
- * batch (device inputs/targets), into host float[HG_MLP_PARAMS]; the loss sum
+ * batch (device inputs/targets), into host float[hg_mlp_param_count]; the loss sum
  * into *loss (nullable).  Parameters are unchanged. */
 hg_status hg_mlp_gradients(hg_mlp* mlp, const float* inputs, const float* targets, uint32_t count, float* grad,
                            float* loss);
@@ -543,8 +556,8 @@ hg_status hg_mlp_train_step(hg_mlp* mlp, const float* inputs, const float* targe
  * inputs (device float[count][10] -> device float[count][12]; beta_n and eta
  * do not enter the fit). */
 hg_status hg_karis_lobes(hg_ctx* ctx, const float* inputs, uint32_t count, float tilt, float* lobes);
-/* Bind (or, with NULL, unbind) the surrogate that hg_shade_desc.shade_model 1
- * uses on this context. */
+/* Bind (or, with NULL, unbind) the surrogate that hg_shade_desc.shade_model
+ * 1, 2 (4 x 64 network) or 3 (compact network) uses on this context. */
 hg_status hg_mlp_bind(hg_ctx* ctx, hg_mlp* mlp);
 
 #ifdef __cplusplus

@@ -69,9 +69,10 @@ _SIGS = {
     "oracle_scan": (None, [_VP, _VP, _VP, _U32, _VP]),
     "oracle_strand_points": (_U32, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "oracle_raster": (None, [_VP, _VP, _VP, _VP, _VP, _U32, _VP, _VP, _VP, _VP, _VP, C.POINTER(Counts)]),
-    "oracle_shade": (None, [_VP, _VP, _VP, _VP, _VP, _U32, _U32, _F, _VP, _VP, _VP, _VP]),
+    "oracle_shade": (None, [_VP, _VP, _VP, _VP, _VP, _U32, _U32, _F, _VP, _U32, _VP, _VP, _VP]),
     "oracle_sample_cube": (None, [_VP, _U32, _U32, _VP, _F, _VP]),
     "oracle_mlp_forward": (None, [_VP, _VP, _U32, _VP]),
+    "oracle_mlp_forward_arch": (None, [_VP, _U32, _VP, _U32, _VP]),
     "oracle_filter": (None, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "oracle_composite": (None, [_VP, _VP, _VP, _VP, _VP]),
     "oracle_hair_visibility": (None, [_VP, _VP, _U32, _U32, _VP, _U32, _VP]),
@@ -157,8 +158,9 @@ def raster(params, mesh, refs, total, center, cons, beta, dom, scene_depth=None)
     return counts.as_dict()
 
 
-def shade(params, center, beta, dom, lights, exposure=1.0, ortho=False, mlp=None, env=None):
-    """Shade model 0 (Karis fit), or model 1 when `mlp` holds the surrogate's parameters;
+def shade(params, center, beta, dom, lights, exposure=1.0, ortho=False, mlp=None, env=None, mlp_arch=0):
+    """Shade model 0 (Karis fit), or the surrogate when `mlp` holds its parameters
+    (mlp_arch 0: the 4 x 64 network of models 1 and 2; 1: the compact network of model 3);
     env: a bevy_hair_gb300.envmap.Environment for the light-probe term."""
     w, h = int(params["screen"][0]), int(params["screen"][1])
     shaded = np.empty(w * h * 4, dtype=np.float32)
@@ -168,7 +170,7 @@ def shade(params, center, beta, dom, lights, exposure=1.0, ortho=False, mlp=None
     mlp_arr = None if mlp is None else np.ascontiguousarray(mlp, dtype=np.float32)
     e, keep = _env(env)
     lib().oracle_shade(_p(params), _p(center), _p(beta), _p(dom_arr), _p(lights) if len(lights) else None,
-                       len(lights), int(ortho), float(exposure), _p(mlp_arr), C.byref(e) if e else None,
+                       len(lights), int(ortho), float(exposure), _p(mlp_arr), int(mlp_arch), C.byref(e) if e else None,
                        _p(shaded), _p(sdepth))
     return shaded, sdepth
 
@@ -181,12 +183,13 @@ def sample_cube(texels: np.ndarray, size: int, levels: int, direction, lod: floa
     return out
 
 
-def mlp_forward(params: np.ndarray, raw: np.ndarray) -> np.ndarray:
-    """The surrogate network on raw inputs (n, 10) -> raw outputs (n, 12), FP16 rounding emulated."""
+def mlp_forward(params: np.ndarray, raw: np.ndarray, arch: int = 0) -> np.ndarray:
+    """The surrogate network on raw inputs (n, 10) -> raw outputs (n, 12), FP16 rounding emulated
+    (arch 0: 4 x 64; 1: the compact 2 x 32)."""
     p = np.ascontiguousarray(params, dtype=np.float32)
     x = np.ascontiguousarray(raw, dtype=np.float32).reshape(-1, 10)
     out = np.empty((len(x), 12), dtype=np.float32)
-    lib().oracle_mlp_forward(_p(p), _p(x), len(x), _p(out))
+    lib().oracle_mlp_forward_arch(_p(p), int(arch), _p(x), len(x), _p(out))
     return out
 
 
@@ -204,7 +207,8 @@ def composite(params, color_src, depth_src, color_dst, depth_dst) -> None:
                            _p(np.ascontiguousarray(depth_src, dtype=np.float32)), _p(color_dst), _p(depth_dst))
 
 
-def frame(mesh, camera, dom_params, lights, exposure=1.0, ortho=False, scene_depth=None, mlp=None, env=None) -> dict:
+def frame(mesh, camera, dom_params, lights, exposure=1.0, ortho=False, scene_depth=None, mlp=None, env=None,
+          mlp_arch=0) -> dict:
     """The per-groom sequence of hair_pass (src/render/pass.rs:375-643) on the CPU."""
     w, h = int(camera["screen"][0]), int(camera["screen"][1])
     out: dict = {}
@@ -225,7 +229,7 @@ def frame(mesh, camera, dom_params, lights, exposure=1.0, ortho=False, scene_dep
         layers = dom_params.copy()
         layers["pass_mode"][0] = 2
         out["counts_dom_layers"] = raster(layers, mesh, refs_d, total_d, center, cons, beta, dom)
-    shaded, sdepth = shade(camera, center, beta, dom, lights, exposure, ortho, mlp, env)
+    shaded, sdepth = shade(camera, center, beta, dom, lights, exposure, ortho, mlp, env, mlp_arch)
     out.update(center=center, cons=cons, beta=beta, dom=dom, shaded=shaded, shaded_depth=sdepth)
     if int(camera["flags"][1]):
         filt, fdepth = filter_(camera, center, cons, shaded, sdepth)

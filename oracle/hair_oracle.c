@@ -961,7 +961,11 @@ static void mlp_layer(const float* w, const float* b, const float* in, int n_in,
     }
 }
 
-void oracle_mlp_forward(const float* params, const float* raw, uint32_t n, float* net) {
+/* arch 0: 10 -> 4 x 64 -> 12 (hg_mlp.cuh); arch 1: the compact 10 -> 2 x 32
+ * -> 12 (hg_mlp_small.cuh), parameters W1[32][16] b1 W2[32][32] b2 W3[16][32]
+ * b3.  Same normalisation, roundings and output space. */
+void oracle_mlp_forward_arch(const float* params, uint32_t arch, const float* raw, uint32_t n, float* net) {
+    const int hid = arch == 1u ? 32 : 64, hidden_layers = arch == 1u ? 2 : 4;
     for (uint32_t s = 0; s < n; ++s) {
         const float* r = raw + 10 * (size_t)s;
         float x[16] = {0}, h0[64], h1[64], y[16];
@@ -975,17 +979,23 @@ void oracle_mlp_forward(const float* params, const float* raw, uint32_t n, float
         x[9] = (r[9] - 1.55f) * 10.0f;
         for (int k = 0; k < 16; ++k) x[k] = round_half(x[k]);
         const float* p = params;
-        mlp_layer(p, p + 1024, x, 16, 64, 1, h0);
-        p += 1024 + 64;
-        mlp_layer(p, p + 4096, h0, 64, 64, 1, h1);
-        p += 4096 + 64;
-        mlp_layer(p, p + 4096, h1, 64, 64, 1, h0);
-        p += 4096 + 64;
-        mlp_layer(p, p + 4096, h0, 64, 64, 1, h1);
-        p += 4096 + 64;
-        mlp_layer(p, p + 1024, h1, 64, 16, 0, y);
+        mlp_layer(p, p + 16 * hid, x, 16, hid, 1, h0);
+        p += 16 * hid + hid;
+        float *in = h0, *out = h1;
+        for (int l = 1; l < hidden_layers; ++l) {
+            mlp_layer(p, p + hid * hid, in, hid, hid, 1, out);
+            p += hid * hid + hid;
+            float* t = in;
+            in = out;
+            out = t;
+        }
+        mlp_layer(p, p + 16 * hid, in, hid, 16, 0, y);
         for (int c = 0; c < 12; ++c) net[12 * (size_t)s + c] = y[c];
     }
+}
+
+void oracle_mlp_forward(const float* params, const float* raw, uint32_t n, float* net) {
+    oracle_mlp_forward_arch(params, 0u, raw, n, net);
 }
 
 static inline float mlp_decode(float y) { return 1e-3f * expm1f(fmaxf(y, 0.0f)); }
@@ -993,7 +1003,7 @@ static inline float mlp_decode(float y) { return 1e-3f * expm1f(fmaxf(y, 0.0f));
 /* Shade model 1: the network's R, TT, TRT and back-scattering per light; the
  * shadowed forward spread keeps dual_scatter's statistics.  beta_n is the
  * fibre roughness clamped to [0.2, 0.8]. */
-static v3 surrogate_bsdf(const float* mlp, v3 tangent, v3 view, v3 light, v3 sigma_a, shape_t shape,
+static v3 surrogate_bsdf(const float* mlp, uint32_t arch, v3 tangent, v3 view, v3 light, v3 sigma_a, shape_t shape,
                          const dual_t* ds, float depth, float roughness) {
     v3 t = safe_normalize(tangent);
     v3 v = safe_normalize(view);
@@ -1008,7 +1018,7 @@ static v3 surrogate_bsdf(const float* mlp, v3 tangent, v3 view, v3 light, v3 sig
     float raw[10] = {sin_i, sin_o, cos_phi, sqrtf(fmaxf(1.0f - cos_phi * cos_phi, 0.0f)), sigma_a.x, sigma_a.y,
                      sigma_a.z, shape.beta.x, clampf(roughness, 0.2f, 0.8f), IOR};
     float y[12];
-    oracle_mlp_forward(mlp, raw, 1, y);
+    oracle_mlp_forward_arch(mlp, arch, raw, 1, y);
     v3 single = V3(mlp_decode(y[0]) + mlp_decode(y[3]) + mlp_decode(y[6]),
                    mlp_decode(y[1]) + mlp_decode(y[4]) + mlp_decode(y[7]),
                    mlp_decode(y[2]) + mlp_decode(y[5]) + mlp_decode(y[8]));
@@ -1019,9 +1029,9 @@ static v3 surrogate_bsdf(const float* mlp, v3 tangent, v3 view, v3 light, v3 sig
     return color;
 }
 
-static v3 light_lobe(const float* mlp, v3 tangent, v3 view, v3 incident, v3 sigma_a, shape_t shape, const dual_t* ds,
-                     float depth, float roughness) {
-    if (mlp) return surrogate_bsdf(mlp, tangent, view, incident, sigma_a, shape, ds, depth, roughness);
+static v3 light_lobe(const float* mlp, uint32_t arch, v3 tangent, v3 view, v3 incident, v3 sigma_a, shape_t shape,
+                     const dual_t* ds, float depth, float roughness) {
+    if (mlp) return surrogate_bsdf(mlp, arch, tangent, view, incident, sigma_a, shape, ds, depth, roughness);
     return hair_bsdf(tangent, view, incident, sigma_a, shape, ds, 1.0f, depth);
 }
 
@@ -1208,7 +1218,7 @@ static inline float spot_mask(const hg_light* L, v3 world) {
 /* shade.wesl:429-521: point, spot, directional then rect lights. */
 static v3 direct_light(const hg_hair_params* p, const uint32_t* dom, const hg_light* lights, uint32_t n_lights,
                        v3 world, v3 tangent, v3 view, v3 albedo, float roughness, float tilt, float beta,
-                       const float* mlp) {
+                       const float* mlp, uint32_t mlp_arch) {
     shape_t shape = lobe_shape(roughness, tilt);
     float tv = dot3(tangent, view);
     float cos_theta_o = sqrtf(fmaxf(1.0f - tv * tv, 1e-6f));
@@ -1226,7 +1236,7 @@ static v3 direct_light(const hg_hair_params* p, const uint32_t* dom, const hg_li
                 v3 incident = safe_normalize(light_to_frag);
                 float inv_r2 = 1.0f / fmaxf(L->range * L->range, 1e-8f);
                 float att = distance_attenuation(dist2, inv_r2);
-                v3 lobe = light_lobe(mlp, tangent, view, incident, sigma_a, shape, &ds, 0.0f, roughness);
+                v3 lobe = light_lobe(mlp, mlp_arch, tangent, view, incident, sigma_a, shape, &ds, 0.0f, roughness);
                 v3 c = mul3s(mul3(lobe, ld3(L->color)), att);
                 if (kind == HG_LIGHT_SPOT) c = mul3s(c, spot_mask(L, world));
                 color = add3(color, c);
@@ -1238,7 +1248,7 @@ static v3 direct_light(const hg_hair_params* p, const uint32_t* dom, const hg_li
                     depth = -logf(fmaxf(dom_visibility(p, dom, world, beta), 1e-6f));
                     dom_left = 0;
                 }
-                v3 lobe = light_lobe(mlp, tangent, view, incident, sigma_a, shape, &ds, depth, roughness);
+                v3 lobe = light_lobe(mlp, mlp_arch, tangent, view, incident, sigma_a, shape, &ds, depth, roughness);
                 color = add3(color, mul3(lobe, ld3(L->color)));
             } else {
                 v3 to_center = sub3(ld3(L->position), world);
@@ -1249,7 +1259,7 @@ static v3 direct_light(const hg_hair_params* p, const uint32_t* dom, const hg_li
                 float solid = L->spot[0] * L->spot[1] * facing / dist2;
                 float range2 = fmaxf(L->range * L->range, 1e-4f);
                 float falloff = range_falloff(dist2, 1.0f / range2);
-                v3 lobe = light_lobe(mlp, tangent, view, incident, sigma_a, shape, &ds, 0.0f, roughness);
+                v3 lobe = light_lobe(mlp, mlp_arch, tangent, view, incident, sigma_a, shape, &ds, 0.0f, roughness);
                 color = add3(color, mul3s(mul3s(mul3(lobe, ld3(L->color)), solid), falloff));
             }
         }
@@ -1261,7 +1271,7 @@ static v3 direct_light(const hg_hair_params* p, const uint32_t* dom, const hg_li
  * in the specialization without ENVIRONMENT_MAP, shade.wesl:384-394). */
 void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_t* beta_buf, const uint32_t* dom,
                   const hg_light* lights, uint32_t n_lights, uint32_t ortho, float exposure, const float* mlp,
-                  const oracle_env* env, float* shaded, float* shaded_depth) {
+                  uint32_t mlp_arch, const oracle_env* env, float* shaded, float* shaded_depth) {
     uint32_t width = f2u(p->screen[0]), height = f2u(p->screen[1]);
     int nthreads = oracle_get_threads();
 #pragma omp parallel for schedule(dynamic, 256) num_threads(nthreads)
@@ -1292,7 +1302,7 @@ void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_
         } else {
             view = safe_normalize(sub3(ld3(p->camera_pos), world));
         }
-        v3 color = direct_light(p, dom, lights, n_lights, world, tangent, view, albedo, roughness, tilt, beta, mlp);
+        v3 color = direct_light(p, dom, lights, n_lights, world, tangent, view, albedo, roughness, tilt, beta, mlp, mlp_arch);
         if (env) {
             v3 fiber_n = safe_normalize(sub3(view, mul3s(tangent, dot3(view, tangent))));
             color = add3(color, mul3s(probe_radiance(env, tangent, fiber_n, view, albedo, roughness, tilt), ao));

@@ -90,16 +90,19 @@ typedef struct oracle_env {
     float intensity;
 } oracle_env;
 
-/* mlp: NULL for shade model 0 (Karis fit); the surrogate's HG_MLP_PARAMS
- * floats for shade model 1.  env: NULL without a light probe. */
+/* mlp: NULL for shade model 0 (Karis fit); else the surrogate's parameters
+ * for shade models 1 and 2 (mlp_arch 0, HG_MLP_PARAMS floats) or 3 (mlp_arch
+ * 1, HG_MLP_COMPACT_PARAMS floats).  env: NULL without a light probe. */
 void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_t* beta, const uint32_t* dom,
                   const hg_light* lights, uint32_t n_lights, uint32_t ortho, float exposure, const float* mlp,
-                  const oracle_env* env, float* shaded, float* shaded_depth);
+                  uint32_t mlp_arch, const oracle_env* env, float* shaded, float* shaded_depth);
 /* One trilinear cubemap sample (RGB9E5 mip chain) for the sampler tests. */
 void oracle_sample_cube(const uint32_t* texels, uint32_t size, uint32_t levels, const float dir[3], float lod,
                         float out[3]);
-/* The surrogate network on raw inputs (n x 10) -> raw outputs (n x 12). */
+/* The surrogate network on raw inputs (n x 10) -> raw outputs (n x 12):
+ * the 4 x 64 network, or the given architecture (0: 4 x 64, 1: 2 x 32). */
 void oracle_mlp_forward(const float* params, const float* raw, uint32_t n, float* net);
+void oracle_mlp_forward_arch(const float* params, uint32_t arch, const float* raw, uint32_t n, float* net);
 void oracle_filter(const hg_hair_params* p, const uint64_t* center, const uint64_t* cons,
                    const float* shaded, const float* shaded_depth, float* filtered, float* filtered_depth);
 /* hair_shadow.wesl:52-75: light is a ShadowLight (28 floats). */

@@ -1,8 +1,9 @@
 """FP64 reference of the shading surrogate's network.  TEST INFRASTRUCTURE ONLY.
 
-Forward and backward passes of the 10 -> 4 x 64 -> 12 ReLU network that
-libhairgb.so trains and evaluates on the tensor cores (bevy_hair_gb300/csrc/
-hg_mlp.cuh, surrogate.cu).  With ``half=True`` the weights, the normalised
+Forward and backward passes of the 10 -> 4 x 64 -> 12 ReLU network (arch 0)
+and of the compact 10 -> 2 x 32 -> 12 network (arch 1) that libhairgb.so
+trains and evaluates (bevy_hair_gb300/csrc/hg_mlp.cuh, hg_mlp_small.cuh,
+surrogate.cu).  With ``half=True`` the weights, the normalised
 inputs and the post-ReLU activations are rounded to FP16 exactly where the
 kernels round them, and everything else is FP64; the gradients are not
 rounded (the kernels round the backward pass's fragments to FP16, so the
@@ -17,18 +18,24 @@ import numpy as np
 
 LAYERS = ((64, 16), (64, 64), (64, 64), (64, 64), (16, 64))
 N_PARAMS = 14608
+COMPACT_LAYERS = ((32, 16), (32, 32), (16, 32))
+COMPACT_PARAMS = 2128
 N_OUT = 12
 
 
-def split(params: np.ndarray):
+def layers_of(arch: int):
+    return COMPACT_LAYERS if arch == 1 else LAYERS
+
+
+def split(params: np.ndarray, arch: int = 0):
     out, o = [], 0
-    for rows, cols in LAYERS:
+    for rows, cols in layers_of(arch):
         w = params[o:o + rows * cols].reshape(rows, cols)
         o += rows * cols
         b = params[o:o + rows]
         o += rows
         out.append((w, b))
-    assert o == N_PARAMS
+    assert o == (COMPACT_PARAMS if arch == 1 else N_PARAMS) == len(params)
     return out
 
 
@@ -48,17 +55,17 @@ def normalise(raw: np.ndarray) -> np.ndarray:
     return x
 
 
-def forward(params: np.ndarray, raw: np.ndarray, half: bool = True):
+def forward(params: np.ndarray, raw: np.ndarray, half: bool = True, arch: int = 0):
     """Network outputs (n, 16; columns 12..15 are padding) and the activations."""
     # The kernels round the FP32 master weights to FP16; the smooth network keeps FP64.
     base = np.asarray(params, np.float32) if half else np.asarray(params, np.float64)
-    layers = [(_h(w, half), np.asarray(b, dtype=np.float64)) for w, b in split(base)]
+    layers = [(_h(w, half), np.asarray(b, dtype=np.float64)) for w, b in split(base, arch)]
     x = _h(normalise(raw), half)
     acts = [x]
     h = x
     for k, (w, b) in enumerate(layers):
         z = h @ w.T + b
-        if k < 4:
+        if k < len(layers) - 1:
             h = _h(np.maximum(z, 0.0), half)
             acts.append(h)
         else:
@@ -66,16 +73,16 @@ def forward(params: np.ndarray, raw: np.ndarray, half: bool = True):
     return h, acts, layers
 
 
-def gradients(params: np.ndarray, raw: np.ndarray, targets: np.ndarray, half: bool = True):
-    """(flat gradient float64[N_PARAMS], loss) of sum((y - t)^2) over the 12 outputs."""
-    y, acts, layers = forward(params, raw, half)
+def gradients(params: np.ndarray, raw: np.ndarray, targets: np.ndarray, half: bool = True, arch: int = 0):
+    """(flat gradient float64[len(params)], loss) of sum((y - t)^2) over the 12 outputs."""
+    y, acts, layers = forward(params, raw, half, arch)
     t = np.asarray(targets, dtype=np.float64).reshape(-1, N_OUT)
     d = np.zeros_like(y)
     d[:, :N_OUT] = y[:, :N_OUT] - t
     loss = float((d * d).sum())
     dz = 2.0 * d
-    grads = [None] * 5
-    for k in range(4, -1, -1):
+    grads = [None] * len(layers)
+    for k in range(len(layers) - 1, -1, -1):
         w, _ = layers[k]
         grads[k] = (dz.T @ acts[k], dz.sum(axis=0))
         if k > 0:

@@ -374,3 +374,181 @@ def test_shipped_surrogate_beats_the_karis_fit(renderer):
     s.close()
     assert ev["karis_bsdf"] > 0.2
     assert ev["surrogate_bsdf"] < 0.25 * ev["karis_bsdf"], ev
+
+
+# ------------------------------------------------------------------ compact network (shade model 3)
+
+COMPACT = abi.MLP_ARCH_COMPACT
+
+
+def test_compact_fp64_reference_matches_finite_differences():
+    p = S.init_params(13, COMPACT).astype(np.float64)
+    x = _inputs(48, 14)
+    t = np.random.default_rng(15).normal(size=(48, 12))
+    g, _ = mlp_ref.gradients(p, x, t, half=False, arch=COMPACT)
+    assert g.shape == (abi.MLP_COMPACT_PARAMS,)
+    for idx in (5, 300, 520, 700, 1500, 1570, 1700, 2100, 2115):
+        e = 1e-6
+        a, b = p.copy(), p.copy()
+        a[idx] += e
+        b[idx] -= e
+        fd = (mlp_ref.gradients(a, x, t, half=False, arch=COMPACT)[1]
+              - mlp_ref.gradients(b, x, t, half=False, arch=COMPACT)[1]) / (2 * e)
+        assert abs(fd - g[idx]) <= 1e-6 * max(1.0, abs(fd)), (idx, fd, g[idx])
+
+
+def test_compact_oracle_emulation_matches_fp64_reference():
+    p = S.init_params(16, COMPACT)
+    x = _inputs(256, 17)
+    got = oracle.mlp_forward(p, x, arch=COMPACT)
+    want, _, _ = mlp_ref.forward(p, x, arch=COMPACT)
+    np.testing.assert_allclose(got, want[:, :12], rtol=0, atol=3e-3)
+    # the two architectures are different functions of the same inputs
+    assert np.abs(oracle.mlp_forward(S.init_params(16), x) - got).max() > 1e-2
+
+
+def test_compact_init_params_keep_padding_zero():
+    p = S.init_params(0, COMPACT)
+    layers = S.split(p, COMPACT)
+    assert [w.shape for w, _ in layers] == [(32, 16), (32, 32), (16, 32)]
+    assert (layers[0][0][:, 10:] == 0).all()
+    assert (layers[2][0][12:, :] == 0).all() and (layers[2][1] == 0).all()
+
+
+def test_shipped_compact_weights_have_the_parameter_layout():
+    p = S.load_params(COMPACT)
+    assert p.shape == (abi.MLP_COMPACT_PARAMS,) and np.isfinite(p).all()
+    layers = S.split(p, COMPACT)
+    assert (layers[0][0][:, 10:] == 0).all() and (layers[2][0][12:, :] == 0).all()
+
+
+@gpu
+def test_compact_surrogate_entry_points_check_the_architecture(renderer):
+    s = S.Surrogate(renderer, None, COMPACT)
+    assert s.n_params == abi.MLP_COMPACT_PARAMS
+    with pytest.raises(abi.HairGbError):
+        s.set_params(S.init_params(0))  # 4 x 64 parameter count
+    torch, dev = _torch()
+    x = torch.from_numpy(_inputs(64, 18)).to(dev)
+    out = torch.empty((64, 12), dtype=torch.float32, device=dev)
+    with pytest.raises(abi.HairGbError):
+        s.infer_tc(x, 64, out)  # tcgen05 inference is for the 4 x 64 network
+    s.close()
+    with pytest.raises(abi.HairGbError):
+        S.Surrogate(renderer, None, 7)
+
+
+@gpu
+@pytest.mark.parametrize("which", ["init", "shipped"])
+def test_compact_forward_matches_the_oracle_emulation(renderer, which):
+    torch, dev = _torch()
+    p = S.init_params(19, COMPACT) if which == "init" else S.load_params(COMPACT)
+    s = S.Surrogate(renderer, p, COMPACT)
+    for n in (5000, 77):
+        xs = _inputs(n, 20)
+        x = torch.from_numpy(xs).to(dev)
+        net = torch.full((n, 12), float("nan"), dtype=torch.float32, device=dev)
+        lob = torch.empty((n, 12), dtype=torch.float32, device=dev)
+        s.infer(x, n, lob, net)
+        assert renderer.synchronize() == 0
+        got, want = net.cpu().numpy(), oracle.mlp_forward(p, xs, arch=COMPACT)
+        assert np.isfinite(got).all()
+        assert np.abs(got - want).mean() < 1e-3
+        np.testing.assert_allclose(got, want, rtol=0, atol=3e-2)
+        np.testing.assert_allclose(lob.cpu().numpy(), 1e-3 * np.expm1(np.maximum(got, 0)), rtol=1e-5, atol=1e-9)
+    s.close()
+
+
+@gpu
+def test_compact_gradients_match_the_fp64_reference(renderer):
+    torch, dev = _torch()
+    n = 3000  # not a multiple of 32: the ragged last block must contribute nothing extra
+    x = torch.empty((n, 10), dtype=torch.float32, device=dev)
+    t = torch.empty((n, 12), dtype=torch.float32, device=dev)
+    S.samples(renderer, 78, 0, n, x, t)
+    p = S.init_params(21, COMPACT)
+    s = S.Surrogate(renderer, p, COMPACT)
+    g, loss = s.gradients(x, t, n)
+    xs, ts = x.cpu().numpy(), t.cpu().numpy()
+    want, want_loss = mlp_ref.gradients(p, xs, ts, arch=COMPACT)
+    assert loss == pytest.approx(want_loss, rel=1e-3)
+    # the backward pass runs in FP32 from the FP16-rounded forward activations
+    err = np.linalg.norm(g - want) / np.linalg.norm(want)
+    cos = float(g @ want / (np.linalg.norm(g) * np.linalg.norm(want)))
+    assert err < 5e-3 and cos > 0.99999, (err, cos)
+    for k, ((gw, gb), (ww, wb)) in enumerate(zip(S.split(g, COMPACT), S.split(want.astype(np.float32), COMPACT))):
+        assert np.linalg.norm(gw - ww) <= 1e-2 * np.linalg.norm(ww) + 1e-6, k
+        assert np.linalg.norm(gb - wb) <= 1e-2 * np.linalg.norm(wb) + 1e-6, k
+    assert (S.split(g, COMPACT)[0][0][:, 10:] == 0).all() and (S.split(g, COMPACT)[2][0][12:, :] == 0).all()
+    np.testing.assert_array_equal(s.get_params(), p)
+    s.close()
+
+
+@gpu
+def test_compact_training_reduces_the_loss(renderer):
+    torch, dev = _torch()
+    n, batch = 1 << 18, 8192
+    x = torch.empty((n, 10), dtype=torch.float32, device=dev)
+    t = torch.empty((n, 12), dtype=torch.float32, device=dev)
+    S.samples(renderer, 98, 0, n, x, t)
+    s = S.Surrogate(renderer, S.init_params(22, COMPACT), COMPACT)
+    steps = 300
+    losses = torch.zeros(steps, dtype=torch.float32, device=dev)
+    for k in range(steps):
+        lo = (k % (n // batch)) * batch
+        s.train_step(x[lo:lo + batch], t[lo:lo + batch], batch, 3e-3, losses[k:k + 1])
+    renderer.synchronize()
+    l = losses.cpu().numpy() / (batch * 12)
+    assert np.isfinite(l).all()
+    assert l[-20:].mean() < 0.25 * l[:5].mean(), (l[:5], l[-20:])
+    p = s.get_params()
+    assert (S.split(p, COMPACT)[0][0][:, 10:] == 0).all() and (S.split(p, COMPACT)[2][0][12:, :] == 0).all()
+    s.close()
+
+
+@gpu
+def test_shade_model_three_matches_the_oracle(renderer):
+    sc = configs.config2(scale=0.02)
+    cam, dom = sc.params()
+    lights = sc.light_array()
+    w, h = sc.view.width, sc.view.height
+    renderer.ensure_targets(w, h, *sc.dom_size)
+    g = renderer.upload(sc.mesh)
+    renderer.render_groom(g, cam, dom, lights)
+    assert renderer.synchronize() == 0
+    deep = S.Surrogate(renderer, S.load_params())
+    renderer.bind_surrogate(deep)
+    with pytest.raises(abi.HairGbError):
+        renderer.shade(cam, lights, model=abi.SHADE_SURROGATE_COMPACT)  # model 3 takes the compact network
+    p = S.load_params(COMPACT)
+    s = S.Surrogate(renderer, p, COMPACT)
+    renderer.bind_surrogate(s)
+    with pytest.raises(abi.HairGbError):
+        renderer.shade(cam, lights, model=abi.SHADE_SURROGATE_MMA)  # models 1 and 2 take the 4 x 64 one
+    renderer.shade(cam, lights, model=abi.SHADE_SURROGATE_COMPACT)
+    assert renderer.synchronize() == 0
+    center, beta, dmap = renderer.read(abi.BUF_CENTER), renderer.read(abi.BUF_BETA), renderer.read(abi.BUF_DOM)
+    shaded, sdepth = renderer.read(abi.BUF_SHADED), renderer.read(abi.BUF_SHADED_DEPTH)
+    o_shaded, o_sdepth = oracle.shade(cam, center, beta, dmap, lights, mlp=p, mlp_arch=COMPACT)
+    hit = center != EMPTY
+    assert hit.sum() > 50
+    np.testing.assert_array_equal(sdepth, o_sdepth)
+    assert np.isfinite(shaded).all()
+    got, want = shaded.reshape(-1, 4)[hit, :3], o_shaded.reshape(-1, 4)[hit, :3]
+    assert S.relative_l1(got, want) < 2e-3
+    np.testing.assert_allclose(got, want, rtol=3e-2, atol=1e-3 * np.abs(want).max())
+    renderer.render_groom(g, cam, dom, lights, model=abi.SHADE_SURROGATE_COMPACT)
+    assert renderer.synchronize() == 0
+    np.testing.assert_array_equal(renderer.read(abi.BUF_SHADED), shaded)
+    renderer.bind_surrogate(None)
+    s.close()
+    deep.close()
+    g.close()
+
+
+@gpu
+def test_shipped_compact_surrogate_beats_the_karis_fit(renderer):
+    s = S.Surrogate(renderer, S.load_params(COMPACT), COMPACT)
+    ev = S.evaluate(renderer, s, n=1 << 15)
+    s.close()
+    assert ev["surrogate_bsdf"] < 0.75 * ev["karis_bsdf"], ev
