@@ -772,11 +772,17 @@ __global__ void karis_lobes_kernel(const float* __restrict__ in, uint32_t n, flo
 
 constexpr uint32_t kLightsPerStep = 1;
 
-// Pixels whose centre word is not empty, appended in warp order; the others
-// get the empty shade outputs.
-__global__ void hair_list_kernel(const unsigned long long* __restrict__ center, uint32_t pixels,
-                                 uint32_t* __restrict__ list, uint32_t* __restrict__ count,
-                                 float4* __restrict__ shaded, float* __restrict__ shaded_depth) {
+// Pixels whose centre word is not empty, appended in block order (one
+// atomic per block of kHairListThreads pixels, ordered within the block);
+// the others get the empty shade outputs.
+constexpr int kHairListThreads = 512;
+
+__global__ void __launch_bounds__(kHairListThreads) hair_list_kernel(const unsigned long long* __restrict__ center,
+                                                                      uint32_t pixels, uint32_t* __restrict__ list,
+                                                                      uint32_t* __restrict__ count,
+                                                                      float4* __restrict__ shaded,
+                                                                      float* __restrict__ shaded_depth) {
+    __shared__ uint32_t warp_base[kHairListThreads / 32 + 1];
     const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
     bool hair = false;
     if (pix < pixels) {
@@ -786,12 +792,21 @@ __global__ void hair_list_kernel(const unsigned long long* __restrict__ center, 
             shaded_depth[pix] = 0.0f;
         }
     }
-    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t m = __ballot_sync(0xffffffffu, hair);
-    uint32_t base = 0;
-    if (lane == 0 && m) base = atomicAdd(count, (uint32_t)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (hair) list[base + __popc(m & ((1u << lane) - 1u))] = pix;
+    if (lane == 0) warp_base[warp] = (uint32_t)__popc(m);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t sum = 0;
+        for (uint32_t w = 0; w < blockDim.x / 32u; ++w) {
+            const uint32_t c = warp_base[w];
+            warp_base[w] = sum;
+            sum += c;
+        }
+        warp_base[kHairListThreads / 32] = sum ? atomicAdd(count, sum) : 0u;
+    }
+    __syncthreads();
+    if (hair) list[warp_base[kHairListThreads / 32] + warp_base[warp] + __popc(m & ((1u << lane) - 1u))] = pix;
 }
 
 __global__ void __launch_bounds__(mlp::tc::kThreads, 1)
@@ -965,10 +980,11 @@ __device__ __forceinline__ void mma_c(float d[4], const uint32_t a[4], uint32_t 
         : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1), "f"(c.x), "f"(c.y), "f"(c.z), "f"(c.w));
 }
 
-// One layer: acc[mt][nt] = bias + A[mt] * W^T, N = 8 NT outputs, K = 16 KT inputs.
-template <int NT, int KT, int PAD>
-__device__ __forceinline__ void compact_layer(float acc[2][NT][4], const uint32_t a[2][KT][4],
-                                              const __half (*w)[PAD], const float4 (*bq)[4], int lane) {
+// One layer for MT m-tiles: acc[mt][nt] = bias + A[mt] * W^T, N = 8 NT
+// outputs, K = 16 KT inputs.
+template <int MT, int NT, int KT, int PAD>
+__device__ __forceinline__ void compact_layer(float acc[][NT][4], const uint32_t a[][KT][4], const __half (*w)[PAD],
+                                              const float4 (*bq)[4], int lane) {
     const int t = lane & 3, mat = lane >> 3, r = lane & 7;
 #pragma unroll
     for (int kt = 0; kt < KT; ++kt) {
@@ -976,28 +992,46 @@ __device__ __forceinline__ void compact_layer(float acc[2][NT][4], const uint32_
         for (int nt = 0; nt < NT; nt += 2) {
             uint32_t b[4];
             mlp::ldsm_x4(b, &w[(nt + (mat >> 1)) * 8 + r][kt * 16 + (mat & 1) * 8]);
-            if (kt == 0) {
-                const float4 c0 = bq[nt][t], c1 = bq[nt + 1][t];
-                mma_c(acc[0][nt], a[0][0], b[0], b[1], c0);
-                mma_c(acc[1][nt], a[1][0], b[0], b[1], c0);
-                mma_c(acc[0][nt + 1], a[0][0], b[2], b[3], c1);
-                mma_c(acc[1][nt + 1], a[1][0], b[2], b[3], c1);
-            } else {
-                mlp::mma(acc[0][nt], a[0][kt], b[0], b[1]);
-                mlp::mma(acc[1][nt], a[1][kt], b[0], b[1]);
-                mlp::mma(acc[0][nt + 1], a[0][kt], b[2], b[3]);
-                mlp::mma(acc[1][nt + 1], a[1][kt], b[2], b[3]);
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt) {
+                if (kt == 0) {
+                    mma_c(acc[mt][nt], a[mt][0], b[0], b[1], bq[nt][t]);
+                    mma_c(acc[mt][nt + 1], a[mt][0], b[2], b[3], bq[nt + 1][t]);
+                } else {
+                    mlp::mma(acc[mt][nt], a[mt][kt], b[0], b[1]);
+                    mlp::mma(acc[mt][nt + 1], a[mt][kt], b[2], b[3]);
+                }
             }
         }
     }
 }
+
+// C fragments of a 32-wide layer -> ReLU -> FP16 A fragments of the next.
+template <int MT>
+__device__ __forceinline__ void compact_relu(const float acc[][4][4], uint32_t a[][2][4]) {
+#pragma unroll
+    for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+        for (int kt = 0; kt < 2; ++kt) {
+            const float* lo = acc[mt][2 * kt];
+            const float* hi = acc[mt][2 * kt + 1];
+            a[mt][kt][0] = mlp::pack_relu(lo[0], lo[1]);
+            a[mt][kt][1] = mlp::pack_relu(lo[2], lo[3]);
+            a[mt][kt][2] = mlp::pack_relu(hi[0], hi[1]);
+            a[mt][kt][3] = mlp::pack_relu(hi[2], hi[3]);
+        }
+}
+
+// m-tiles evaluated together (2) or one after the other (1): one after the
+// other leaves room for three blocks per SM.
+constexpr int kCompactTiles = 1;
 
 __device__ __forceinline__ float4 bias_quad(const float* b, int nt, int t) {
     const float lo = b[nt * 8 + 2 * t], hi = b[nt * 8 + 2 * t + 1];
     return make_float4(lo, hi, lo, hi);
 }
 
-__global__ void __launch_bounds__(kCompactWarps * 32, 2)
+__global__ void __launch_bounds__(kCompactWarps * 32, 3)
     shade_compact_kernel(const ShadeArgs a, const __half* __restrict__ w16, const float* __restrict__ mparams,
                          const EnvArgs env, const uint32_t* __restrict__ list, const uint32_t* __restrict__ count) {
     __shared__ __align__(16) CompactSmem sm;
@@ -1041,12 +1075,27 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2)
         }
     const uint32_t n = *count;
     const uint32_t chunks = (n + 31u) >> 5;
-    for (uint32_t ch = blockIdx.x * kCompactWarps + warp; ch < chunks; ch += gridDim.x * kCompactWarps) {
-        const uint32_t idx = ch * 32u + lane;
-        const bool active = idx < n;
-        const uint32_t pix = active ? __ldg(&list[idx]) : 0u;
+    const uint32_t stride = gridDim.x * kCompactWarps;
+    // Loads run ahead of the shading: list entries two chunks, centre and
+    // beta words one chunk.
+    constexpr uint32_t kNone = 0xffffffffu;
+    auto list_at = [&](uint32_t c) -> uint32_t {
+        return c < chunks && c * 32u + lane < n ? __ldg(&list[c * 32u + lane]) : kNone;
+    };
+    uint32_t ch = blockIdx.x * kCompactWarps + warp;
+    uint32_t pix_next = list_at(ch), pix_after = list_at(ch + stride);
+    unsigned long long word_next = pix_next != kNone ? __ldg(&a.center[pix_next]) : 0ull;
+    uint32_t beta_next = pix_next != kNone ? __ldg(&a.beta[pix_next]) : 0u;
+    for (; ch < chunks; ch += stride) {
+        const bool active = pix_next != kNone;
+        const uint32_t pix = active ? pix_next : 0u;
+        const unsigned long long word = word_next;
+        const uint32_t beta_word = beta_next;
+        word_next = pix_after != kNone ? __ldg(&a.center[pix_after]) : 0ull;
+        beta_next = pix_after != kNone ? __ldg(&a.beta[pix_after]) : 0u;
+        pix_next = pix_after;
+        pix_after = list_at(ch + 2 * stride);
         const uint32_t x = pix % width, y = pix / width;
-        const unsigned long long word = active ? __ldg(&a.center[pix]) : 0ull;
         const uint32_t low = (uint32_t)word, high = (uint32_t)(word >> 32);
         const float view_dist = dequantize_depth(high >> 8u, p.screen[2], p.screen[3]);
         const f3 world = reconstruct_world(p, (int32_t)x, (int32_t)y, view_dist);
@@ -1092,7 +1141,7 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2)
         float dom_direct = 1.0f;
         if (dom_light >= 0 && active) {
             const hg_light& L = sm.lights[dom_light];
-            const float beta = (float)(__ldg(&a.beta[pix]) & 0xffu) / 255.0f;
+            const float beta = (float)(beta_word & 0xffu) / 255.0f;
             const float depth = -logf(fmaxf(dom_visibility(p, a.dom, world, beta), 1e-6f));
             dom_direct = expf(-depth);
             if (depth > 1e-3f) {
@@ -1118,30 +1167,36 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2)
             st_h2(&xr[lane][0], sin_i, sin_o);
             st_h2(&xr[lane][2], cos_phi, sqrtf(fmaxf(1.0f - cos_phi * cos_phi, 0.0f)));
             __syncwarp();
-            uint32_t a0[2][1][4];
-#pragma unroll
-            for (int mt = 0; mt < 2; ++mt) {
-                a0[mt][0][0] = mlp::ld32(&xr[4 * g + 2 * mt][2 * t]);
-                a0[mt][0][1] = mlp::ld32(&xr[4 * g + 2 * mt + 1][2 * t]);
-                a0[mt][0][2] = a_hi[mt][0];
-                a0[mt][0][3] = a_hi[mt][1];
-            }
-            float acc[2][4][4];
-            uint32_t ah[2][2][4];
-            compact_layer<4, 1, mlps::kPadIn>(acc, a0, sm.w1, sm.bq1, (int)lane);
-            mlps::relu_to_a(acc, ah);
-            compact_layer<4, 2, mlps::kPadHid>(acc, ah, sm.w2, sm.bq2, (int)lane);
-            mlps::relu_to_a(acc, ah);
-            float out[2][2][4];
-            compact_layer<2, 2, mlps::kPadHid>(out, ah, sm.w3, sm.bq3, (int)lane);
             // part[k]: lobe t's rgb in network row g + 8k (columns 2t, 2t+1, 8+2t)
             float part[4][3];
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-                const int mt = k >> 1, h = k & 1;
-                const float y3[3] = {out[mt][0][2 * h], out[mt][0][2 * h + 1], out[mt][1][2 * h]};
+            for (int m0 = 0; m0 < 2; m0 += kCompactTiles) {
+                uint32_t a0[kCompactTiles][1][4];
 #pragma unroll
-                for (int c = 0; c < 3; ++c) part[k][c] = fmaf(lobe_w, __expf(fmaxf(y3[c], 0.0f)), -lobe_w);
+                for (int q = 0; q < kCompactTiles; ++q) {
+                    const int mt = m0 + q;
+                    a0[q][0][0] = mlp::ld32(&xr[4 * g + 2 * mt][2 * t]);
+                    a0[q][0][1] = mlp::ld32(&xr[4 * g + 2 * mt + 1][2 * t]);
+                    a0[q][0][2] = a_hi[mt][0];
+                    a0[q][0][3] = a_hi[mt][1];
+                }
+                float acc[kCompactTiles][4][4];
+                uint32_t ah[kCompactTiles][2][4];
+                compact_layer<kCompactTiles, 4, 1, mlps::kPadIn>(acc, a0, sm.w1, sm.bq1, (int)lane);
+                compact_relu<kCompactTiles>(acc, ah);
+                compact_layer<kCompactTiles, 4, 2, mlps::kPadHid>(acc, ah, sm.w2, sm.bq2, (int)lane);
+                compact_relu<kCompactTiles>(acc, ah);
+                float out[kCompactTiles][2][4];
+                compact_layer<kCompactTiles, 2, 2, mlps::kPadHid>(out, ah, sm.w3, sm.bq3, (int)lane);
+#pragma unroll
+                for (int q = 0; q < kCompactTiles; ++q)
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const int k = 2 * (m0 + q) + h;
+                        const float y3[3] = {out[q][0][2 * h], out[q][0][2 * h + 1], out[q][1][2 * h]};
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) part[k][c] = fmaf(lobe_w, __expf(fmaxf(y3[c], 0.0f)), -lobe_w);
+                    }
             }
             // reduce-scatter over the quad: lane t keeps row slot t
             const bool hi = (t >> 1) != 0, lo = (t & 1) != 0;
@@ -1165,15 +1220,38 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 2)
         }
         if (active) {
             if (env.spec) {
-                const f3 fiber_n = safe_normalize(sub3(view, mul3s(tangent, dot3(view, tangent))));
-                const f3 pr = probe_radiance(env, tangent, fiber_n, view, albedo, roughness, p.appearance[1]);
-                color = add3(color, mul3s(pr, pixel_ao(p, low)));
+                // the probe's inputs again from the centre word (fewer registers live across the light loop)
+                const uint32_t lw = (uint32_t)word, hw = (uint32_t)(word >> 32);
+                const f3 tg = oct_decode(hw & 0xffu, lw >> 24u);
+                const float uz = (float)((lw >> 6u) & 0x3fu) / 63.0f;
+                const float rough = fmaxf(p.appearance[0] * (0.65f + 0.7f * uz), 0.04f);
+                const float as = 0.65f + 0.35f * uz;
+                const f3 alb = {p.albedo[0] * as, p.albedo[1] * as, p.albedo[2] * as};
+                f3 vw;
+                if (a.ortho) {
+                    vw = safe_normalize(mk3(p.clip_from_world[2], p.clip_from_world[6], p.clip_from_world[10]));
+                } else {
+                    vw = safe_normalize(sub3(ld3(p.camera_pos), world));
+                }
+                const f3 fiber_n = safe_normalize(sub3(vw, mul3s(tg, dot3(vw, tg))));
+                const f3 pr = probe_radiance(env, tg, fiber_n, vw, alb, rough, p.appearance[1]);
+                color = add3(color, mul3s(pr, pixel_ao(p, lw)));
             }
             color = mul3s(color, a.exposure);
             a.shaded[pix] = make_float4(color.x, color.y, color.z, 1.0f);
-            a.shaded_depth[pix] = view_dist;
+            a.shaded_depth[pix] = dequantize_depth((uint32_t)(word >> 40), p.screen[2], p.screen[3]);
         }
     }
+}
+
+// The hair-pixel list of shade models 1 and 3 (and the empty pixels' outputs).
+cudaError_t launch_hair_list(hg_ctx* ctx) {
+    const uint32_t pixels = ctx->width * ctx->height;
+    cudaError_t e = cudaMemsetAsync(ctx->hair_count, 0, sizeof(uint32_t), ctx->stream);
+    if (e != cudaSuccess) return e;
+    hair_list_kernel<<<(pixels + kHairListThreads - 1) / kHairListThreads, kHairListThreads, 0, ctx->stream>>>(
+        ctx->center, pixels, ctx->hair_list, ctx->hair_count, ctx->shaded, ctx->shaded_depth);
+    return cudaGetLastError();
 }
 
 std::mutex g_surrogate_attr_mutex;
@@ -1244,13 +1322,8 @@ cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights
                 g_tc_attr[ctx->device] = true;
             }
         }
-        const uint32_t pixels = ctx->width * ctx->height;
-        cudaError_t e = cudaMemsetAsync(ctx->hair_count, 0, sizeof(uint32_t), ctx->stream);
+        cudaError_t e = launch_hair_list(ctx);
         if (e != cudaSuccess) return e;
-        hair_list_kernel<<<(pixels + 255u) / 256u, 256, 0, ctx->stream>>>(ctx->center, pixels, ctx->hair_list,
-                                                                          ctx->hair_count, ctx->shaded,
-                                                                          ctx->shaded_depth);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
         // one CTA per SM: it holds all 512 TMEM columns and most of the shared memory
         shade_tc_kernel<<<ctx->sm_count, mlp::tc::kThreads, mlp::tc::kSmemBytes, ctx->stream>>>(
             a, reinterpret_cast<const __half*>(ctx->surrogate->w16), ctx->surrogate->params, env, ctx->hair_list,
@@ -1282,14 +1355,10 @@ cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights
     }
     if (model == 3u) {
         const uint32_t pixels = ctx->width * ctx->height;
-        cudaError_t e = cudaMemsetAsync(ctx->hair_count, 0, sizeof(uint32_t), ctx->stream);
+        cudaError_t e = launch_hair_list(ctx);
         if (e != cudaSuccess) return e;
-        hair_list_kernel<<<(pixels + 255u) / 256u, 256, 0, ctx->stream>>>(ctx->center, pixels, ctx->hair_list,
-                                                                          ctx->hair_count, ctx->shaded,
-                                                                          ctx->shaded_depth);
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-        // two resident blocks per SM (the kernel's launch bounds), grid-striding over 32-pixel chunks
-        uint32_t blocks = (uint32_t)ctx->sm_count * 2u;
+        // three resident blocks per SM (the kernel's launch bounds), grid-striding over 32-pixel chunks
+        uint32_t blocks = (uint32_t)ctx->sm_count * 3u;
         const uint32_t max_chunks = (pixels + 31u) / 32u;
         const uint32_t needed = (max_chunks + kCompactWarps - 1) / kCompactWarps;
         if (blocks > needed) blocks = needed;

@@ -246,7 +246,7 @@ def train(renderer: HairRenderer, n_samples: int = 16 << 20, batch: int = 16384,
             "steps": steps, "batch": batch, "epochs": epochs,
             "samples": n_samples, "final_mse": losses[-n_batches:].mean().item() / (batch * 12),
             "first_mse": losses[:min(50, steps)].mean().item() / (batch * 12)}
-    hist.update(evaluate(renderer, s))
+    hist["heldout"] = evaluate(renderer, s)
     s.close()
     return params, hist
 
