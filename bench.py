@@ -220,7 +220,7 @@ def tensor_peak() -> tuple[float, str]:
 
 
 MLP_FLOP_PER_EVAL = 27392  # 2 * (10*64 + 3*64*64 + 64*12)
-COMPACT_FLOP_PER_EVAL = 3456  # 2 * (10*32 + 32*32 + 32*12)
+COMPACT_FLOP_PER_EVAL = 2752  # 2 * (10*32 + 32*32 + 32*3)
 
 
 def surrogate_section(r, cam, lights, flush, stream, reps: int, karis_ms: float, hair_px: int) -> dict | None:
@@ -272,13 +272,12 @@ def surrogate_section(r, cam, lights, flush, stream, reps: int, karis_ms: float,
         r.bind_surrogate(None)
         c.close()
         compact = {
-            "network": "10 -> 32 -> 32 -> 12 (shade model 3, mma.sync m16n8k16, FP16 weights, FP32 accumulation)",
+            "network": "10 -> 32 -> 32 -> 3 BSDF channels (shade model 3, mma.sync m16n8k16, FP16 weights, "
+                       "FP32 accumulation)",
             "shade_ms": round(ms_c, 4), "ratio_vs_karis": round(ms_c / karis_ms, 3),
             "flop_per_eval": COMPACT_FLOP_PER_EVAL,
             "achieved_tflops": round(evals * COMPACT_FLOP_PER_EVAL / (ms_c * 1e-3) / 1e12, 2),
-            "error": {"surrogate": round(ev_c["surrogate_bsdf"], 5), "karis": round(ev_c["karis_bsdf"], 5),
-                      "per_lobe": {k: round(v, 5) for k, v in ev_c.items() if k.startswith("surrogate_")
-                                   and not k.endswith("bsdf")}},
+            "error": {"surrogate": round(ev_c["surrogate_bsdf"], 5), "karis": round(ev_c["karis_bsdf"], 5)},
         }
     return {
         "shade_ms": round(ms, 4), "karis_shade_ms": round(karis_ms, 4), "ratio_vs_karis": round(ms / karis_ms, 3),

@@ -21,6 +21,7 @@ MAX_LIGHTS = 256
 SCAN_NOALLOC_MAX_BUNDLES = 65536
 MLP_PARAMS = 14608
 MLP_COMPACT_PARAMS = 2128
+MLP_COMPACT_OUTPUTS = 3
 MLP_INPUTS = 10
 MLP_OUTPUTS = 12
 MLP_ARCH_DEEP, MLP_ARCH_COMPACT = 0, 1
@@ -223,6 +224,7 @@ _SIGNATURES = {
     "hg_mlp_create": (_I32, [_VP, C.POINTER(_VP)]),
     "hg_mlp_create_arch": (_I32, [_VP, _U32, C.POINTER(_VP)]),
     "hg_mlp_param_count": (_U32, [_VP]),
+    "hg_mlp_output_count": (_U32, [_VP]),
     "hg_mlp_destroy": (None, [_VP]),
     "hg_mlp_set_params": (_I32, [_VP, _VP, _U32]),
     "hg_mlp_get_params": (_I32, [_VP, _VP, _U32]),

@@ -1,13 +1,14 @@
-// The compact shading surrogate: 10 inputs -> 2 x 32 ReLU -> 12 outputs, the
-// same inputs, normalisation and output transform as the 4 x 64 network
-// (hg_mlp.cuh), FP16 weights and activations with FP32 accumulation on
-// mma.sync m16n8k16.  A network of this size already fits the FP64 lobes
-// better than the Karis fit does, at an eighth of the 4 x 64 network's
-// multiply-adds.
+// The compact shading surrogate: 10 inputs -> 2 x 32 ReLU -> 3 outputs, the
+// same inputs and normalisation as the 4 x 64 network (hg_mlp.cuh), FP16
+// weights and activations with FP32 accumulation on mma.sync m16n8k16.  It
+// predicts what the shade pass adds per light at zero deep-opacity depth,
+// the BSDF R + TT + TRT + 0.7 B per colour channel, as log1p(bsdf / 1e-3):
+// one value per channel instead of twelve lobes, which is what lets the
+// shading kernel decode a single row per lane.
 //
-// Parameter layout (float, HG_MLP_SMALL_PARAMS): W1[32][16] b1[32] W2[32][32]
-// b2[32] W3[16][32] b3[16]; W[out][in].  Inputs beyond 10 and outputs beyond
-// 12 are padding (zero weights, ignored).
+// Parameter layout (float, HG_MLP_COMPACT_PARAMS): W1[32][16] b1[32]
+// W2[32][32] b2[32] W3[16][32] b3[16]; W[out][in].  Inputs beyond 10 and
+// outputs beyond 3 are padding (zero weights, ignored).
 #pragma once
 
 #include "hg_mlp.cuh"
@@ -17,7 +18,9 @@ namespace mlps {
 
 constexpr int kIn = mlp::kIn;    // 16 (10 used)
 constexpr int kHid = 32;
-constexpr int kOut = mlp::kOut;  // 16 (12 used)
+constexpr int kOut = mlp::kOut;  // 16 (3 used)
+constexpr int kUsedOut = 3;
+constexpr float kBack = 0.7f;  // the shade pass's back-scattering density
 constexpr int kW1 = 0, kB1 = kW1 + kHid * kIn;
 constexpr int kW2 = kB1 + kHid, kB2 = kW2 + kHid * kHid;
 constexpr int kW3 = kB2 + kHid, kB3 = kW3 + kOut * kHid;
@@ -62,8 +65,8 @@ __device__ __forceinline__ void relu_to_a(const float acc[2][4][4], uint32_t a[2
 }
 
 // Forward pass of the 32 samples held by the warp's lanes (x: this lane's
-// normalised inputs; y: its 12 outputs in the transformed space).  Every lane
-// of the warp calls it.
+// normalised inputs; y: its outputs in the transformed space, the first
+// kUsedOut meaningful).  Every lane of the warp calls it.
 __device__ __forceinline__ void forward(const Weights& w, mlp::WarpIo& io, const float x[mlp::kUsedIn],
                                         float y[mlp::kUsedOut]) {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
@@ -93,6 +96,14 @@ struct TrainWeights {
 };
 
 __device__ __forceinline__ float round_half(float v) { return __half2float(__float2half_rn(v)); }
+
+// Training target of channel c from the twelve transformed FP64 lobes of
+// hg_mlp_samples (log1p(lobe / 1e-3)): log1p(bsdf / 1e-3) with bsdf =
+// R + TT + TRT + kBack * B.
+__device__ __forceinline__ float bsdf_target(const float* t12, int c) {
+    const float s = expm1f(t12[c]) + expm1f(t12[3 + c]) + expm1f(t12[6 + c]) + kBack * expm1f(t12[9 + c]);
+    return log1pf(s);
+}
 
 }  // namespace mlps
 }  // namespace hg

@@ -929,19 +929,18 @@ __global__ void __launch_bounds__(mlp::tc::kThreads, 1)
 }
 
 // ---------------------------------------------------------------- compact surrogate
-// Shade model 3: the compact 2 x 32 network (hg_mlp_small.cuh) on mma.sync.
-// The hair-pixel list of shade model 1 fills every lane: a warp shades 32
-// listed pixels and evaluates the network for all of them once per light.
+// Shade model 3: the compact 2 x 32 network (hg_mlp_small.cuh), whose three
+// outputs are the per-light BSDF rgb, on mma.sync.  The hair-pixel list of
+// shade model 1 fills every lane: a warp shades 32 listed pixels and
+// evaluates the network for all of them once per light.
 //
 // Layout choices that keep the light loop short:
-// * Lane L = 4g + t puts its pixel in network row g + 8t.  That is the row
-//   whose outputs a reduce-scatter over the lane's quad leaves in lane L, so
-//   the outputs are decoded and summed in the C-fragment layout without a
-//   trip through shared memory.
-// * The output layer's rows are permuted in shared memory so that lane t's
-//   C-fragment columns 2t, 2t+1 and 8+2t are the red, green and blue of lobe
-//   t (R, TT, TRT, B) and column 9+2t is padding: every lane decodes 12
-//   values and weighs them with one factor.
+// * Lane L = 4g + t puts its pixel in network row g + 8t, and the output
+//   layer's rows are duplicated in shared memory so that every lane's
+//   C-fragment columns 2t, 2t+1, 8+2t are red, green, blue (9+2t is zero):
+//   each lane then holds the three outputs of all four rows g + 8k of its
+//   fragments and keeps row g + 8t, its own pixel.  No shuffles, three
+//   exponentials per lane and light.
 // * Each pixel's inputs sit in shared row L (row stride 13 words: stores
 //   and the permuted fragment loads are both free of bank conflicts); the
 //   per-pixel inputs (sin theta_o, absorption, roughnesses, IOR) are written
@@ -951,20 +950,71 @@ __global__ void __launch_bounds__(mlp::tc::kThreads, 1)
 constexpr int kCompactWarps = 8;
 constexpr int kXPad = 26;  // halves per input row
 
+// A light with its per-light constants worked out once per block.
+struct CompactLight {
+    float4 pos;     // position, 1 / max(range^2, 1e-8)
+    float4 dir;     // direction (normalized for directional lights), kind as bits
+    float4 color;   // colour, spot scale
+    float4 normal;  // rect normal, spot offset
+    float4 rect;    // rect area (spot[0] * spot[1]), 1 / max(range^2, 1e-4), flags as bits, 0
+};
+
 struct CompactSmem {
     __half w1[mlps::kHid][mlps::kPadIn];
     __half w2[mlps::kHid][mlps::kPadHid];
-    __half w3[mlps::kOut][mlps::kPadHid];  // rows permuted, see above
+    __half w3[mlps::kOut][mlps::kPadHid];  // rows duplicated, see above
     float4 bq1[4][4], bq2[4][4], bq3[2][4];  // [n-tile][t]
     __half x[kCompactWarps][32][kXPad];
-    hg_light lights[HG_MAX_LIGHTS];
+    CompactLight lights[HG_MAX_LIGHTS];
 };
 
-// Output row of the network in physical column pc of the permuted layer.
+__device__ __forceinline__ CompactLight compact_light(const hg_light& L) {
+    CompactLight c;
+    const f3 dir = L.kind == HG_LIGHT_DIRECTIONAL ? safe_normalize(ld3(L.direction)) : ld3(L.direction);
+    const f3 nrm = safe_normalize(cross3(ld3(L.up), ld3(L.right)));
+    c.pos = make_float4(L.position[0], L.position[1], L.position[2], 1.0f / fmaxf(L.range * L.range, 1e-8f));
+    c.dir = make_float4(dir.x, dir.y, dir.z, __uint_as_float(L.kind));
+    c.color = make_float4(L.color[0], L.color[1], L.color[2], L.spot[0]);
+    c.normal = make_float4(nrm.x, nrm.y, nrm.z, L.spot[1]);
+    c.rect = make_float4(L.spot[0] * L.spot[1], 1.0f / fmaxf(L.range * L.range, 1e-4f), __uint_as_float(L.flags), 0.0f);
+    return c;
+}
+
+// light_weight with the per-light constants; l is the unit direction to the light.
+__device__ __forceinline__ float compact_weight(const CompactLight& c, f3 world, f3& l) {
+    const uint32_t kind = __float_as_uint(c.dir.w);
+    if (kind == HG_LIGHT_DIRECTIONAL) {
+        l = mk3(c.dir.x, c.dir.y, c.dir.z);
+        return 1.0f;
+    }
+    const f3 to_l = sub3(mk3(c.pos.x, c.pos.y, c.pos.z), world);
+    if (kind == HG_LIGHT_POINT || kind == HG_LIGHT_SPOT) {
+        const float dist2 = dot3(to_l, to_l);
+        l = safe_normalize(to_l);
+        float w = range_window(dist2, c.pos.w) / fmaxf(dist2, 1e-4f);
+        if (kind == HG_LIGHT_SPOT) {
+            const float cd = -dot3(mk3(c.dir.x, c.dir.y, c.dir.z), l);
+            const float sm = clampf(cd * c.color.w + c.normal.w, 0.0f, 1.0f);
+            w *= sm * sm;
+        }
+        return w;
+    }
+    if (kind == HG_LIGHT_RECT) {
+        const float dist2 = fmaxf(dot3(to_l, to_l), 1e-4f);
+        l = mul3s(to_l, rsqrtf(dist2));
+        const float facing = fmaxf(dot3(mk3(c.normal.x, c.normal.y, c.normal.z), l), 0.0f);
+        return c.rect.x * facing / dist2 * range_window(dist2, c.rect.y);
+    }
+    l = mk3(0.0f, 1.0f, 0.0f);
+    return 0.0f;
+}
+
+// Output row of the network in physical column pc of the duplicated layer:
+// red in even columns 0..6, green in odd columns 1..7, blue in even columns
+// 8..14, zero (padding row 15) in odd columns 9..15.
 __device__ __forceinline__ int compact_out_row(int pc) {
-    if (pc < 8) return 3 * (pc >> 1) + (pc & 1);
-    const int t = (pc - 8) >> 1;
-    return (pc & 1) ? 12 + t : 3 * t + 2;  // 12..15: zero padding rows
+    if (pc < 8) return pc & 1;
+    return (pc & 1) ? mlps::kOut - 1 : 2;
 }
 
 __device__ __forceinline__ void st_h2(__half* p, float lo, float hi) {
@@ -1054,22 +1104,21 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 3)
                 sm.bq3[nt][tt] = make_float4(lo, hi, lo, hi);
             }
         }
-        const uint32_t words = a.n_lights * (uint32_t)(sizeof(hg_light) / 4);
-        for (uint32_t i = tid; i < words; i += nth)
-            reinterpret_cast<uint32_t*>(sm.lights)[i] = __ldg(reinterpret_cast<const uint32_t*>(a.lights) + i);
+        for (uint32_t i = tid; i < a.n_lights; i += nth) sm.lights[i] = compact_light(a.lights[i]);
     }
     __syncthreads();
+    // Everything above reads only the weights and lights; the hair list
+    // comes from the kernel before (programmatic dependent launch).
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const hg_hair_params& p = a.p;
     const uint32_t width = f2u(p.screen[0]);
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const int g = (int)(lane >> 2), t = (int)(lane & 3u);
     __half(*xr)[kXPad] = sm.x[warp];
-    // lobe t's factor: the lobe scale, times the back-scattering density for B
-    const float lobe_w = t == 3 ? mlp::kScale * kDensityBack : mlp::kScale;
     // The light that receives the deep-opacity depth (shade.wesl:486-503).
     int dom_light = -1;
     for (uint32_t i = 0; i < a.n_lights; ++i)
-        if (sm.lights[i].kind == HG_LIGHT_DIRECTIONAL && (sm.lights[i].flags & HG_LIGHT_CASTS_SHADOWS)) {
+        if (a.lights[i].kind == HG_LIGHT_DIRECTIONAL && (a.lights[i].flags & HG_LIGHT_CASTS_SHADOWS)) {
             dom_light = (int)i;
             break;
         }
@@ -1140,26 +1189,28 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 3)
         f3 color = spl(0.0f);
         float dom_direct = 1.0f;
         if (dom_light >= 0 && active) {
-            const hg_light& L = sm.lights[dom_light];
+            const CompactLight& L = sm.lights[dom_light];
             const float beta = (float)(beta_word & 0xffu) / 255.0f;
             const float depth = -logf(fmaxf(dom_visibility(p, a.dom, world, beta), 1e-6f));
             dom_direct = expf(-depth);
             if (depth > 1e-3f) {
                 const float tv = dot3(tangent, view);
                 const Dual ds = dual_scatter(sqrtf(fmaxf(1.0f - tv * tv, 1e-6f)), sigma_a, shape);
-                const Geometry gm = light_geometry(t_n, v_n, ld3(L.direction));
-                color = vmul(spread_term(shape, ds, gm.theta_h, depth, dom_direct), ld3(L.color));
+                const Geometry gm = light_geometry(t_n, v_n, mk3(L.dir.x, L.dir.y, L.dir.z));
+                color = vmul(spread_term(shape, ds, gm.theta_h, depth, dom_direct),
+                             mk3(L.color.x, L.color.y, L.color.z));
             }
         }
         for (uint32_t i = 0; i < a.n_lights; ++i) {
-            const hg_light& L = sm.lights[i];
-            f3 incident;
-            float weight = light_weight(L, world, incident);
+            const CompactLight& L = sm.lights[i];
+            // unit direction to the light (normalized once, where the
+            // reference normalizes the already unit vector a second time)
+            f3 l;
+            float weight = compact_weight(L, world, l);
             if ((int)i == dom_light) weight = dom_direct;
             const bool use = active && weight > 0.0f;
             if (!__any_sync(0xffffffffu, use)) continue;
             // sin theta_i and cos phi as light_geometry computes them
-            const f3 l = safe_normalize(incident);
             const float sin_i = clampf(dot3(t_n, l), -1.0f, 1.0f);
             const f3 t_i = sub3(l, mul3s(t_n, sin_i));
             const float cos_phi = clampf(dot3(t_i, t_o) * rsqrtf(fmaxf(dot3(t_i, t_i) * to2, 1e-8f)), -1.0f, 1.0f);
@@ -1167,8 +1218,8 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 3)
             st_h2(&xr[lane][0], sin_i, sin_o);
             st_h2(&xr[lane][2], cos_phi, sqrtf(fmaxf(1.0f - cos_phi * cos_phi, 0.0f)));
             __syncwarp();
-            // part[k]: lobe t's rgb in network row g + 8k (columns 2t, 2t+1, 8+2t)
-            float part[4][3];
+            // this lane's row is g + 8t: m-tile t >> 1, half t & 1 of its fragments
+            float yr = 0.0f, yg = 0.0f, yb = 0.0f;
 #pragma unroll
             for (int m0 = 0; m0 < 2; m0 += kCompactTiles) {
                 uint32_t a0[kCompactTiles][1][4];
@@ -1190,33 +1241,15 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 3)
                 compact_layer<kCompactTiles, 2, 2, mlps::kPadHid>(out, ah, sm.w3, sm.bq3, (int)lane);
 #pragma unroll
                 for (int q = 0; q < kCompactTiles; ++q)
-#pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        const int k = 2 * (m0 + q) + h;
-                        const float y3[3] = {out[q][0][2 * h], out[q][0][2 * h + 1], out[q][1][2 * h]};
-#pragma unroll
-                        for (int c = 0; c < 3; ++c) part[k][c] = fmaf(lobe_w, __expf(fmaxf(y3[c], 0.0f)), -lobe_w);
+                    if ((t >> 1) == m0 + q) {
+                        const bool odd = (t & 1) != 0;  // selects, not a dynamic index (no local memory)
+                        yr = odd ? out[q][0][2] : out[q][0][0];
+                        yg = odd ? out[q][0][3] : out[q][0][1];
+                        yb = odd ? out[q][1][2] : out[q][1][0];
                     }
             }
-            // reduce-scatter over the quad: lane t keeps row slot t
-            const bool hi = (t >> 1) != 0, lo = (t & 1) != 0;
-            float kept[2][3];
-#pragma unroll
-            for (int j = 0; j < 2; ++j)
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const float mine = hi ? part[2 + j][c] : part[j][c];
-                    const float other = hi ? part[j][c] : part[2 + j][c];
-                    kept[j][c] = mine + __shfl_xor_sync(0xffffffffu, other, 2);
-                }
-            float v[3];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float mine = lo ? kept[1][c] : kept[0][c];
-                const float other = lo ? kept[0][c] : kept[1][c];
-                v[c] = mine + __shfl_xor_sync(0xffffffffu, other, 1);
-            }
-            if (use) color = add3(color, mul3s(vmul(mk3(v[0], v[1], v[2]), ld3(L.color)), weight));
+            const f3 bsdf = {mlp::decode_fast(yr), mlp::decode_fast(yg), mlp::decode_fast(yb)};
+            if (use) color = add3(color, mul3s(vmul(bsdf, mk3(L.color.x, L.color.y, L.color.z)), weight));
         }
         if (active) {
             if (env.spec) {
@@ -1362,10 +1395,24 @@ cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights
         const uint32_t max_chunks = (pixels + 31u) / 32u;
         const uint32_t needed = (max_chunks + kCompactWarps - 1) / kCompactWarps;
         if (blocks > needed) blocks = needed;
-        shade_compact_kernel<<<blocks, kCompactWarps * 32, 0, ctx->stream>>>(
-            a, reinterpret_cast<const __half*>(ctx->surrogate->w16), ctx->surrogate->params, env, ctx->hair_list,
-            ctx->hair_count);
-        return cudaGetLastError();
+        // Programmatic dependent launch: the kernel's blocks start as the list
+        // pass's blocks retire and load weights and lights before they wait
+        // for the list.  (Letting the list pass trigger its dependents early
+        // was slower: the waiting blocks take the SM slots the pass needs.)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(blocks);
+        cfg.blockDim = dim3(kCompactWarps * 32);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = ctx->stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, shade_compact_kernel, a, reinterpret_cast<const __half*>(ctx->surrogate->w16),
+                                  static_cast<const float*>(ctx->surrogate->params), env,
+                                  static_cast<const uint32_t*>(ctx->hair_list),
+                                  static_cast<const uint32_t*>(ctx->hair_count));
     }
     dim3 block(32, 8);
     dim3 grid((ctx->width + 31) / 32, (ctx->height + 7) / 8);

@@ -265,7 +265,8 @@ __global__ void __launch_bounds__(kWarps * 32) infer_kernel(const InferArgs a) {
     }
 }
 
-// The compact network (hg_mlp_small.cuh) on mma.sync, 32 samples per warp.
+// The compact network (hg_mlp_small.cuh) on mma.sync, 32 samples per warp;
+// three outputs per sample (the BSDF rgb).
 __global__ void __launch_bounds__(kWarps * 32) infer_small_kernel(const InferArgs a) {
     __shared__ __align__(16) mlps::Weights w;
     __shared__ __align__(16) WarpIo io[kWarps];
@@ -275,15 +276,15 @@ __global__ void __launch_bounds__(kWarps * 32) infer_small_kernel(const InferArg
     for (uint32_t base = (blockIdx.x * kWarps + warp) * 32u; base < a.n; base += gridDim.x * kWarps * 32u) {
         const uint32_t i = base + lane;
         const bool valid = i < a.n;
-        float raw[10], x[10], y[12];
+        float raw[10], x[10], y[mlps::kUsedOut];
         load_raw(a.inputs, i, valid, raw);
         normalise(raw, x);
         mlps::forward(w, io[warp], x, y);
         if (valid) {
 #pragma unroll
-            for (int c = 0; c < 12; ++c) {
-                if (a.lobes) a.lobes[(size_t)i * 12 + c] = decode(y[c]);
-                if (a.net) a.net[(size_t)i * 12 + c] = y[c];
+            for (int c = 0; c < mlps::kUsedOut; ++c) {
+                if (a.lobes) a.lobes[(size_t)i * mlps::kUsedOut + c] = decode(y[c]);
+                if (a.net) a.net[(size_t)i * mlps::kUsedOut + c] = y[c];
             }
         }
     }
@@ -292,10 +293,12 @@ __global__ void __launch_bounds__(kWarps * 32) infer_small_kernel(const InferArg
 // Training of the compact network: one thread per sample (32 per block) runs
 // the forward pass with the inference roundings and the backward pass in
 // FP32; the block then sums its samples' weight gradients (each thread a
-// strided set of parameters, over the block's 32 samples) into `grad`.
+// strided set of parameters, over the block's 32 samples) into `grad`.  The
+// targets are the twelve transformed lobes of hg_mlp_samples; the kernel
+// forms the three BSDF targets from them (mlps::bsdf_target).
 struct SmallTrainArgs {
     const float* inputs;   // [n][10] raw
-    const float* targets;  // [n][12] transformed
+    const float* targets;  // [n][12] transformed lobes
     uint32_t n;
     const __half* w16;
     const float* params;
@@ -342,6 +345,9 @@ __global__ void __launch_bounds__(kSmallTrainThreads) small_train_kernel(const S
         for (int i = 0; i < mlps::kHid; ++i) z += w.w2[j][i] * a1[i];
         a2[j] = mlps::round_half(fmaxf(z, 0.0f));
     }
+    float t12[12];
+#pragma unroll
+    for (int o = 0; o < 12; ++o) t12[o] = valid ? __ldg(&a.targets[(size_t)k * 12 + o]) : 0.0f;
     float dy[mlps::kOut];
     float loss = 0.0f;
 #pragma unroll
@@ -349,7 +355,7 @@ __global__ void __launch_bounds__(kSmallTrainThreads) small_train_kernel(const S
         float y = w.b3[o];
 #pragma unroll
         for (int j = 0; j < mlps::kHid; ++j) y += w.w3[o][j] * a2[j];
-        const float d = valid && o < mlp::kUsedOut ? y - __ldg(&a.targets[(size_t)k * 12 + o]) : 0.0f;
+        const float d = valid && o < mlps::kUsedOut ? y - mlps::bsdf_target(t12, o) : 0.0f;
         loss += d * d;
         dy[o] = 2.0f * d;
     }
@@ -1016,6 +1022,11 @@ void hg_mlp_destroy(hg_mlp* m) {
 
 uint32_t hg_mlp_param_count(const hg_mlp* m) { return m ? m->n_params : 0u; }
 
+uint32_t hg_mlp_output_count(const hg_mlp* m) {
+    if (!m) return 0u;
+    return m->arch == HG_MLP_ARCH_COMPACT ? (uint32_t)hg::mlps::kUsedOut : (uint32_t)hg::mlp::kUsedOut;
+}
+
 hg_status hg_mlp_set_params(hg_mlp* m, const float* params, uint32_t count) {
     if (!m || !params) return HG_INVALID_ARG;
     hg_ctx* ctx = m->ctx;
@@ -1111,7 +1122,7 @@ hg_status hg_mlp_train_step(hg_mlp* m, const float* inputs, const float* targets
     const double b1t = 1.0 - std::pow(0.9, (double)m->step), b2t = 1.0 - std::pow(0.999, (double)m->step);
     const float lr_t = (float)(lr * std::sqrt(b2t) / b1t);
     const float eps_t = (float)(1e-8 * std::sqrt(b2t));
-    MLP_CUDA(ctx, hg::convert(m, 1, lr_t, eps_t, 1.0f / ((float)count * 12.0f)));
+    MLP_CUDA(ctx, hg::convert(m, 1, lr_t, eps_t, 1.0f / ((float)count * (float)hg_mlp_output_count(m))));
     if (loss_sum) {
         MLP_CUDA(ctx, cudaMemcpyAsync(loss_sum, m->loss, sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
     }

@@ -2,9 +2,9 @@
 
 A ReLU network (FP16 weights and activations, FP32 accumulation on the
 tensor cores) that stands in for the Karis-fit lobes of
-``shade.wesl:94-190``: 10 -> 4 x 64 -> 12 (``MLP_ARCH_DEEP``, shade models 1
-and 2) or the compact 10 -> 2 x 32 -> 12 (``MLP_ARCH_COMPACT``, shade model
-3).  It is trained on FP64 samples of the exact lobes
+``shade.wesl:94-190``: 10 -> 4 x 64 -> 12 lobes (``MLP_ARCH_DEEP``, shade
+models 1 and 2) or the compact 10 -> 2 x 32 -> 3 (``MLP_ARCH_COMPACT``, shade
+model 3), which predicts the per-light BSDF R + TT + TRT + 0.7 B directly.  It is trained on FP64 samples of the exact lobes
 (Gauss-Legendre integration of the Marschner/d'Eon azimuthal scattering plus
 the Zinke back-scattering term), generated on the GPU by ``hg_mlp_samples``.
 
@@ -43,6 +43,10 @@ def param_count(arch: int = abi.MLP_ARCH_DEEP) -> int:
     return abi.MLP_COMPACT_PARAMS if arch == abi.MLP_ARCH_COMPACT else abi.MLP_PARAMS
 
 
+def output_count(arch: int = abi.MLP_ARCH_DEEP) -> int:
+    return abi.MLP_COMPACT_OUTPUTS if arch == abi.MLP_ARCH_COMPACT else abi.MLP_OUTPUTS
+
+
 def split(params: np.ndarray, arch: int = abi.MLP_ARCH_DEEP) -> list[tuple[np.ndarray, np.ndarray]]:
     """Views (W[out][in], b[out]) of each layer of a flat parameter vector."""
     out, o = [], 0
@@ -67,7 +71,7 @@ def init_params(seed: int = 0, arch: int = abi.MLP_ARCH_DEEP) -> np.ndarray:
         w[...] = rng.normal(0.0, std, size=w.shape).astype(np.float32)
     layers[0][0][:, abi.MLP_INPUTS:] = 0.0
     w_out, b_out = layers[-1]
-    w_out[abi.MLP_OUTPUTS:, :] = 0.0
+    w_out[output_count(arch):, :] = 0.0
     b_out[...] = 0.0
     return p
 
@@ -102,6 +106,7 @@ class Surrogate:
         _check(self.lib, renderer.ctx, self.lib.hg_mlp_create_arch(renderer.ctx, self.arch, C.byref(h)))
         self.handle = h
         self.n_params = int(self.lib.hg_mlp_param_count(h))
+        self.n_out = int(self.lib.hg_mlp_output_count(h))
         if not hasattr(renderer, "_surrogates"):
             renderer._surrogates = []
         renderer._surrogates.append(self)
@@ -121,7 +126,8 @@ class Surrogate:
         return p
 
     def infer(self, inputs, n: int, lobes=None, net=None) -> None:
-        """Device float[n][10] inputs -> device float[n][12] decoded lobes and/or raw outputs."""
+        """Device float[n][10] inputs -> device float[n][n_out] decoded outputs and/or raw outputs
+        (12 lobes, or the compact network's 3 BSDF channels)."""
         self._check(self.lib.hg_mlp_infer(self.handle, _ptr(inputs), n, _ptr(lobes), _ptr(net)))
 
     def infer_tc(self, inputs, n: int, lobes=None, net=None) -> None:
@@ -184,17 +190,20 @@ def evaluate(renderer: HairRenderer, surrogate: Surrogate, n: int = 1 << 16, see
     dev = torch.device("cuda", torch.cuda.current_device())
     x = torch.empty((n, 10), dtype=torch.float32, device=dev)
     exact = torch.empty((n, 12), dtype=torch.float64, device=dev)
-    pred = torch.empty((n, 12), dtype=torch.float32, device=dev)
+    pred = torch.empty((n, surrogate.n_out), dtype=torch.float32, device=dev)
     kar = torch.empty((n, 12), dtype=torch.float32, device=dev)
     samples(renderer, seed, HOLDOUT_FIRST, n, x, None, exact)
     surrogate.infer(x, n, pred)
     karis_lobes(renderer, x, n, kar)
     renderer.synchronize()
     e, p, k = exact.cpu().numpy(), pred.cpu().numpy(), kar.cpu().numpy()
-    out = {"samples": n, "surrogate_bsdf": relative_l1(bsdf(p), bsdf(e)), "karis_bsdf": relative_l1(bsdf(k), bsdf(e))}
+    per_light = p if surrogate.n_out == 3 else bsdf(p)
+    out = {"samples": n, "surrogate_bsdf": relative_l1(per_light, bsdf(e)),
+           "karis_bsdf": relative_l1(bsdf(k), bsdf(e))}
     for i, name in enumerate(("R", "TT", "TRT", "B")):
         sl = slice(3 * i, 3 * i + 3)
-        out[f"surrogate_{name}"] = relative_l1(p[:, sl], e[:, sl])
+        if surrogate.n_out == 12:
+            out[f"surrogate_{name}"] = relative_l1(p[:, sl], e[:, sl])
         out[f"karis_{name}"] = relative_l1(k[:, sl], e[:, sl])
     return out
 

@@ -506,10 +506,13 @@ hg_status hg_batch_copy_out_async(hg_batch* batch, uint32_t item, hg_buffer_id w
 #define HG_MLP_PARAMS 14608u
 #define HG_MLP_INPUTS 10u
 #define HG_MLP_OUTPUTS 12u
-/* The compact network: 10 -> 32 -> 32 -> 12, the same inputs, outputs,
- * roundings and output transform; HG_MLP_COMPACT_PARAMS floats W1[32][16]
- * b1[32] W2[32][32] b2[32] W3[16][32] b3[16] (padding columns 10..15 of W1
- * and rows 12..15 of W3 and b3 stay zero).  Shade model 3 evaluates it. */
+/* The compact network: 10 -> 32 -> 32 -> 3, the same inputs and roundings;
+ * its 3 outputs are the per-light BSDF R + TT + TRT + 0.7 B (rgb) that the
+ * shade pass adds at zero deep-opacity depth, as log1p(bsdf / 1e-3).
+ * HG_MLP_COMPACT_PARAMS floats W1[32][16] b1[32] W2[32][32] b2[32] W3[16][32]
+ * b3[16] (padding columns 10..15 of W1 and rows 3..15 of W3 and b3 stay
+ * zero).  Trained on the same twelve-lobe targets, from which it forms the
+ * three BSDF targets.  Shade model 3 evaluates it. */
 #define HG_MLP_COMPACT_PARAMS 2128u
 #define HG_MLP_ARCH_DEEP 0u     /* 4 x 64, HG_MLP_PARAMS */
 #define HG_MLP_ARCH_COMPACT 1u  /* 2 x 32, HG_MLP_COMPACT_PARAMS */
@@ -522,6 +525,8 @@ hg_status hg_mlp_create_arch(hg_ctx* ctx, uint32_t arch, hg_mlp** out);
 void hg_mlp_destroy(hg_mlp* mlp);
 /* Number of parameters of the surrogate's architecture (0 for NULL). */
 uint32_t hg_mlp_param_count(const hg_mlp* mlp);
+/* Outputs per sample: 12 lobes (4 x 64 network) or 3 BSDF channels (compact). */
+uint32_t hg_mlp_output_count(const hg_mlp* mlp);
 /* Host float[count], count == hg_mlp_param_count; resets the optimiser state. */
 hg_status hg_mlp_set_params(hg_mlp* mlp, const float* params, uint32_t count);
 hg_status hg_mlp_get_params(hg_mlp* mlp, float* params, uint32_t count);
@@ -533,8 +538,8 @@ hg_status hg_mlp_get_params(hg_mlp* mlp, float* params, uint32_t count);
 hg_status hg_mlp_samples(hg_ctx* ctx, uint64_t seed, uint64_t first, uint32_t count, float tilt, float* inputs,
                          float* targets, double* lobes);
 /* Network evaluation.  Device buffers: inputs float[count][10]; lobes
- * float[count][12] (decoded, nullable); net float[count][12] (raw outputs,
- * nullable). */
+ * float[count][k] (decoded, nullable); net float[count][k] (raw outputs,
+ * nullable); k = hg_mlp_output_count. */
 hg_status hg_mlp_infer(hg_mlp* mlp, const float* inputs, uint32_t count, float* lobes, float* net);
 /* The same evaluation on the tcgen05 tensor cores: 128 rows per MMA,
  * accumulators in tensor memory, biases as two extra FP16 (high, low)
@@ -543,7 +548,9 @@ hg_status hg_mlp_infer(hg_mlp* mlp, const float* inputs, uint32_t count, float* 
 hg_status hg_mlp_infer_tc(hg_mlp* mlp, const float* inputs, uint32_t count, float* lobes, float* net);
 /* Gradient of the sum over samples and outputs of (net - target)^2 for one
  * batch (device inputs/targets), into host float[hg_mlp_param_count]; the loss sum
- * into *loss (nullable).  Parameters are unchanged. */
+ * into *loss (nullable).  Parameters are unchanged.  Targets are always the
+ * twelve transformed lobes of hg_mlp_samples (float[count][12]); the compact
+ * network's targets are the three BSDF channels formed from them. */
 hg_status hg_mlp_gradients(hg_mlp* mlp, const float* inputs, const float* targets, uint32_t count, float* grad,
                            float* loss);
 /* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) on the mean squared error

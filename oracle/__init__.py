@@ -184,11 +184,11 @@ def sample_cube(texels: np.ndarray, size: int, levels: int, direction, lod: floa
 
 
 def mlp_forward(params: np.ndarray, raw: np.ndarray, arch: int = 0) -> np.ndarray:
-    """The surrogate network on raw inputs (n, 10) -> raw outputs (n, 12), FP16 rounding emulated
-    (arch 0: 4 x 64; 1: the compact 2 x 32)."""
+    """The surrogate network on raw inputs (n, 10) -> raw outputs, FP16 rounding emulated
+    (arch 0: 4 x 64, (n, 12) lobes; 1: the compact 2 x 32, (n, 3) BSDF channels)."""
     p = np.ascontiguousarray(params, dtype=np.float32)
     x = np.ascontiguousarray(raw, dtype=np.float32).reshape(-1, 10)
-    out = np.empty((len(x), 12), dtype=np.float32)
+    out = np.empty((len(x), 3 if arch == 1 else 12), dtype=np.float32)
     lib().oracle_mlp_forward_arch(_p(p), int(arch), _p(x), len(x), _p(out))
     return out
 

@@ -961,11 +961,13 @@ static void mlp_layer(const float* w, const float* b, const float* in, int n_in,
     }
 }
 
-/* arch 0: 10 -> 4 x 64 -> 12 (hg_mlp.cuh); arch 1: the compact 10 -> 2 x 32
- * -> 12 (hg_mlp_small.cuh), parameters W1[32][16] b1 W2[32][32] b2 W3[16][32]
- * b3.  Same normalisation, roundings and output space. */
+/* arch 0: 10 -> 4 x 64 -> 12 lobes (hg_mlp.cuh); arch 1: the compact
+ * 10 -> 2 x 32 -> 3 (hg_mlp_small.cuh), parameters W1[32][16] b1 W2[32][32]
+ * b2 W3[16][32] b3, whose outputs are the per-light BSDF rgb
+ * (R + TT + TRT + 0.7 B) as log1p(bsdf / 1e-3).  Same normalisation and
+ * roundings; net holds 12 (arch 0) or 3 (arch 1) values per sample. */
 void oracle_mlp_forward_arch(const float* params, uint32_t arch, const float* raw, uint32_t n, float* net) {
-    const int hid = arch == 1u ? 32 : 64, hidden_layers = arch == 1u ? 2 : 4;
+    const int hid = arch == 1u ? 32 : 64, hidden_layers = arch == 1u ? 2 : 4, n_out = arch == 1u ? 3 : 12;
     for (uint32_t s = 0; s < n; ++s) {
         const float* r = raw + 10 * (size_t)s;
         float x[16] = {0}, h0[64], h1[64], y[16];
@@ -990,7 +992,7 @@ void oracle_mlp_forward_arch(const float* params, uint32_t arch, const float* ra
             out = t;
         }
         mlp_layer(p, p + 16 * hid, in, hid, 16, 0, y);
-        for (int c = 0; c < 12; ++c) net[12 * (size_t)s + c] = y[c];
+        for (int c = 0; c < n_out; ++c) net[(size_t)n_out * s + c] = y[c];
     }
 }
 
@@ -1019,12 +1021,18 @@ static v3 surrogate_bsdf(const float* mlp, uint32_t arch, v3 tangent, v3 view, v
                      sigma_a.z, shape.beta.x, clampf(roughness, 0.2f, 0.8f), IOR};
     float y[12];
     oracle_mlp_forward_arch(mlp, arch, raw, 1, y);
-    v3 single = V3(mlp_decode(y[0]) + mlp_decode(y[3]) + mlp_decode(y[6]),
-                   mlp_decode(y[1]) + mlp_decode(y[4]) + mlp_decode(y[7]),
-                   mlp_decode(y[2]) + mlp_decode(y[5]) + mlp_decode(y[8]));
-    v3 back = V3(mlp_decode(y[9]), mlp_decode(y[10]), mlp_decode(y[11]));
+    v3 bsdf;
+    if (arch == 1u) {
+        bsdf = V3(mlp_decode(y[0]), mlp_decode(y[1]), mlp_decode(y[2]));
+    } else {
+        v3 single = V3(mlp_decode(y[0]) + mlp_decode(y[3]) + mlp_decode(y[6]),
+                       mlp_decode(y[1]) + mlp_decode(y[4]) + mlp_decode(y[7]),
+                       mlp_decode(y[2]) + mlp_decode(y[5]) + mlp_decode(y[8]));
+        v3 back = V3(mlp_decode(y[9]), mlp_decode(y[10]), mlp_decode(y[11]));
+        bsdf = add3(single, mul3s(back, DENSITY_BACK));
+    }
     float direct = expf(-depth);
-    v3 color = mul3s(add3(single, mul3s(back, DENSITY_BACK)), direct);
+    v3 color = mul3s(bsdf, direct);
     if (depth > 1e-3f) color = add3(color, spread_term(shape, ds, theta_h, depth, direct));
     return color;
 }

@@ -99,8 +99,9 @@ void oracle_shade(const hg_hair_params* p, const uint64_t* center, const uint32_
 /* One trilinear cubemap sample (RGB9E5 mip chain) for the sampler tests. */
 void oracle_sample_cube(const uint32_t* texels, uint32_t size, uint32_t levels, const float dir[3], float lod,
                         float out[3]);
-/* The surrogate network on raw inputs (n x 10) -> raw outputs (n x 12):
- * the 4 x 64 network, or the given architecture (0: 4 x 64, 1: 2 x 32). */
+/* The surrogate network on raw inputs (n x 10) -> raw outputs: the 4 x 64
+ * network (n x 12 lobes), or the given architecture (0: 4 x 64, n x 12;
+ * 1: the compact 2 x 32, n x 3 BSDF channels). */
 void oracle_mlp_forward(const float* params, const float* raw, uint32_t n, float* net);
 void oracle_mlp_forward_arch(const float* params, uint32_t arch, const float* raw, uint32_t n, float* net);
 void oracle_filter(const hg_hair_params* p, const uint64_t* center, const uint64_t* cons,

@@ -1,16 +1,19 @@
 """FP64 reference of the shading surrogate's network.  TEST INFRASTRUCTURE ONLY.
 
-Forward and backward passes of the 10 -> 4 x 64 -> 12 ReLU network (arch 0)
-and of the compact 10 -> 2 x 32 -> 12 network (arch 1) that libhairgb.so
-trains and evaluates (bevy_hair_gb300/csrc/hg_mlp.cuh, hg_mlp_small.cuh,
-surrogate.cu).  With ``half=True`` the weights, the normalised
+Forward and backward passes of the 10 -> 4 x 64 -> 12 ReLU network (arch 0,
+the twelve lobes) and of the compact 10 -> 2 x 32 -> 3 network (arch 1, the
+per-light BSDF rgb) that libhairgb.so trains and evaluates
+(bevy_hair_gb300/csrc/hg_mlp.cuh, hg_mlp_small.cuh, surrogate.cu).  With ``half=True`` the weights, the normalised
 inputs and the post-ReLU activations are rounded to FP16 exactly where the
 kernels round them, and everything else is FP64; the gradients are not
 rounded (the kernels round the backward pass's fragments to FP16, so the
 comparison uses a tolerance).  With ``half=False`` the network is smooth FP64
 for finite-difference checks of the analytic gradient.
 
-Loss: sum over samples and the 12 outputs of (y - target)^2.
+Loss: sum over samples and the used outputs of (y - target)^2.  Targets are
+the twelve transformed lobes log1p(lobe / 1e-3) in both cases; arch 1's three
+targets are log1p(bsdf / 1e-3) with bsdf = R + TT + TRT + 0.7 B formed from
+them (``bsdf_targets``).
 """
 from __future__ import annotations
 
@@ -25,6 +28,16 @@ N_OUT = 12
 
 def layers_of(arch: int):
     return COMPACT_LAYERS if arch == 1 else LAYERS
+
+
+def outputs_of(arch: int) -> int:
+    return 3 if arch == 1 else N_OUT
+
+
+def bsdf_targets(targets12: np.ndarray) -> np.ndarray:
+    """(n, 12) transformed lobes -> (n, 3) transformed BSDF channels (FP64)."""
+    e = np.expm1(np.asarray(targets12, dtype=np.float64).reshape(-1, 12))
+    return np.log1p(e[:, 0:3] + e[:, 3:6] + e[:, 6:9] + 0.7 * e[:, 9:12])
 
 
 def split(params: np.ndarray, arch: int = 0):
@@ -77,8 +90,11 @@ def gradients(params: np.ndarray, raw: np.ndarray, targets: np.ndarray, half: bo
     """(flat gradient float64[len(params)], loss) of sum((y - t)^2) over the 12 outputs."""
     y, acts, layers = forward(params, raw, half, arch)
     t = np.asarray(targets, dtype=np.float64).reshape(-1, N_OUT)
+    if arch == 1:
+        t = bsdf_targets(t)
+    k = outputs_of(arch)
     d = np.zeros_like(y)
-    d[:, :N_OUT] = y[:, :N_OUT] - t
+    d[:, :k] = y[:, :k] - t
     loss = float((d * d).sum())
     dz = 2.0 * d
     grads = [None] * len(layers)

@@ -384,7 +384,7 @@ COMPACT = abi.MLP_ARCH_COMPACT
 def test_compact_fp64_reference_matches_finite_differences():
     p = S.init_params(13, COMPACT).astype(np.float64)
     x = _inputs(48, 14)
-    t = np.random.default_rng(15).normal(size=(48, 12))
+    t = np.random.default_rng(15).uniform(0.0, 3.0, size=(48, 12))  # transformed lobes
     g, _ = mlp_ref.gradients(p, x, t, half=False, arch=COMPACT)
     assert g.shape == (abi.MLP_COMPACT_PARAMS,)
     for idx in (5, 300, 520, 700, 1500, 1570, 1700, 2100, 2115):
@@ -402,9 +402,16 @@ def test_compact_oracle_emulation_matches_fp64_reference():
     x = _inputs(256, 17)
     got = oracle.mlp_forward(p, x, arch=COMPACT)
     want, _, _ = mlp_ref.forward(p, x, arch=COMPACT)
-    np.testing.assert_allclose(got, want[:, :12], rtol=0, atol=3e-3)
-    # the two architectures are different functions of the same inputs
-    assert np.abs(oracle.mlp_forward(S.init_params(16), x) - got).max() > 1e-2
+    assert got.shape == (256, abi.MLP_COMPACT_OUTPUTS)
+    np.testing.assert_allclose(got, want[:, :3], rtol=0, atol=3e-3)
+
+
+def test_compact_targets_are_the_per_light_bsdf():
+    rng = np.random.default_rng(23)
+    lobes = rng.uniform(0.0, 2.0, size=(64, 12))
+    t12 = np.log1p(lobes / 1e-3)
+    want = np.log1p(S.bsdf(lobes) / 1e-3)
+    np.testing.assert_allclose(mlp_ref.bsdf_targets(t12), want, rtol=1e-12)
 
 
 def test_compact_init_params_keep_padding_zero():
@@ -412,25 +419,25 @@ def test_compact_init_params_keep_padding_zero():
     layers = S.split(p, COMPACT)
     assert [w.shape for w, _ in layers] == [(32, 16), (32, 32), (16, 32)]
     assert (layers[0][0][:, 10:] == 0).all()
-    assert (layers[2][0][12:, :] == 0).all() and (layers[2][1] == 0).all()
+    assert (layers[2][0][abi.MLP_COMPACT_OUTPUTS:, :] == 0).all() and (layers[2][1] == 0).all()
 
 
 def test_shipped_compact_weights_have_the_parameter_layout():
     p = S.load_params(COMPACT)
     assert p.shape == (abi.MLP_COMPACT_PARAMS,) and np.isfinite(p).all()
     layers = S.split(p, COMPACT)
-    assert (layers[0][0][:, 10:] == 0).all() and (layers[2][0][12:, :] == 0).all()
+    assert (layers[0][0][:, 10:] == 0).all() and (layers[2][0][abi.MLP_COMPACT_OUTPUTS:, :] == 0).all()
 
 
 @gpu
 def test_compact_surrogate_entry_points_check_the_architecture(renderer):
     s = S.Surrogate(renderer, None, COMPACT)
-    assert s.n_params == abi.MLP_COMPACT_PARAMS
+    assert s.n_params == abi.MLP_COMPACT_PARAMS and s.n_out == abi.MLP_COMPACT_OUTPUTS
     with pytest.raises(abi.HairGbError):
         s.set_params(S.init_params(0))  # 4 x 64 parameter count
     torch, dev = _torch()
     x = torch.from_numpy(_inputs(64, 18)).to(dev)
-    out = torch.empty((64, 12), dtype=torch.float32, device=dev)
+    out = torch.empty((64, 3), dtype=torch.float32, device=dev)
     with pytest.raises(abi.HairGbError):
         s.infer_tc(x, 64, out)  # tcgen05 inference is for the 4 x 64 network
     s.close()
@@ -447,15 +454,18 @@ def test_compact_forward_matches_the_oracle_emulation(renderer, which):
     for n in (5000, 77):
         xs = _inputs(n, 20)
         x = torch.from_numpy(xs).to(dev)
-        net = torch.full((n, 12), float("nan"), dtype=torch.float32, device=dev)
-        lob = torch.empty((n, 12), dtype=torch.float32, device=dev)
+        # one extra row each: the kernel writes n rows of 3, nothing past them
+        net = torch.full((n + 1, 3), float("nan"), dtype=torch.float32, device=dev)
+        lob = torch.full((n + 1, 3), -7.0, dtype=torch.float32, device=dev)
         s.infer(x, n, lob, net)
         assert renderer.synchronize() == 0
-        got, want = net.cpu().numpy(), oracle.mlp_forward(p, xs, arch=COMPACT)
+        got_all, lob_all = net.cpu().numpy(), lob.cpu().numpy()
+        assert np.isnan(got_all[n]).all() and (lob_all[n] == -7.0).all()
+        got, want = got_all[:n], oracle.mlp_forward(p, xs, arch=COMPACT)
         assert np.isfinite(got).all()
         assert np.abs(got - want).mean() < 1e-3
         np.testing.assert_allclose(got, want, rtol=0, atol=3e-2)
-        np.testing.assert_allclose(lob.cpu().numpy(), 1e-3 * np.expm1(np.maximum(got, 0)), rtol=1e-5, atol=1e-9)
+        np.testing.assert_allclose(lob_all[:n], 1e-3 * np.expm1(np.maximum(got, 0)), rtol=1e-5, atol=1e-9)
     s.close()
 
 
@@ -479,7 +489,7 @@ def test_compact_gradients_match_the_fp64_reference(renderer):
     for k, ((gw, gb), (ww, wb)) in enumerate(zip(S.split(g, COMPACT), S.split(want.astype(np.float32), COMPACT))):
         assert np.linalg.norm(gw - ww) <= 1e-2 * np.linalg.norm(ww) + 1e-6, k
         assert np.linalg.norm(gb - wb) <= 1e-2 * np.linalg.norm(wb) + 1e-6, k
-    assert (S.split(g, COMPACT)[0][0][:, 10:] == 0).all() and (S.split(g, COMPACT)[2][0][12:, :] == 0).all()
+    assert (S.split(g, COMPACT)[0][0][:, 10:] == 0).all() and (S.split(g, COMPACT)[2][0][3:, :] == 0).all()
     np.testing.assert_array_equal(s.get_params(), p)
     s.close()
 
@@ -502,7 +512,7 @@ def test_compact_training_reduces_the_loss(renderer):
     assert np.isfinite(l).all()
     assert l[-20:].mean() < 0.25 * l[:5].mean(), (l[:5], l[-20:])
     p = s.get_params()
-    assert (S.split(p, COMPACT)[0][0][:, 10:] == 0).all() and (S.split(p, COMPACT)[2][0][12:, :] == 0).all()
+    assert (S.split(p, COMPACT)[0][0][:, 10:] == 0).all() and (S.split(p, COMPACT)[2][0][3:, :] == 0).all()
     s.close()
 
 
