@@ -1178,14 +1178,6 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 3)
             for (int c = 10; c < mlps::kIn; c += 2) st_h2(&xr[lane][c], 0.0f, 0.0f);
             __syncwarp();
         }
-        // A-fragment registers of columns 8..15, the same for every light;
-        // network row g + 8k holds the pixel of lane 4g + k
-        uint32_t a_hi[2][2];
-#pragma unroll
-        for (int mt = 0; mt < 2; ++mt) {
-            a_hi[mt][0] = mlp::ld32(&xr[4 * g + 2 * mt][8 + 2 * t]);
-            a_hi[mt][1] = mlp::ld32(&xr[4 * g + 2 * mt + 1][8 + 2 * t]);
-        }
         f3 color = spl(0.0f);
         float dom_direct = 1.0f;
         if (dom_light >= 0 && active) {
@@ -1218,7 +1210,10 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 3)
             st_h2(&xr[lane][0], sin_i, sin_o);
             st_h2(&xr[lane][2], cos_phi, sqrtf(fmaxf(1.0f - cos_phi * cos_phi, 0.0f)));
             __syncwarp();
-            // this lane's row is g + 8t: m-tile t >> 1, half t & 1 of its fragments
+            // Network row g + 8k holds the pixel of lane 4g + k, so this lane's
+            // own row is g + 8t: m-tile t >> 1, half t & 1 of its fragments.
+            // Columns 8..15 (per-pixel inputs) are reloaded per light rather
+            // than held, which keeps the kernel within 80 registers.
             float yr = 0.0f, yg = 0.0f, yb = 0.0f;
 #pragma unroll
             for (int m0 = 0; m0 < 2; m0 += kCompactTiles) {
@@ -1228,8 +1223,8 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 3)
                     const int mt = m0 + q;
                     a0[q][0][0] = mlp::ld32(&xr[4 * g + 2 * mt][2 * t]);
                     a0[q][0][1] = mlp::ld32(&xr[4 * g + 2 * mt + 1][2 * t]);
-                    a0[q][0][2] = a_hi[mt][0];
-                    a0[q][0][3] = a_hi[mt][1];
+                    a0[q][0][2] = mlp::ld32(&xr[4 * g + 2 * mt][8 + 2 * t]);
+                    a0[q][0][3] = mlp::ld32(&xr[4 * g + 2 * mt + 1][8 + 2 * t]);
                 }
                 float acc[kCompactTiles][4][4];
                 uint32_t ah[kCompactTiles][2][4];
