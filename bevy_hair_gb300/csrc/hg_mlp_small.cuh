@@ -65,8 +65,9 @@ __device__ __forceinline__ void relu_to_a(const float acc[2][4][4], uint32_t a[2
 }
 
 // Forward pass of the 32 samples held by the warp's lanes (x: this lane's
-// normalised inputs; y: its outputs in the transformed space, the first
-// kUsedOut meaningful).  Every lane of the warp calls it.
+// normalised inputs; y: 12 columns of its outputs in the transformed space,
+// the first kUsedOut meaningful, the rest padding).  Every lane of the warp
+// calls it.
 __device__ __forceinline__ void forward(const Weights& w, mlp::WarpIo& io, const float x[mlp::kUsedIn],
                                         float y[mlp::kUsedOut]) {
     const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;

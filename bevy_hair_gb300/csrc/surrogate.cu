@@ -276,7 +276,7 @@ __global__ void __launch_bounds__(kWarps * 32) infer_small_kernel(const InferArg
     for (uint32_t base = (blockIdx.x * kWarps + warp) * 32u; base < a.n; base += gridDim.x * kWarps * 32u) {
         const uint32_t i = base + lane;
         const bool valid = i < a.n;
-        float raw[10], x[10], y[mlps::kUsedOut];
+        float raw[10], x[10], y[mlp::kUsedOut];  // forward() fills 12 columns; the first kUsedOut are outputs
         load_raw(a.inputs, i, valid, raw);
         normalise(raw, x);
         mlps::forward(w, io[warp], x, y);
