@@ -562,3 +562,33 @@ def test_shipped_compact_surrogate_beats_the_karis_fit(renderer):
     ev = S.evaluate(renderer, s, n=1 << 15)
     s.close()
     assert ev["surrogate_bsdf"] < 0.75 * ev["karis_bsdf"], ev
+
+
+@gpu
+def test_shade_model_three_on_an_empty_g_buffer_and_without_lights(renderer):
+    """No hair pixel (empty list) and no light: the pass writes the empty outputs and nothing else."""
+    sc = configs.config2(scale=0.02)
+    cam, dom = sc.params()
+    lights = sc.light_array()
+    renderer.ensure_targets(sc.view.width, sc.view.height, *sc.dom_size)
+    s = S.Surrogate(renderer, S.load_params(COMPACT), COMPACT)
+    renderer.bind_surrogate(s)
+    renderer.clear()
+    renderer.shade(cam, lights, model=abi.SHADE_SURROGATE_COMPACT)
+    assert renderer.synchronize() == 0
+    assert (renderer.read(abi.BUF_SHADED) == 0).all() and (renderer.read(abi.BUF_SHADED_DEPTH) == 0).all()
+    g = renderer.upload(sc.mesh)
+    renderer.render_groom(g, cam, dom, lights)
+    assert renderer.synchronize() == 0
+    renderer.shade(cam, lights[:0], model=abi.SHADE_SURROGATE_COMPACT)
+    assert renderer.synchronize() == 0
+    center = renderer.read(abi.BUF_CENTER)
+    shaded = renderer.read(abi.BUF_SHADED).reshape(-1, 4)
+    hit = center != EMPTY
+    want, _ = oracle.shade(cam, center, renderer.read(abi.BUF_BETA), renderer.read(abi.BUF_DOM), lights[:0],
+                           mlp=S.load_params(COMPACT), mlp_arch=COMPACT)
+    np.testing.assert_array_equal(shaded[:, 3], hit.astype(np.float32))
+    np.testing.assert_allclose(shaded[hit, :3], want.reshape(-1, 4)[hit, :3], rtol=1e-5, atol=1e-7)
+    renderer.bind_surrogate(None)
+    s.close()
+    g.close()
