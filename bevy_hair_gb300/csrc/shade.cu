@@ -1131,11 +1131,16 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 3)
     auto list_at = [&](uint32_t c) -> uint32_t {
         return c < chunks && c * 32u + lane < n ? __ldg(&list[c * 32u + lane]) : kNone;
     };
-    uint32_t ch = blockIdx.x * kCompactWarps + warp;
+    // The block's warps take chunks in lockstep (every warp runs the same
+    // number of iterations) and meet at a barrier before the probe: warps
+    // spread over the prologue, the light loop and the probe at once ran more
+    // code than the instruction caches hold (8 % slower with the probe on).
+    const uint32_t first = blockIdx.x * kCompactWarps;
+    uint32_t ch = first + warp;
     uint32_t pix_next = list_at(ch), pix_after = list_at(ch + stride);
     unsigned long long word_next = pix_next != kNone ? __ldg(&a.center[pix_next]) : 0ull;
     uint32_t beta_next = pix_next != kNone ? __ldg(&a.beta[pix_next]) : 0u;
-    for (; ch < chunks; ch += stride) {
+    for (uint32_t block_ch = first; block_ch < chunks; block_ch += stride, ch += stride) {
         const bool active = pix_next != kNone;
         const uint32_t pix = active ? pix_next : 0u;
         const unsigned long long word = word_next;
@@ -1246,6 +1251,7 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 3)
             const f3 bsdf = {mlp::decode_fast(yr), mlp::decode_fast(yg), mlp::decode_fast(yb)};
             if (use) color = add3(color, mul3s(vmul(bsdf, mk3(L.color.x, L.color.y, L.color.z)), weight));
         }
+        __syncthreads();
         if (active) {
             if (env.spec) {
                 // the probe's inputs again from the centre word (fewer registers live across the light loop)
