@@ -489,3 +489,52 @@ def test_async_readback_lands_before_the_next_frame_writes(renderer):
     with pytest.raises(abi.HairGbError):
         renderer.read_async(abi.BUF_COLOR, color.data_ptr(), 16)
     g.close()
+
+
+@pytest.mark.parametrize("model", [abi.SHADE_KARIS, abi.SHADE_SURROGATE_COMPACT])
+def test_orthographic_camera(renderer, model):
+    """An orthographic camera: visibility bit-exact, and the shade pass's view
+    direction the camera axis (hg_shade_desc.ortho), against the oracle."""
+    from bevy_hair_gb300 import surrogate as S
+
+    sc = configs.config1(scale=0.05)
+    w, h = sc.view.width, sc.view.height
+    ext = float(np.max(np.asarray(sc.mesh.bounds_max) - np.asarray(sc.mesh.bounds_min)))
+    half = 0.6 * ext
+    proj = host.orthographic_rh(-half * w / h, half * w / h, -half, half, 1.0, 4000.0)
+    view = host.View(sc.view.world_from_view, proj, w, h)
+    cam, dom = host.groom_params(view, sc.groom, sc.mesh.bounds_min, sc.mesh.bounds_max, sc.mesh.bundle_count,
+                                 sc.directionals, sc.dom_size)
+    got = _visibility(renderer, sc, cam, dom)
+    want = _oracle_visibility(sc, cam, dom)
+    assert (want["center"] != EMPTY).sum() > 100
+    _check_visibility(got, want)
+    lights = sc.light_array()
+    s, mlp, arch = None, None, abi.MLP_ARCH_DEEP
+    if model == abi.SHADE_SURROGATE_COMPACT:
+        arch = abi.MLP_ARCH_COMPACT
+        mlp = S.load_params(arch)
+        s = S.Surrogate(renderer, mlp, arch)
+        renderer.bind_surrogate(s)
+    g = renderer.upload(sc.mesh)
+    renderer.render_groom(g, cam, dom, lights, ortho=True, model=model)
+    assert renderer.synchronize() == 0
+    center = renderer.read(abi.BUF_CENTER)
+    _assert_equal("center", center, want["center"])
+    shaded = renderer.read(abi.BUF_SHADED)
+    o_shaded, _ = oracle.shade(cam, center, renderer.read(abi.BUF_BETA), renderer.read(abi.BUF_DOM), lights,
+                               ortho=True, mlp=mlp, mlp_arch=arch)
+    hit = center != EMPTY
+    got4, want4 = shaded.reshape(-1, 4)[hit, :3], o_shaded.reshape(-1, 4)[hit, :3]
+    if model == abi.SHADE_KARIS:
+        np.testing.assert_allclose(shaded, o_shaded, rtol=SHADE_RTOL, atol=SHADE_ATOL)
+    else:
+        assert np.abs(got4 - want4).sum() / np.abs(want4).sum() < 2e-3
+    # the perspective view direction gives a different picture
+    o_persp, _ = oracle.shade(cam, center, renderer.read(abi.BUF_BETA), renderer.read(abi.BUF_DOM), lights,
+                              ortho=False, mlp=mlp, mlp_arch=arch)
+    assert np.abs(o_persp.reshape(-1, 4)[hit, :3] - want4).max() > 1e-3
+    if s is not None:
+        renderer.bind_surrogate(None)
+        s.close()
+    g.close()
