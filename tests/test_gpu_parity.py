@@ -538,3 +538,16 @@ def test_orthographic_camera(renderer, model):
         renderer.bind_surrogate(None)
         s.close()
     g.close()
+
+
+@pytest.mark.parametrize("name", ["config1", "config2", "config3"])
+def test_full_size_visibility_bit_exact(renderer, name):
+    """The configurations at full size (config 2 is the benchmark workload:
+    100k strands, 1920x1080, DOM 1024^2): LOD records, refs, G-buffer words
+    and both DOM passes equal to the oracle's."""
+    sc = getattr(configs, name)(scale=1.0)
+    cam, dom = sc.params()
+    got = _visibility(renderer, sc, cam, dom)
+    want = _oracle_visibility(sc, cam, dom)
+    assert (want["center"] != EMPTY).sum() > 20_000
+    _check_visibility(got, want)
