@@ -342,16 +342,25 @@ def test_shade_filter_composite_within_tolerance(renderer, name):
     np.testing.assert_allclose(color, o_color, rtol=1e-6, atol=1e-7)
 
 
-def test_full_frame_against_the_oracle_frame(renderer):
-    """hg_groom_frame against the oracle's whole hair_pass sequence."""
-    sc = configs.config2(scale=0.02)
+@pytest.mark.parametrize("scale", [0.02, 1.0])
+def test_full_frame_against_the_oracle_frame(renderer, scale):
+    """hg_groom_frame against the oracle's whole hair_pass sequence; at scale 1
+    the benchmark frame itself, light probe included."""
+    sc = configs.config2(scale=scale)
     cam, dom = sc.params()
     lights = sc.light_array()
+    env = None
+    if scale == 1.0:
+        from bevy_hair_gb300 import envmap
+
+        env = envmap.procedural()
+    renderer.set_environment(env)
     renderer.ensure_targets(sc.view.width, sc.view.height, *sc.dom_size)
     g = renderer.upload(sc.mesh)
     renderer.render_groom(g, cam, dom, lights)
     assert renderer.synchronize() == 0
-    want = oracle.frame(sc.mesh, cam, dom, lights)
+    renderer.set_environment(None)
+    want = oracle.frame(sc.mesh, cam, dom, lights, env=env)
     _assert_equal("center", renderer.read(abi.BUF_CENTER), want["center"])
     _assert_equal("conservative", renderer.read(abi.BUF_CONSERVATIVE), want["cons"])
     _assert_equal("beta", renderer.read(abi.BUF_BETA), want["beta"])
