@@ -215,3 +215,23 @@ def test_batch_argument_errors(renderer, batch_scene):
     assert renderer.synchronize() == 0
     b.close()
     g0.close()
+
+
+def test_full_size_batch_items_match_the_oracle(renderer):
+    """The config 4 benchmark batch itself (64 grooms, 128 views) as one graph
+    replay: three items (first, largest, last) against the oracle's frames."""
+    bs = configs.config4(scale=1.0)
+    b, grooms, params = _make(renderer, bs)
+    lights = bs.light_array()
+    b.frame(lights, abi.BATCH_GRAPH)
+    assert renderer.synchronize() == 0
+    largest = max(range(len(grooms)), key=lambda k: bs.scenes[k].mesh.strand_count())
+    for k in sorted({0, largest, len(grooms) - 1}):
+        cam, dom = params[k]
+        want = oracle.frame(bs.scenes[k].mesh, cam, dom, lights)
+        np.testing.assert_array_equal(b.read(k, abi.BUF_CENTER), want["center"])
+        np.testing.assert_array_equal(b.read(k, abi.BUF_CONSERVATIVE), want["cons"])
+        np.testing.assert_array_equal(b.read(k, abi.BUF_BETA), want["beta"])
+        np.testing.assert_array_equal(b.read(k, abi.BUF_DOM), want["dom"])
+        np.testing.assert_allclose(b.read(k, abi.BUF_COLOR), want["color"], rtol=2e-3, atol=1e-5)
+    _close(b, grooms)
