@@ -1,6 +1,7 @@
 // Learned shading surrogate: FP64 training samples of the hair lobes, the
-// FP16 tensor-core network's inference and training kernels (forward +
-// backward per warp, split-K weight gradients, Adam), and their C entry
+// FP16 tensor-core networks' inference and training kernels (4 x 64: forward
+// + backward per warp, split-K weight gradients, Adam; compact 2 x 32: one
+// sample per thread, block-summed weight gradients, Adam), and their C entry
 // points.  The reference has no counterpart; the shading it replaces is the
 // Karis fit of shade.wesl:94-190.
 #include <cuda_fp16.h>
