@@ -303,7 +303,7 @@ def surrogate_section(r, cam, lights, flush, stream, reps: int, karis_ms: float,
         "evaluations": int(evals), "flop_per_eval": MLP_FLOP_PER_EVAL,
         "roofline": {"bound": "tensor", "achieved": round(tflops, 2), "peak": peak, "peak_source": src,
                      "unit": "TFLOP/s", "frac": round(tflops / peak, 4)},
-        "error": {"judge": "FP64 lobes (64-point Gauss-Legendre in gamma_i, hg_mlp_samples), 65,536 held-out samples",
+        "error": {"reference": "FP64 lobes (64-point Gauss-Legendre in gamma_i, hg_mlp_samples), 65,536 held-out samples",
                   "metric": "relative L1 of R + TT + TRT + 0.7 B",
                   "surrogate": round(ev["surrogate_bsdf"], 5), "karis": round(ev["karis_bsdf"], 5),
                   "per_lobe": {k: round(v, 5) for k, v in ev.items() if k.startswith(("surrogate_", "karis_"))

@@ -256,7 +256,7 @@ def hair_visibility(light: np.ndarray, dom: np.ndarray, dom_w: int, dom_h: int, 
 def lobes(inputs: np.ndarray, model: str = "marschner", tilt: float = 0.08) -> np.ndarray:
     """FP64 hair lobes for inputs (n, 10): sin_i, sin_o, cos_phi, sin_phi, sigma_a rgb,
     beta_m, beta_n, eta.  Returns (n, 12): R, TT, TRT, B (rgb each).  model
-    "marschner": exact azimuthal integrals (the judge); "karis": shade.wesl's fits."""
+    "marschner": exact azimuthal integrals (the FP64 reference); "karis": shade.wesl's fits."""
     x = np.ascontiguousarray(inputs, dtype=np.float64).reshape(-1, 10)
     out = np.empty((len(x), 12), dtype=np.float64)
     lib().oracle_lobes_batch(0 if model == "marschner" else 1, _p(x), len(x), float(tilt), _p(out))

@@ -1,7 +1,7 @@
 /*
  * marschner.c -- FP64 hair scattering lobes.  TEST INFRASTRUCTURE ONLY.
  *
- * The judge of shading error: the single-scattering lobes R, TT, TRT of a
+ * The FP64 reference for shading error: the single-scattering lobes R, TT, TRT of a
  * dielectric cylinder (Marschner et al. 2003, "Light Scattering from Human
  * Hair Fibers"; d'Eon et al. 2011, "An Energy-Conserving Hair Reflectance
  * Model"; Chiang et al. 2016, "A Practical and Controllable Hair and Fur Model
@@ -9,7 +9,7 @@
  * exactly over the offset h, and the local back-scattering term of the dual
  * scattering approximation (Zinke et al. 2008) built from the same exact
  * lobes.  It follows shade.wesl's conventions so that the Karis-fit lobes of
- * shade.wesl:94-128 and the learned surrogate are judged on the same terms:
+ * shade.wesl:94-128 and the learned surrogate are measured against it on the same terms:
  *   S_p = M_p(theta_i + theta_o - alpha_p; beta_p) * N_p(phi; theta_d)
  * with shade.wesl's Gaussian longitudinal lobes (alpha = tilt, -tilt/2,
  * -3 tilt/2; beta = b_m, b_m/2, 2 b_m) and

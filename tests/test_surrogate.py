@@ -1,4 +1,4 @@
-"""The learned shading surrogate: its FP64 judge, the FP16 tensor-core network
+"""The learned shading surrogate: its FP64 reference lobes, the FP16 tensor-core network
 (inference, gradients, training) and shade model 1.
 
 CPU tests pin the FP64 lobe integrator against an independent brute-force
