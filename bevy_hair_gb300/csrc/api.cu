@@ -409,6 +409,21 @@ hg_status hg_groom_upload(hg_ctx* ctx, const hg_gpu_bundle* bundles, uint32_t bu
     }
     alloc(g->strand_base, base.size() * 4);
     alloc(g->strand_bundle, (size_t)g->strand_total * 4);
+    // The DOM depth pass's order for a full draw (every strand; its refs then
+    // sit at base[b] + s): bundles in the order of a multiplicative hash of
+    // their index, so that strands drawn at the same time come from bundles
+    // far apart and contend less for the same texels.
+    std::vector<uint32_t> hashed(bundle_count), dom_order;
+    for (uint32_t b = 0; b < bundle_count; ++b) hashed[b] = b;
+    std::stable_sort(hashed.begin(), hashed.end(),
+                     [](uint32_t x, uint32_t y) { return x * 0x9e3779b1u < y * 0x9e3779b1u; });
+    dom_order.reserve(g->strand_total);
+    for (uint32_t b : hashed)
+        for (uint32_t r = base[b]; r < base[b + 1]; ++r) dom_order.push_back(r);
+    alloc(g->dom_order, (size_t)g->strand_total * 4);
+    if (e == cudaSuccess && g->strand_total)
+        e = cudaMemcpyAsync(g->dom_order, dom_order.data(), dom_order.size() * 4, cudaMemcpyHostToDevice,
+                            ctx->stream);
     if (e == cudaSuccess) e = cudaMemcpyAsync(g->strand_base, base.data(), base.size() * 4, cudaMemcpyHostToDevice,
                                               ctx->stream);
     if (e == cudaSuccess && g->strand_total)
@@ -445,6 +460,7 @@ hg_status hg_groom_destroy(hg_ctx* ctx, hg_groom* g) {
     free_dev(g->style);
     free_dev(g->strand_base);
     free_dev(g->strand_bundle);
+    free_dev(g->dom_order);
     free_dev(g->cache);
     for (int s = 0; s < 2; ++s) {
         free_dev(g->lod[s]);

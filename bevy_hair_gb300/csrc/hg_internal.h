@@ -29,6 +29,12 @@ struct hg_groom {
     uint32_t* sorted_off[2] = {nullptr, nullptr};  // scan of n_lod in that order, bundle_count + 1
     uint32_t* draw_order[2] = {nullptr, nullptr};  // permutation of refs, ref_capacity
     uint32_t* order_meta[2] = {nullptr, nullptr};  // (live bundles, order valid)
+    // Draw order of the DOM depth pass when every strand is drawn (the usual
+    // case): the refs of bundles in a hashed order (scheduling only).  Its
+    // atomicMin on the front plane contends when neighbouring strands draw
+    // together; the layers pass, whose counter adds gain from locality, keeps
+    // the bundle order.
+    uint32_t* dom_order = nullptr;  // strand_total
     // Strand cache (hg_generate): world-space control points of every strand.
     uint32_t* strand_bundle = nullptr;  // bundle of each strand, strand_total
     uint32_t* strand_base = nullptr;    // first strand of each bundle, bundle_count + 1

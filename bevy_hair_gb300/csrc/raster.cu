@@ -403,6 +403,8 @@ struct RasterArgs {
     const uint32_t* indirect;
     const uint32_t* draw_order;  // permutation of refs to visit, or nullptr
     const uint32_t* order_meta;  // (live bundles, order valid)
+    const uint32_t* full_order;  // DOM depth pass: permutation for a draw of every strand, or nullptr
+    uint32_t full_total;         // the ref count of such a draw
     const float4* cache;         // strand cache (kCacheCps positions then tangents per strand), or nullptr
     const uint32_t* strand_base; // first strand of each bundle in the cache
     unsigned long long* center;
@@ -1059,6 +1061,10 @@ __global__ void __launch_bounds__(kRasterThreads, raster_min_blocks<MODE>()) ras
     const unsigned long long total = a.indirect[0];
     const uint32_t r0 = (uint32_t)((total * a.part_lo) >> 8), r1 = (uint32_t)((total * a.part_hi) >> 8);
     const uint32_t* order = a.draw_order && a.order_meta[1] ? a.draw_order : nullptr;
+    // A draw of every strand (no bundle culled or thinned: then, and only
+    // then, the ref count is the groom's strand count) lays its refs out as
+    // full_order expects.
+    if (MODE == 1 && a.full_order && total == (unsigned long long)a.full_total) order = a.full_order;
     const uint32_t nwarps = gridDim.x * kRasterWarps;
     for (uint32_t r = r0 + blockIdx.x * kRasterWarps + warp; r < r1; r += nwarps) {
         const hg_strand_ref ref = a.refs[order ? order[r] : r];
@@ -1334,6 +1340,8 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
     a.indirect = g->indirect[slot];
     a.draw_order = p.pass_mode[0] == 0u ? g->draw_order[slot] : nullptr;
     a.order_meta = g->order_meta[slot];
+    a.full_order = p.pass_mode[0] == 1u ? g->dom_order : nullptr;
+    a.full_total = g->strand_total;
     const bool cached = g->cache && g->cache_valid &&
                         std::memcmp(g->cache_model, p.world_from_model, sizeof(g->cache_model)) == 0;
     a.cache = cached ? g->cache : nullptr;
