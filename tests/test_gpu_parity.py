@@ -560,3 +560,18 @@ def test_full_size_visibility_bit_exact(renderer, name):
     want = _oracle_visibility(sc, cam, dom)
     assert (want["center"] != EMPTY).sum() > 20_000
     _check_visibility(got, want)
+
+
+def test_dom_pass_over_part_of_the_bundles(renderer):
+    """A DOM view over the first half of the bundles (pass_mode.y): the depth
+    pass cannot use the hashed order of a full draw and must fall back to the
+    refs' own order; the map stays bit-exact."""
+    sc = configs.config2(scale=0.02)
+    cam, dom = sc.params()
+    dom = dom.copy()
+    dom["pass_mode"][1] = max(1, sc.mesh.bundle_count // 2)
+    got = _visibility(renderer, sc, cam, dom)
+    want = _oracle_visibility(sc, cam, dom)
+    assert int(got["dom_indirect"][0]) < sc.mesh.strand_count()
+    assert (want["dom_depth"][: sc.dom_size[0] * sc.dom_size[1]] != 0xFFFFFFFF).any()
+    _check_visibility(got, want)
