@@ -55,7 +55,8 @@ def parse_args():
     ap.add_argument("--cpu-scale", type=float, default=1.0,
                     help="scale of the CPU sample (strand count and pixel count)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-surrogate", action="store_true", help="skip the shade-model-1 measurement")
+    ap.add_argument("--no-surrogate", action="store_true",
+                    help="skip the learned-surrogate measurements (shade models 1-3)")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-frame (config 4) measurement")
     ap.add_argument("--batch-scale", type=float, default=1.0, help="scale of the config-4 batch")
     return ap.parse_args()
@@ -224,9 +225,11 @@ COMPACT_FLOP_PER_EVAL = 2752  # 2 * (10*32 + 32*32 + 32*3)
 
 
 def surrogate_section(r, cam, lights, flush, stream, reps: int, karis_ms: float, hair_px: int) -> dict | None:
-    """Shade model 1 (the learned surrogate) on the same G-buffer: its time
-    beside the Karis shade, its tensor-core throughput, and both models'
-    error against FP64 lobes on 65,536 held-out samples."""
+    """The learned surrogates on the same G-buffer: the 4 x 64 network (shade
+    model 1 on tcgen05, model 2 on mma.sync) and the compact BSDF network
+    (model 3), their times beside the Karis shade, the 4 x 64 network's
+    tensor-core throughput, and every model's error against FP64 lobes on
+    65,536 held-out samples."""
     import torch
 
     from bevy_hair_gb300 import abi
