@@ -735,7 +735,7 @@ def run_reference_batch(args, world, threads):
     segs = items = 0
     for step in range(max(args.steps, 1)):
         for sc in bs.scenes:
-            cam, dom = sc.params()
+            cam, dom = sc.params(native=False)
             out = oracle.frame(sc.mesh, cam, dom, lights)
             segs += int(out["counts_camera"]["segments"])
             items += 1
@@ -771,7 +771,7 @@ def run_reference(args, rank, world):
     if args.config == 4:
         return run_reference_batch(args, world, threads)
     sc = configs.CONFIGS[args.config](scale)
-    cam, dom = sc.params()
+    cam, dom = sc.params(native=False)  # the uniforms without the product library
     lights = sc.light_array()
     env = bench_env(args.config)
     for _ in range(min(args.warmup, 1)):

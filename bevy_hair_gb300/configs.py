@@ -43,9 +43,12 @@ class Scene:
     directionals: list[host.Directional] = field(default_factory=list)
     exposure: float = 1.0
 
-    def params(self) -> tuple[np.ndarray, np.ndarray]:
-        return host.groom_params(self.view, self.groom, self.mesh.bounds_min, self.mesh.bounds_max,
-                                 self.mesh.bundle_count, self.directionals, self.dom_size)
+    def params(self, native: bool = True) -> tuple[np.ndarray, np.ndarray]:
+        """Camera and DOM uniforms: through the library's native host code, or
+        (native=False) through the NumPy restatement, which loads no library."""
+        fn = host.groom_params if native else host.groom_params_numpy
+        return fn(self.view, self.groom, self.mesh.bounds_min, self.mesh.bounds_max, self.mesh.bundle_count,
+                  self.directionals, self.dom_size)
 
     def light_array(self) -> np.ndarray:
         return pack_lights(self.lights)

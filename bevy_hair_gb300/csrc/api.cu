@@ -34,6 +34,21 @@ hg_status cuda_fail(hg_ctx* ctx, cudaError_t e, const char* where) {
         if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #expr); \
     } while (0)
 
+// A CUDA error already pending on the calling thread (a failed launch of the
+// caller's own, or a device fault) is reported before a pass launches
+// anything, and left in place for the caller: the launch checks below then
+// read only the status of this call's own launches.
+hg_status check_pending(hg_ctx* ctx) {
+    const cudaError_t e = cudaPeekAtLastError();
+    return e == cudaSuccess ? HG_OK : cuda_fail(ctx, e, "a CUDA error was pending before this call");
+}
+
+#define HG_PENDING(ctx)                          \
+    do {                                         \
+        hg_status p_ = check_pending(ctx);       \
+        if (p_ != HG_OK) return p_;              \
+    } while (0)
+
 template <typename T>
 void free_dev(T*& p) {
     if (p) cudaFree((void*)p);
@@ -227,6 +242,7 @@ hg_status hg_env_set(hg_ctx* ctx, const hg_env_desc* env) {
         free_dev(ctx->env_spec);
         free_dev(ctx->env_diff);
         ctx->env_spec_size = ctx->env_spec_levels = ctx->env_diff_size = ctx->env_diff_levels = 0;
+        ctx->env_generation += 1;
         return HG_OK;
     }
     if (!env->specular || !env->diffuse) return fail(ctx, HG_INVALID_ARG, "null cubemap texels");
@@ -239,6 +255,8 @@ hg_status hg_env_set(hg_ctx* ctx, const hg_env_desc* env) {
     free_dev(ctx->env_spec);
     free_dev(ctx->env_diff);
     ctx->env_spec_size = ctx->env_spec_levels = ctx->env_diff_size = ctx->env_diff_levels = 0;
+    // the old cubemaps are gone: graphs that captured them must not replay
+    ctx->env_generation += 1;
     const size_t ns = cube_texels(env->specular_size, env->specular_levels);
     const size_t nd = cube_texels(env->diffuse_size, env->diffuse_levels);
     HG_CUDA(ctx, cudaMalloc((void**)&ctx->env_spec, ns * 4));
@@ -510,6 +528,7 @@ hg_status hg_clear(hg_ctx* ctx) {
     if (!ctx) return HG_INVALID_ARG;
     hg_status s = check_targets(ctx, false);
     if (s != HG_OK) return s;
+    HG_PENDING(ctx);
     HG_CUDA(ctx, guard_writes(ctx, kGbufferBits));
     HG_CUDA(ctx, hg::launch_clear(ctx));
     return HG_OK;
@@ -519,6 +538,7 @@ hg_status hg_clear_dom(hg_ctx* ctx) {
     if (!ctx) return HG_INVALID_ARG;
     hg_status s = check_targets(ctx, true);
     if (s != HG_OK) return s;
+    HG_PENDING(ctx);
     HG_CUDA(ctx, guard_writes(ctx, 1u << HG_BUF_DOM));
     HG_CUDA(ctx, hg::launch_clear_dom(ctx));
     return HG_OK;
@@ -526,18 +546,21 @@ hg_status hg_clear_dom(hg_ctx* ctx) {
 
 hg_status hg_lod(hg_ctx* ctx, hg_groom* g, const hg_hair_params* p, hg_view_slot slot) {
     if (!ctx || !g || !p || (slot != HG_SLOT_CAMERA && slot != HG_SLOT_DOM)) return HG_INVALID_ARG;
+    HG_PENDING(ctx);
     HG_CUDA(ctx, hg::launch_lod(ctx, g, *p, slot));
     return HG_OK;
 }
 
 hg_status hg_scan(hg_ctx* ctx, hg_groom* g, const hg_hair_params* p, hg_view_slot slot) {
     if (!ctx || !g || !p || (slot != HG_SLOT_CAMERA && slot != HG_SLOT_DOM)) return HG_INVALID_ARG;
+    HG_PENDING(ctx);
     HG_CUDA(ctx, hg::launch_scan(ctx, g, *p, slot));
     return HG_OK;
 }
 
 hg_status hg_generate(hg_ctx* ctx, hg_groom* g, const hg_hair_params* p) {
     if (!ctx || !g || !p) return HG_INVALID_ARG;
+    HG_PENDING(ctx);
     if (!g->cache && g->strand_total) {
         cudaSetDevice(ctx->device);
         size_t bytes = (size_t)g->strand_total * 2u * hg::kStrandCacheCps * sizeof(float4);
@@ -554,6 +577,7 @@ hg_status hg_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params* p, hg_view_s
     if (!ctx || !g || !p || (slot != HG_SLOT_CAMERA && slot != HG_SLOT_DOM)) return HG_INVALID_ARG;
     hg_status s = check_screen(ctx, p);
     if (s != HG_OK) return s;
+    HG_PENDING(ctx);
     HG_CUDA(ctx, guard_writes(ctx, p->pass_mode[0] == 0u ? kGbufferBits : 1u << HG_BUF_DOM));
     HG_CUDA(ctx, hg::launch_raster(ctx, g, *p, slot, p->pass_mode[0] == 0u ? scene_depth : nullptr));
     return HG_OK;
@@ -575,6 +599,7 @@ hg_status hg_shade(hg_ctx* ctx, const hg_hair_params* p, const hg_shade_desc* d)
     if (p->flags[3] && !ctx->dom) return fail(ctx, HG_NOT_READY, "deep opacity enabled without a map");
     if (p->flags[3] && (p->dom_info[0] != (float)ctx->dom_w || p->dom_info[1] != (float)ctx->dom_h))
         return fail(ctx, HG_INVALID_ARG, "camera params dom_info.xy differ from the map size");
+    HG_PENDING(ctx);
     // Stable order by kind: point, spot, directional, rect (shade.wesl:452-518).
     uint32_t n = 0;
     for (uint32_t i = 0; i < d->light_count; ++i)
@@ -599,6 +624,7 @@ hg_status hg_filter(hg_ctx* ctx, const hg_hair_params* p) {
     if (!ctx || !p) return HG_INVALID_ARG;
     hg_status s = check_screen(ctx, p);
     if (s != HG_OK) return s;
+    HG_PENDING(ctx);
     HG_CUDA(ctx, guard_writes(ctx, 1u << HG_BUF_FILTERED | 1u << HG_BUF_FILTERED_DEPTH));
     HG_CUDA(ctx, hg::launch_filter(ctx, *p));
     return HG_OK;
@@ -608,6 +634,7 @@ hg_status hg_composite(hg_ctx* ctx, const hg_hair_params* p, uint32_t source_fil
     if (!ctx || !p) return HG_INVALID_ARG;
     hg_status s = check_screen(ctx, p);
     if (s != HG_OK) return s;
+    HG_PENDING(ctx);
     HG_CUDA(ctx, guard_writes(ctx, kColorBits));
     HG_CUDA(ctx, hg::launch_composite(ctx, *p, source_filtered));
     return HG_OK;
@@ -617,6 +644,7 @@ hg_status hg_clear_color(hg_ctx* ctx, float depth_clear) {
     if (!ctx) return HG_INVALID_ARG;
     hg_status s = check_targets(ctx, false);
     if (s != HG_OK) return s;
+    HG_PENDING(ctx);
     HG_CUDA(ctx, guard_writes(ctx, kColorBits));
     HG_CUDA(ctx, hg::launch_clear_color(ctx, depth_clear));
     return HG_OK;
@@ -646,6 +674,7 @@ hg_status hg_hair_visibility(hg_ctx* ctx, const hg_shadow_light* light, const fl
     if (!ctx || !light || (n && (!points || !visibility))) return HG_INVALID_ARG;
     hg_status s = check_targets(ctx, true);
     if (s != HG_OK) return s;
+    HG_PENDING(ctx);
     HG_CUDA(ctx, hg::launch_visibility(ctx, *light, points, n, visibility));
     return HG_OK;
 }

@@ -66,6 +66,7 @@ struct hg_batch {
     cudaEvent_t uploaded = nullptr;
     uint32_t g_lights = 0, g_ortho = 0;
     float g_exposure = 0.0f;
+    uint64_t g_env = 0;  // ctx->env_generation the graphs were captured at
     cudaEvent_t done = nullptr;
 };
 
@@ -322,7 +323,27 @@ hg_status capture(hg_batch* b) {
     b->g_lights = b->dev.n_lights;
     b->g_ortho = b->dev.ortho;
     b->g_exposure = b->dev.exposure;
+    b->g_env = ctx->env_generation;
     return HG_OK;
+}
+
+// Every batched frame (graph or direct launches) regenerates each item's
+// strand cache with the item's camera transform; the per-groom passes trust
+// the cache when its recorded transform matches theirs.  Before the batched
+// kernels are enqueued the caches are marked stale (a failed enqueue may
+// leave them half written), and once the frame is enqueued the transform is
+// recorded.
+void invalidate_caches(hg_batch* b) {
+    for (uint32_t i = 0; i < b->n; ++i) b->grooms[i]->cache_valid = false;
+}
+
+void note_cache_writes(hg_batch* b) {
+    for (uint32_t i = 0; i < b->n; ++i) {
+        hg_groom* g = b->grooms[i];
+        if (!g->cache) continue;
+        std::memcpy(g->cache_model, b->cam[i].world_from_model, sizeof(g->cache_model));
+        g->cache_valid = true;
+    }
 }
 
 cudaError_t launch_graphs(hg_batch* b) {
@@ -566,6 +587,7 @@ hg_status hg_batch_frame(hg_batch* b, const hg_shade_desc* shade, hg_batch_mode 
     hg_ctx* ctx = b->ctx;
     if (!ready(b)) return fail(ctx, HG_NOT_READY, "set every item's params before a frame");
     cudaSetDevice(ctx->device);
+    BATCH_CUDA(ctx, cudaPeekAtLastError());  // an earlier error is reported, not cleared
     if (mode == HG_BATCH_SEPARATE) {
         if (shade->shade_model != 0u) return fail(ctx, HG_INVALID_ARG, "batched frames shade with model 0");
         BATCH_CUDA(ctx, guard_readback(b));
@@ -580,16 +602,18 @@ hg_status hg_batch_frame(hg_batch* b, const hg_shade_desc* shade, hg_batch_mode 
     refresh_tables(b);
     hg_status s = stage_lights(b, shade);
     if (s != HG_OK) return s;
+    invalidate_caches(b);
     if (mode == HG_BATCH_LAUNCHES) {
         BATCH_CUDA(ctx, enqueue_frame(b));
     } else {
         if (!b->graph_valid || b->g_lights != b->dev.n_lights || b->g_ortho != b->dev.ortho ||
-            b->g_exposure != b->dev.exposure) {
+            b->g_exposure != b->dev.exposure || b->g_env != ctx->env_generation) {
             if ((s = capture(b)) != HG_OK) return s;
         }
         BATCH_CUDA(ctx, upload_tables(b));
         BATCH_CUDA(ctx, launch_graphs(b));
     }
+    note_cache_writes(b);
     BATCH_CUDA(ctx, cudaEventRecord(b->done, ctx->stream));
     return HG_OK;
 }
@@ -627,10 +651,12 @@ hg_status hg_batch_profile(hg_batch* b, const hg_shade_desc* shade, float* ms) {
     hg_ctx* ctx = b->ctx;
     if (!ready(b)) return fail(ctx, HG_NOT_READY, "set every item's params before a frame");
     cudaSetDevice(ctx->device);
+    BATCH_CUDA(ctx, cudaPeekAtLastError());
     BATCH_CUDA(ctx, cudaEventSynchronize(b->done));
     refresh_tables(b);
     hg_status s = stage_lights(b, shade);
     if (s != HG_OK) return s;
+    invalidate_caches(b);
     cudaEvent_t ev[5] = {};
     cudaError_t e = cudaSuccess;
     for (int i = 0; i < 5 && e == cudaSuccess; ++i) e = cudaEventCreate(&ev[i]);
@@ -658,6 +684,7 @@ hg_status hg_batch_profile(hg_batch* b, const hg_shade_desc* shade, float* ms) {
     for (int i = 0; i < 5; ++i)
         if (ev[i]) cudaEventDestroy(ev[i]);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "profiling the batched frame");
+    note_cache_writes(b);
     BATCH_CUDA(ctx, cudaEventRecord(b->done, ctx->stream));
     return HG_OK;
 }
@@ -689,9 +716,11 @@ hg_status hg_batch_tune(hg_batch* b, const hg_shade_desc* shade, hg_batch_tuning
     hg_ctx* ctx = b->ctx;
     if (!ready(b)) return fail(ctx, HG_NOT_READY, "set every item's params before tuning");
     cudaSetDevice(ctx->device);
+    BATCH_CUDA(ctx, cudaPeekAtLastError());
     BATCH_CUDA(ctx, cudaEventSynchronize(b->done));
     hg_status s = stage_lights(b, shade);
     if (s != HG_OK) return s;
+    invalidate_caches(b);
     *count = 0;
     const hg_batch_tuning start = b->tuning;
     hg_batch_tuning best = start;
@@ -746,6 +775,7 @@ hg_status hg_batch_tune(hg_batch* b, const hg_shade_desc* shade, hg_batch_tuning
     build_tables(b);
     b->tables_dirty = false;
     b->graph_valid = false;
+    note_cache_writes(b);
     BATCH_CUDA(ctx, cudaEventRecord(b->done, ctx->stream));
     return HG_OK;
 }

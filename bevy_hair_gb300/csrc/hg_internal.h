@@ -108,6 +108,10 @@ struct hg_ctx {
     uint32_t env_spec_size = 0, env_spec_levels = 0, env_diff_size = 0, env_diff_levels = 0;
     float env_rot[4] = {0.0f, 0.0f, 0.0f, 1.0f};
     float env_intensity = 0.0f;
+    // Bumped by every hg_env_set: a captured batch graph holds the probe's
+    // device pointers, sizes and rotation by value and is re-captured when
+    // this differs from the count it was captured at.
+    uint64_t env_generation = 0;
     std::string last_error;
 };
 

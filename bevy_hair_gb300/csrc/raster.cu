@@ -1470,26 +1470,65 @@ namespace {
 constexpr uint32_t kNoAllocMaxBundles = 65536;
 static __device__ __align__(256) uint32_t g_noalloc_offsets[kNoAllocMaxBundles + 1];
 
-// Device address of g_noalloc_offsets per device ordinal, looked up once.
-// The host-side name g_noalloc_offsets is not a device address, so kernels
-// are only ever given the address from cudaGetSymbolAddress.
+// Device address of g_noalloc_offsets, looked up once per CUDA context.  The
+// host-side name g_noalloc_offsets is not a device address, so kernels are
+// only ever given the address from cudaGetSymbolAddress.  The cache is keyed
+// on the current context's unique ID (cuCtxGetId, reached through the
+// runtime's driver entry points, so the library needs no link to libcuda):
+// after a reset of the device's primary context (cudaDeviceReset) the module
+// is loaded again, the array may sit at another address, and the new
+// context's ID differs, so the address is looked up again.
+using CtxGetCurrentFn = int (*)(void** ctx);
+using CtxGetIdFn = int (*)(void* ctx, unsigned long long* id);
+
+struct NoAllocSlot {
+    unsigned long long ctx_id = 0;  // 0: never looked up (context IDs start at 1)
+    uint32_t* ptr = nullptr;
+};
 constexpr int kNoAllocMaxDevices = 64;
-uint32_t* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+NoAllocSlot g_noalloc_slot[kNoAllocMaxDevices];
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
 std::mutex g_noalloc_mutex;
+
+cudaError_t current_context_id(unsigned long long* id) {
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        void* f0 = nullptr;
+        void* f1 = nullptr;
+        cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound, q1 = q0;
+        cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0);
+        if (e == cudaSuccess)
+            e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1);
+        if (e != cudaSuccess) return e;
+        if (q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1)
+            return cudaErrorNotSupported;
+        g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+        g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f1);
+    }
+    void* ctx = nullptr;
+    if (g_ctx_get_current(&ctx) != 0 || !ctx) return cudaErrorDeviceUninitialized;
+    return g_ctx_get_id(ctx, id) == 0 ? cudaSuccess : cudaErrorDeviceUninitialized;
+}
 
 cudaError_t noalloc_scratch(uint32_t** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+    // makes the device's primary context current (created if need be)
+    if ((e = cudaSetDevice(dev)) != cudaSuccess) return e;
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
+    unsigned long long id = 0;
+    if ((e = current_context_id(&id)) != cudaSuccess) return e;
+    NoAllocSlot& slot = g_noalloc_slot[dev];
+    if (slot.ctx_id != id || !slot.ptr) {
         uint32_t* ptr = nullptr;
         e = cudaGetSymbolAddress((void**)&ptr, g_noalloc_offsets);
         if (e != cudaSuccess) return e;
-        g_noalloc_ptr[dev] = ptr;
+        slot.ptr = ptr;
+        slot.ctx_id = id;
     }
-    *out = g_noalloc_ptr[dev];
+    *out = slot.ptr;
     return cudaSuccess;
 }
 
@@ -1497,15 +1536,20 @@ cudaError_t noalloc_scratch(uint32_t** out) {
 }  // namespace hg
 
 // See include/hairgb.h.  The first call on a device (the device current on
-// the calling thread) looks up the scratch array's device address; make that
-// first call before any stream capture on that device.  Every call shares the
-// one array, so calls that overlap on the GPU (different streams, no ordering
-// between them) race on it; the offsets are fully rewritten by each call, so
-// nothing needs clearing between calls.
+// the calling thread) looks up the scratch array's device address, and so
+// does the first call after that device's primary context was reset; make
+// those calls before any stream capture on that device.  Every call shares
+// the one array, so calls that overlap on the GPU (different streams, no
+// ordering between them) race on it; the offsets are fully rewritten by each
+// call, so nothing needs clearing between calls.  A CUDA error already
+// pending on the calling thread is reported (HG_CUDA_ERROR) before anything
+// is launched and left in place, so the launch checks below see only this
+// call's launches.
 extern "C" hg_status hg_scan_noalloc(const hg_lod_record* lod, uint32_t bundle_count, uint32_t capacity,
                                      hg_strand_ref* refs, uint32_t* indirect, void* stream) {
     if (!indirect || (bundle_count && (!lod || !refs)) || capacity == 0) return HG_INVALID_ARG;
     if (bundle_count > hg::kNoAllocMaxBundles) return HG_CAPACITY_EXCEEDED;
+    if (cudaPeekAtLastError() != cudaSuccess) return HG_CUDA_ERROR;
     uint32_t* offsets = nullptr;
     if (hg::noalloc_scratch(&offsets) != cudaSuccess) return HG_CUDA_ERROR;
     cudaStream_t st = (cudaStream_t)stream;

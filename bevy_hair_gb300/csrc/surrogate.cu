@@ -1061,6 +1061,7 @@ hg_status hg_mlp_samples(hg_ctx* ctx, uint64_t seed, uint64_t first, uint32_t co
     if (!inputs) return fail(ctx, HG_INVALID_ARG, "null inputs buffer");
     if (!std::isfinite(tilt)) return fail(ctx, HG_INVALID_ARG, "non-finite tilt");
     cudaSetDevice(ctx->device);
+    MLP_CUDA(ctx, cudaPeekAtLastError());  // an earlier error is reported, not cleared
     MLP_CUDA(ctx, hg::ensure_device_setup(ctx->device));
     hg::SampleArgs a;
     a.seed = seed;
@@ -1079,6 +1080,7 @@ hg_status hg_mlp_infer(hg_mlp* m, const float* inputs, uint32_t count, float* lo
     if (!m) return HG_INVALID_ARG;
     if (count == 0) return HG_OK;
     if (!inputs || (!lobes && !net)) return fail(m->ctx, HG_INVALID_ARG, "null buffer");
+    MLP_CUDA(m->ctx, cudaPeekAtLastError());
     MLP_CUDA(m->ctx, hg::launch_mlp_infer(m, inputs, count, lobes, net));
     return HG_OK;
 }
@@ -1088,6 +1090,7 @@ hg_status hg_mlp_infer_tc(hg_mlp* m, const float* inputs, uint32_t count, float*
     if (m->arch != HG_MLP_ARCH_DEEP) return fail(m->ctx, HG_INVALID_ARG, "tcgen05 inference runs the 4 x 64 network");
     if (count == 0) return HG_OK;
     if (!inputs || (!lobes && !net)) return fail(m->ctx, HG_INVALID_ARG, "null buffer");
+    MLP_CUDA(m->ctx, cudaPeekAtLastError());
     MLP_CUDA(m->ctx, hg::launch_mlp_infer_tc(m, inputs, count, lobes, net));
     return HG_OK;
 }
@@ -1097,6 +1100,7 @@ hg_status hg_mlp_gradients(hg_mlp* m, const float* inputs, const float* targets,
     if (!m) return HG_INVALID_ARG;
     hg_ctx* ctx = m->ctx;
     if (count == 0 || !inputs || !targets || !grad) return fail(ctx, HG_INVALID_ARG, "empty batch or null buffer");
+    MLP_CUDA(ctx, cudaPeekAtLastError());
     if (m->arch == HG_MLP_ARCH_DEEP) MLP_CUDA(ctx, hg::ensure_scratch(m, count));
     const size_t pf = sizeof(float) * m->n_params;
     MLP_CUDA(ctx, cudaMemsetAsync(m->grad, 0, pf, ctx->stream));
@@ -1117,6 +1121,7 @@ hg_status hg_mlp_train_step(hg_mlp* m, const float* inputs, const float* targets
     hg_ctx* ctx = m->ctx;
     if (count == 0 || !inputs || !targets) return fail(ctx, HG_INVALID_ARG, "empty batch or null buffer");
     if (!(lr >= 0.0f) || !std::isfinite(lr)) return fail(ctx, HG_INVALID_ARG, "learning rate must be finite, >= 0");
+    MLP_CUDA(ctx, cudaPeekAtLastError());
     if (m->arch == HG_MLP_ARCH_DEEP) MLP_CUDA(ctx, hg::ensure_scratch(m, count));
     MLP_CUDA(ctx, hg::run_gradients(m, inputs, targets, count));
     m->step += 1;
@@ -1137,6 +1142,7 @@ hg_status hg_karis_lobes(hg_ctx* ctx, const float* inputs, uint32_t count, float
     if (!inputs || !lobes) return fail(ctx, HG_INVALID_ARG, "null buffer");
     if (!std::isfinite(tilt)) return fail(ctx, HG_INVALID_ARG, "non-finite tilt");
     cudaSetDevice(ctx->device);
+    MLP_CUDA(ctx, cudaPeekAtLastError());
     MLP_CUDA(ctx, hg::launch_karis_lobes(ctx, inputs, count, tilt, lobes));
     return HG_OK;
 }

@@ -374,13 +374,17 @@ hg_status hg_hair_visibility(hg_ctx* ctx, const hg_shadow_light* light, const fl
  * The per-bundle offsets live in a fixed device array of
  * HG_SCAN_NOALLOC_MAX_BUNDLES + 1 words (256 KB) that every device holds while
  * the library is loaded; larger bundle counts return HG_CAPACITY_EXCEEDED.
- * The first call on a device looks up that array's device address, so make
- * the first call on each device before any stream capture on it.  All calls
- * share the one array: calls that can overlap on the GPU (unordered streams)
- * race and must be serialised by the caller.  Each call rewrites the offsets
- * it reads, so nothing has to be cleared between calls.  Returns
- * HG_INVALID_ARG for null pointers or capacity 0 and HG_CUDA_ERROR when a
- * launch fails. */
+ * The first call on a device looks up that array's device address (kept per
+ * CUDA context: after a reset of the device's primary context, e.g. by
+ * cudaDeviceReset, the next call looks it up again), so make the first call
+ * on each device, and the first one after such a reset, before any stream
+ * capture on it.  All calls share the one array: calls that can overlap on
+ * the GPU (unordered streams) race and must be serialised by the caller.
+ * Each call rewrites the offsets it reads, so nothing has to be cleared
+ * between calls.  Returns HG_INVALID_ARG for null pointers or capacity 0,
+ * and HG_CUDA_ERROR when a launch fails or when a CUDA error was already
+ * pending on the calling thread (that error is left in place, and nothing is
+ * launched). */
 hg_status hg_scan_noalloc(const hg_lod_record* lod, uint32_t bundle_count, uint32_t capacity,
                           hg_strand_ref* refs, uint32_t* indirect, void* stream);
 

@@ -10,12 +10,13 @@ there is no Rust toolchain) and records every literal input/expected pair:
 * src/render/pass.rs:1066-1090 and the shaders -- DOM_SIZE / DOM_LAYERS
 
 Usage: python tests/golden/make_reference_kat.py [reference_root]
-(default /root/reference).  The JSON is committed; tests never read the
-reference tree.
+(default: the checkout named by the BEVY_HAIR_REFERENCE environment variable).
+The JSON is committed; tests never read the reference tree.
 """
 from __future__ import annotations
 
 import json
+import os
 import re
 import sys
 from pathlib import Path
@@ -116,7 +117,12 @@ def extract(root: Path) -> dict:
 
 
 def main() -> None:
-    root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    if len(sys.argv) > 1:
+        root = Path(sys.argv[1])
+    elif os.environ.get("BEVY_HAIR_REFERENCE"):
+        root = Path(os.environ["BEVY_HAIR_REFERENCE"])
+    else:
+        sys.exit("usage: make_reference_kat.py REFERENCE_ROOT (or set BEVY_HAIR_REFERENCE)")
     data = extract(root)
     dst = Path(__file__).with_name("reference_kat.json")
     dst.write_text(json.dumps(data, indent=1) + "\n")

@@ -235,3 +235,74 @@ def test_full_size_batch_items_match_the_oracle(renderer):
         np.testing.assert_array_equal(b.read(k, abi.BUF_DOM), want["dom"])
         np.testing.assert_allclose(b.read(k, abi.BUF_COLOR), want["color"], rtol=2e-3, atol=1e-5)
     _close(b, grooms)
+
+
+def test_graph_follows_a_new_light_probe(renderer, batch_scene):
+    """hg_env_set after a graph was captured: the next graph frame must shade
+    with the new probe (the captured graph held the old cubemaps' addresses),
+    exactly as direct launches of the same frame do; and again after the probe
+    is dropped."""
+    from bevy_hair_gb300 import envmap
+
+    bs = batch_scene
+    b, grooms, _ = _make(renderer, bs)
+    lights = bs.light_array()
+    b.frame(lights, abi.BATCH_GRAPH)  # captured without a probe
+    renderer.synchronize()
+    no_probe = _read_all(b, len(grooms))
+    for env in (envmap.procedural(size=64, levels=7, diffuse_size=8),
+                envmap.procedural(seed=7, size=32, levels=6, diffuse_size=8), None):
+        renderer.set_environment(env)
+        b.frame(lights, abi.BATCH_GRAPH)
+        assert renderer.synchronize() == 0
+        graph = _read_all(b, len(grooms))
+        b.frame(lights, abi.BATCH_LAUNCHES)
+        assert renderer.synchronize() == 0
+        _compare(graph, _read_all(b, len(grooms)), colour_exact=True)
+        if env is not None:  # the probe lights the hair: colour changed
+            assert any(np.abs(g[abi.BUF_SHADED] - w[abi.BUF_SHADED]).max() > 1e-4
+                       for g, w in zip(graph, no_probe))
+    _compare(graph, no_probe, colour_exact=True)
+    _close(b, grooms)
+
+
+def test_batched_frame_keeps_the_strand_cache_honest(renderer):
+    """A batched frame rewrites each item's strand cache with the item's own
+    transform.  A per-groom raster afterwards, with the transform the cache
+    held before, must draw its own geometry (the cache is regenerated or
+    ignored), not the batch's."""
+    bs = configs.config4(scale=0.03, items=2)
+    b, grooms, params = _make(renderer, bs)
+    lights = bs.light_array()
+    sc = bs.scenes[0]
+    cam, dom = params[0]
+    moved_cam, moved_dom = cam.copy(), dom.copy()
+    for p in (moved_cam, moved_dom):
+        p["world_from_model"][12] += 40.0  # translate the groom along x
+    w, h, dw, dh = bs.sizes()[0]
+    renderer.ensure_targets(w, h, dw, dh)
+    g = grooms[0]
+    renderer.generate(g, cam)  # cache at the original transform
+    b.set_params(0, moved_cam, moved_dom)
+    b.frame(lights, abi.BATCH_GRAPH)  # cache now at the moved transform
+    assert renderer.synchronize() == 0
+    renderer.clear_dom()
+    renderer.lod(g, dom, abi.SLOT_DOM)
+    renderer.scan(g, dom, abi.SLOT_DOM)
+    renderer.raster(g, dom, abi.SLOT_DOM)  # every DOM strand is at 65 control points
+    renderer.clear()
+    renderer.lod(g, cam, abi.SLOT_CAMERA)
+    renderer.scan(g, cam, abi.SLOT_CAMERA)
+    renderer.raster(g, cam, abi.SLOT_CAMERA)
+    assert renderer.synchronize() == 0
+    cap = max(sc.mesh.strand_count(), 1)
+    center, cons, beta = oracle.clear_targets(w, h)
+    refs, total = oracle.scan(cam, oracle.lod(cam, sc.mesh), cap)
+    oracle.raster(cam, sc.mesh, refs, total, center, cons, beta, None)
+    d = oracle.clear_dom(dw, dh)
+    drefs, dtotal = oracle.scan(dom, oracle.lod(dom, sc.mesh), cap)
+    oracle.raster(dom, sc.mesh, drefs, dtotal, center, cons, beta, d)
+    np.testing.assert_array_equal(renderer.read(abi.BUF_DOM)[:dw * dh], d[:dw * dh])
+    np.testing.assert_array_equal(renderer.read(abi.BUF_CENTER), center)
+    np.testing.assert_array_equal(renderer.read(abi.BUF_CONSERVATIVE), cons)
+    _close(b, grooms)
