@@ -645,6 +645,31 @@ def run_ours(args, rank, world, local):
         for k, p in enumerate(passes):
             acc[p] += ev[k].elapsed_time(ev[k + 1]) / reps
     per_pass = {p: round(v, 4) for p, v in acc.items()}
+
+    # the camera raster kinds (hg_set_camera_raster), each alone after the
+    # same clear / lod / scan, L2 flushed: direct (the default) and binned
+    def camera_ms(mode: int) -> float:
+        r.set_camera_raster(mode)
+        t = []
+        for _ in range(reps + 1):
+            flush.fill_(5)
+            r.clear()
+            r.lod(g, cam, 0)
+            r.scan(g, cam, 0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            r.raster(g, cam, 0)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            t.append(e0.elapsed_time(e1))
+        r.set_camera_raster(abi.CAMERA_RASTER_DIRECT)
+        return float(np.median(t[1:]))
+
+    camera_kinds = {"binned_ms": round(camera_ms(abi.CAMERA_RASTER_BINNED), 4),
+                    "direct_ms": round(camera_ms(abi.CAMERA_RASTER_DIRECT), 4),
+                    "note": "hg_raster of the camera view alone after an L2 flush, median; binned: segments "
+                            "listed per 32x32 tile and resolved in shared memory (bin, scan, sort, resolve, long "
+                            "segments); direct: global atomics per sample in two stages with 8x8 tile depths"}
     surr = None if args.no_surrogate else surrogate_section(r, cam, lights, flush, stream, reps, acc["shade"],
                                                              hair_px)
     small = None if args.no_config1 else small_frame_measure(local, stream, flush, max(args.steps, 10), 3)
@@ -718,8 +743,8 @@ def run_ours(args, rank, world, local):
     e2e_total = time.perf_counter() - t_s
     e2e_value, e2e_ms, _ = aggregate(dist, e2e_total * 1e3, float(seg_c) * args.steps)
     # per frame: clear, 2 x lod, 2 x (scan offsets + expand), clear_dom, generate,
-    # camera raster (2 stages + tile depths between them), 2 x DOM raster,
-    # shade, filter, clear_color, composite
+    # camera raster (direct, the default: 2 stages + tile depths between them),
+    # 2 x DOM raster, shade, filter, clear_color, composite
     launches = 18 * args.steps
 
     cpu = None
@@ -779,6 +804,7 @@ def run_ours(args, rank, world, local):
                    "lights": int(len(lights)), "l2": "flushed between timed steps (256 MB device write)",
                    "parallelism": f"replicas x{world}"},
         "per_pass_ms": per_pass,
+        "camera_raster_kinds": camera_kinds,
         "per_pass_roofline": per_pass_roofline,
         "roofline": roofline,
         "surrogate": surr,

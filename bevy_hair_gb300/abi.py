@@ -67,6 +67,7 @@ LIGHT_POINT, LIGHT_SPOT, LIGHT_DIRECTIONAL, LIGHT_RECT = 0, 1, 2, 3
 LIGHT_CASTS_SHADOWS = 1
 
 SLOT_CAMERA, SLOT_DOM = 0, 1
+CAMERA_RASTER_DIRECT, CAMERA_RASTER_BINNED = 0, 1
 BUF_CENTER, BUF_CONSERVATIVE, BUF_BETA, BUF_DOM = 0, 1, 2, 3
 BUF_SHADED, BUF_SHADED_DEPTH, BUF_FILTERED, BUF_FILTERED_DEPTH = 4, 5, 6, 7
 BUF_COLOR, BUF_DEPTH = 8, 9
@@ -208,6 +209,7 @@ _SIGNATURES = {
     "hg_lod": (_I32, [_VP, _VP, _VP, _I32]),
     "hg_scan": (_I32, [_VP, _VP, _VP, _I32]),
     "hg_raster": (_I32, [_VP, _VP, _VP, _I32, _VP]),
+    "hg_set_camera_raster": (_I32, [_VP, _U32]),
     "hg_generate": (_I32, [_VP, _VP, _VP]),
     "hg_shade": (_I32, [_VP, _VP, C.POINTER(ShadeDesc)]),
     "hg_filter": (_I32, [_VP, _VP]),

@@ -480,6 +480,7 @@ hg_status hg_groom_destroy(hg_ctx* ctx, hg_groom* g) {
     free_dev(g->strand_bundle);
     free_dev(g->dom_order);
     free_dev(g->cache);
+    hg::release_bins(g);
     for (int s = 0; s < 2; ++s) {
         free_dev(g->lod[s]);
         free_dev(g->refs[s]);
@@ -580,6 +581,14 @@ hg_status hg_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params* p, hg_view_s
     HG_PENDING(ctx);
     HG_CUDA(ctx, guard_writes(ctx, p->pass_mode[0] == 0u ? kGbufferBits : 1u << HG_BUF_DOM));
     HG_CUDA(ctx, hg::launch_raster(ctx, g, *p, slot, p->pass_mode[0] == 0u ? scene_depth : nullptr));
+    return HG_OK;
+}
+
+hg_status hg_set_camera_raster(hg_ctx* ctx, uint32_t mode) {
+    if (!ctx) return HG_INVALID_ARG;
+    if (mode != HG_CAMERA_RASTER_DIRECT && mode != HG_CAMERA_RASTER_BINNED)
+        return fail(ctx, HG_INVALID_ARG, "camera raster mode must be HG_CAMERA_RASTER_DIRECT or _BINNED");
+    ctx->camera_raster = mode;
     return HG_OK;
 }
 

@@ -10,6 +10,24 @@
 
 #include "../../include/hairgb.h"
 
+// Scratch of the binned camera raster (raster.cu), per groom, allocated on
+// its first binned frame and grown with the ref capacity and the screen.
+struct hg_bin_buffers {
+    uint32_t ref_cap = 0;         // refs (draw slots) the buffers hold
+    uint32_t tile_cap = 0;        // 32x32 screen tiles
+    size_t pair_cap = 0;          // ref_cap * 126 segments * 4 tiles
+    float4* scr = nullptr;        // ref_cap * 128: screen x, y, ao, in_front of each control point
+    float4* cpw = nullptr;        // ref_cap * 256: world position, then world tangent + w (strands not cached)
+    uint4* rinfo = nullptr;       // ref_cap: cache slot or ~0u, quv | beta_q << 12, control points, ref index
+    uint2* pairs = nullptr;       // pair_cap: (tile, entry) in the order the bin pass emitted them
+    uint32_t* entries = nullptr;  // pair_cap: entries (draw slot << 7 | segment) sorted by tile
+    uint32_t* tile_count = nullptr;  // tile_cap
+    uint32_t* tile_off = nullptr;    // tile_cap + 1
+    uint32_t* cursor = nullptr;      // tile_cap
+    uint32_t* longs = nullptr;       // ref_cap * 126: segments drawn with global atomics
+    uint32_t* meta = nullptr;        // pairs, long segments, largest chunk count, work counter
+};
+
 struct hg_groom {
     hg_gpu_bundle* bundles = nullptr;
     float4* layers = nullptr;  // 2 float4 per GpuLayer
@@ -41,6 +59,7 @@ struct hg_groom {
     float4* cache = nullptr;            // strand_total * 2 * 65 float4, allocated on first use
     bool cache_valid = false;
     float cache_model[16] = {};         // world_from_model the cache was generated with
+    hg_bin_buffers bins;                // binned camera raster scratch
 };
 
 // Learned shading surrogate (surrogate.cu): FP32 master parameters, Adam
@@ -82,6 +101,8 @@ struct hg_ctx {
     // any of its G-buffer words (an upper bound once built, since the words
     // only decrease during the pass).
     uint32_t* tile_depth = nullptr;
+    // Camera raster kind (hg_set_camera_raster): HG_CAMERA_RASTER_BINNED or _DIRECT.
+    uint32_t camera_raster = HG_CAMERA_RASTER_DIRECT;
     // Asynchronous readback (hg_copy_out_async): copies run on copy_stream
     // behind ev_copy_src; ev_copy_done follows the last one.  pending_reads
     // has bit (1 << hg_buffer_id) set for buffers whose copy a later writer
@@ -192,6 +213,7 @@ cudaError_t launch_lod(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int sl
 cudaError_t launch_scan(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot);
 cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int slot, const float* scene);
 cudaError_t launch_generate(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p);
+void release_bins(hg_groom* g);  // frees the binned camera raster's scratch
 constexpr uint32_t kStrandCacheCps = 65;
 
 // shade.cu

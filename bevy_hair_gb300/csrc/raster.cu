@@ -366,6 +366,7 @@ struct alignas(16) StrandSmem {
     float4 cp[128];  // control point: model position, then world position + in_front flag
     float4 ct[128];  // camera: world tangent xyz + w (uvw.z)
     float4 cs[128];  // screen xy, ao; camera: RN(1/n) for the segment's DDA step count n
+    float vd[128];   // camera: view distance of the control point (project_world)
     union {
         struct {
             float4 lp[16];  // layer sample: position, ao
@@ -584,6 +585,7 @@ __device__ __forceinline__ void store_cp(const hg_hair_params& p, StrandSmem& sm
     if (MODE == 0) {
         sm.ct[idx] = make_float4(wt.x, wt.y, wt.z, w);
         sm.cs[idx] = make_float4(pr.screen.x, pr.screen.y, ao, 0.0f);
+        sm.vd[idx] = pr.view_dist;
     } else {
         sm.cs[idx] = make_float4(pr.screen.x, pr.screen.y, 0.0f, 0.0f);
     }
@@ -755,6 +757,20 @@ __device__ __forceinline__ bool hidden_segment(const hg_hair_params& p, const ui
     return lower > held;
 }
 
+// A lower bound of quantize_depth(d) for every d >= dist, within a few units
+// of it and without a division: (dist - near) times a rounded reciprocal of
+// the range differs from the correctly rounded quotient by at most 3 ulp of a
+// value <= 1, i.e. 3 units after the scale by 16777214, plus half a unit for
+// each rounded product, so after truncation the two quantised depths differ
+// by at most 5 (both are clamped the same way, which keeps the bound; a NaN
+// gives 0, which rejects nothing).
+constexpr uint32_t kApproxDepthSlack = 8;
+__device__ __forceinline__ uint32_t approx_depth(float dist, float near_, float inv_range) {
+    const float q = clampf((dist - near_) * inv_range, 0.0f, 1.0f);
+    const uint32_t r = f2u(q * 16777214.0f);
+    return r < 0x00fffffeu ? r : 0x00fffffeu;
+}
+
 // One warp per 8x8 tile: the largest quantised depth among the tile's
 // conservative, centre and beta words (empty words count as the far value
 // 0xffffff, which rejects nothing; pixels beyond the screen edge are never
@@ -802,12 +818,15 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
     // behind the tile depths, has no samples, every other one n + 1 >= 2; the
     // non-empty segments are listed in order with their first sample.
     int32_t carry = 0, runs = 0;
+    float mag = 0.0f;  // largest |coordinate| of the strand's control points
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         int32_t j = (int32_t)lane + 32 * k;
         int32_t cnt = 0;
         if (j < nseg) {
             float4 pa = sm.cp[j], pb = sm.cp[j + 1];
+            mag = fmaxf(mag, fmaxf(fmaxf(fmaxf(fabsf(pa.x), fabsf(pa.y)), fmaxf(fabsf(pa.z), fabsf(pb.x))),
+                                   fmaxf(fabsf(pb.y), fabsf(pb.z))));
             int32_t n = 0;
             if (pa.w != 0.0f || pb.w != 0.0f) {
                 float4 A = sm.cs[j], B = sm.cs[j + 1];
@@ -824,6 +843,18 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
     __syncwarp();
 
     const int32_t total = carry;
+    // Depth pre-test.  A sample's computed view distance lies within
+    // 42 u (M + C) (u = 2^-24; M, C: largest control-point and camera
+    // coordinate) of mix(vd[j], vd[j+1], t) computed in floats: 21 u (M + C)
+    // from the exact linear distance, 12 u (M + C) for each endpoint's, and
+    // below 9 u (M + C) for the float mix; 1e-5 (M + C) is four times that.
+    // approx_depth of the lowered value minus kApproxDepthSlack is then below
+    // the sample's quantised depth, and a sample whose bound is above every
+    // word it could write changes nothing: it is dropped before its exact
+    // position and depth are computed.  Non-finite values never drop a sample.
+    const float cmag = fmaxf(fmaxf(fabsf(cam.x), fabsf(cam.y)), fabsf(cam.z));
+    const float slack = 1e-5f * (__uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(mag))) + cmag);
+    const float inv_range = __frcp_rn(fmaxf(p.screen[3] - p.screen[2], 1e-3f));
     const float r2_max = sqrt_bound(fmaxf(p.appearance[3], 0.05f) * 0.5f);
     const uint32_t beta_q = f2u(clampf(beta, 0.0f, 1.0f) * 255.0f + 0.5f);
     const bool ao_on = p.flags[2] != 0u;
@@ -865,6 +896,11 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
         const uint32_t cur_m0 = on0 ? hi_word_l1(&a.center[pix0]) : 0u;
         const uint32_t cur_c1 = on1 ? hi_word_l1(&a.cons[pix1]) : 0u;
         const uint32_t cur_c2 = on2 ? hi_word_l1(&a.cons[pix2]) : 0u;
+        {
+            const uint32_t held = max(max(cur_c0, cur_m0), max(cur_c1, cur_c2)) >> 8u;
+            const uint32_t bound = approx_depth(mixf(sm.vd[j], sm.vd[j + 1], t) - slack, p.screen[2], inv_range);
+            if (bound > held + kApproxDepthSlack) continue;
+        }
 
         // write_pixel (raster.wgsl:83-115): depth first; the rest of the payload
         // only when some word can still take it.
@@ -1229,6 +1265,547 @@ __global__ void __launch_bounds__(kRasterThreads, 6) batch_raster_kernel(const B
     }
 }
 
+// ------------------------------------------------------------------ binned camera raster
+// The camera pass with each 32x32 screen tile's G-buffer words resolved in
+// shared memory.  Every write is a commutative min, so the words equal the
+// direct pass's.
+//  1. bin_kernel: a warp per ref (in draw order) generates the strand exactly
+//     as the direct pass does, keeps the control points' screen positions (and
+//     world points of strands outside the strand cache), and lists each segment
+//     as (tile, entry) pairs under the tiles its pixel box touches -- at most
+//     2x2 tiles; a segment spanning more goes to a list of long segments.
+//  2. bin_scan_kernel, bin_sort_kernel: per-tile counts scanned, the pairs
+//     counting-sorted into per-tile runs of entries (roughly in draw order).
+//  3. tile_resolve_kernel: a block per (tile, chunk of <= kBinChunk entries)
+//     holds the tile's centre, conservative and beta words in shared memory,
+//     draws the samples of its segments that land in the tile against them
+//     (read-before-write and atomicMin in shared memory), and ends with one
+//     global atomicMin per word it lowered.  long_segment_kernel draws the long
+//     segments with global atomics.
+constexpr int kBinShift = 5;                  // 32x32 pixel tiles
+constexpr int kBinSize = 1 << kBinShift;
+constexpr int kBinPixels = kBinSize * kBinSize;
+constexpr uint32_t kBinChunk = 2048;          // entries per resolve work item
+constexpr int kResolveWarps = 8;
+constexpr int kResolveThreads = kResolveWarps * 32;
+constexpr uint32_t kBinSegBits = 7;           // entry = draw slot << 7 | segment
+constexpr uint32_t kBinMaxSlots = 1u << (32 - kBinSegBits);
+constexpr uint32_t kNoCache = 0xffffffffu;
+
+struct BinDev {
+    float4* scr;
+    float4* cpw;
+    uint4* rinfo;
+    uint2* pairs;
+    uint32_t* entries;
+    uint32_t* tile_count;
+    uint32_t* tile_off;
+    uint32_t* cursor;
+    uint32_t* longs;
+    uint32_t* meta;  // [0] pairs, [1] long segments, [2] largest chunk count of a tile, [3] work counter
+    size_t pair_cap;
+    uint32_t tiles_x, tiles_y;
+};
+
+// Tiles (up to 2x2) whose pixels segment (A, B) can reach, by the same pixel
+// box as hidden_segment: floor(min) - 1 .. floor(max) + 1, clamped to the
+// screen.  Returns the tile count (0: nothing on screen) or -1 for a segment
+// that needs the long path (more than 2x2 tiles, or coordinates beyond 2^20).
+__device__ __forceinline__ int segment_tiles(float4 A, float4 B, int32_t width, int32_t height, uint32_t tiles_x,
+                                             uint32_t tile[4]) {
+    const float lim = 1048576.0f;
+    if (!(fabsf(A.x) < lim && fabsf(A.y) < lim && fabsf(B.x) < lim && fabsf(B.y) < lim)) return -1;
+    const int32_t x0 = max(f2i(floorf(fminf(A.x, B.x))) - 1, 0), x1 = min(f2i(floorf(fmaxf(A.x, B.x))) + 1, width - 1);
+    const int32_t y0 = max(f2i(floorf(fminf(A.y, B.y))) - 1, 0), y1 = min(f2i(floorf(fmaxf(A.y, B.y))) + 1, height - 1);
+    if (x0 > x1 || y0 > y1) return 0;
+    const int32_t tx0 = x0 >> kBinShift, tx1 = x1 >> kBinShift, ty0 = y0 >> kBinShift, ty1 = y1 >> kBinShift;
+    if (tx1 - tx0 > 1 || ty1 - ty0 > 1) return -1;
+    int n = 0;
+    for (int32_t ty = ty0; ty <= ty1; ++ty)
+        for (int32_t tx = tx0; tx <= tx1; ++tx) tile[n++] = (uint32_t)ty * tiles_x + (uint32_t)tx;
+    return n;
+}
+
+// Step 1.  One warp per ref slot r (draw order); entry r << 7 | j for segment j.
+__global__ void __launch_bounds__(kRasterThreads, 6) bin_kernel(const RasterArgs a, const BinDev d) {
+    __shared__ StrandSmem smem[kRasterWarps];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    StrandSmem& sm = smem[warp];
+    const uint32_t total = a.indirect[0];
+    const uint32_t* order = a.draw_order && a.order_meta[1] ? a.draw_order : nullptr;
+    const hg_hair_params& p = a.p;
+    const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
+    const uint32_t nwarps = gridDim.x * kRasterWarps;
+    for (uint32_t r = blockIdx.x * kRasterWarps + warp; r < total; r += nwarps) {
+        const uint32_t ri = order ? order[r] : r;
+        const hg_strand_ref ref = a.refs[ri];
+        if (ref.bundle >= a.bundle_count) {
+            if (lane == 0) atomicOr(a.err, kErrBadRef);
+            continue;
+        }
+        const hg_gpu_bundle bundle = a.bundles[ref.bundle];
+        const float2 uv = pcg_uv(ref.strand ^ (ref.bundle * 0x85ebca6bu));
+        const uint32_t ncp = generate_strand<0>(a, sm, ref, bundle, uv, lane);
+        const bool cached = a.cache && ncp == kCacheCps;
+        if (lane == 0) {
+            const float beta = __fdiv_rn(__uint2float_rn(ref.n_lod), __uint2float_rn(max(bundle.strand_count, 1u)));
+            const uint32_t beta_q = f2u(clampf(beta, 0.0f, 1.0f) * 255.0f + 0.5f);
+            const uint32_t quv = quant63(uv.x) | quant63(uv.y) << 6u;
+            d.rinfo[r] = make_uint4(cached ? a.strand_base[ref.bundle] + ref.strand : kNoCache, quv | beta_q << 12u,
+                                    ncp, ri);
+        }
+        float4* scr = d.scr + (size_t)r * 128u;
+        float4* cpw = d.cpw + (size_t)r * 256u;
+        for (uint32_t idx = lane; idx < ncp; idx += 32u) {
+            const float4 cs = sm.cs[idx], cp = sm.cp[idx];
+            scr[idx] = make_float4(cs.x, cs.y, cs.z, cp.w);
+            if (!cached) {
+                cpw[idx] = make_float4(cp.x, cp.y, cp.z, 0.0f);
+                cpw[128u + idx] = sm.ct[idx];
+            }
+        }
+        const int32_t nseg = (int32_t)ncp - 1;
+#pragma unroll 1
+        for (int k = 0; k < 4; ++k) {
+            const int32_t j = (int32_t)lane + 32 * k;
+            uint32_t tile[4] = {kNoCache, kNoCache, kNoCache, kNoCache};
+            int nt = 0;
+            if (j < nseg) {
+                const float4 pa = sm.cp[j], pb = sm.cp[j + 1];
+                if (pa.w != 0.0f || pb.w != 0.0f) nt = segment_tiles(sm.cs[j], sm.cs[j + 1], width, height, d.tiles_x, tile);
+            }
+            const uint32_t entry = r << kBinSegBits | (uint32_t)j;
+            // long segments
+            const uint32_t lmask = __ballot_sync(0xffffffffu, nt < 0);
+            if (lmask) {
+                uint32_t lbase = 0;
+                if (lane == 0) lbase = atomicAdd(&d.meta[1], __popc(lmask));
+                lbase = __shfl_sync(0xffffffffu, lbase, 0);
+                if (nt < 0) d.longs[lbase + __popc(lmask & ((1u << lane) - 1u))] = entry;
+                if (nt < 0) nt = 0;
+            }
+            // (tile, entry) pairs: one reservation per warp round
+            int32_t incl = nt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int32_t)lane >= o) incl += y;
+            }
+            const uint32_t round_total = (uint32_t)__shfl_sync(0xffffffffu, incl, 31);
+            if (round_total == 0) continue;
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(&d.meta[0], round_total);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            const uint32_t mine = base + (uint32_t)(incl - nt);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                if (q < nt) d.pairs[mine + q] = make_uint2(tile[q], entry);
+                // per-tile counts, one atomic per distinct tile of the round
+                const uint32_t key = q < nt ? tile[q] : kNoCache;
+                const uint32_t group = __match_any_sync(0xffffffffu, key);
+                if (key != kNoCache && lane == (uint32_t)(__ffs(group) - 1))
+                    atomicAdd(&d.tile_count[key], (uint32_t)__popc(group));
+            }
+        }
+    }
+}
+
+// Step 2a (one block): tile offsets, the sort cursors and the largest chunk
+// count; resets the resolve work counter.
+__global__ void __launch_bounds__(kScanThreads) bin_scan_kernel(const BinDev d) {
+    __shared__ uint32_t warp_sums[33];
+    __shared__ uint32_t s_max;
+    const uint32_t tiles = d.tiles_x * d.tiles_y;
+    if (threadIdx.x == 0) s_max = 0;
+    __syncthreads();
+    uint32_t carry = 0, local_max = 0;
+    for (uint32_t base = 0; base < tiles; base += kScanThreads * kScanItems)
+        carry += scan_pass(
+            base, tiles, carry, warp_sums,
+            [&](uint32_t i) {
+                const uint32_t c = d.tile_count[i];
+                local_max = max(local_max, (c + kBinChunk - 1) / kBinChunk);
+                return c;
+            },
+            [&](uint32_t i, uint32_t at) {
+                d.tile_off[i] = at;
+                d.cursor[i] = at;
+            });
+    atomicMax(&s_max, local_max);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        d.tile_off[tiles] = carry;
+        d.meta[2] = s_max;
+        d.meta[3] = 0u;
+    }
+}
+
+// Step 2b: pairs into per-tile runs (one atomic per distinct tile of a warp).
+__global__ void bin_sort_kernel(const BinDev d) {
+    const uint32_t n = (uint32_t)min((size_t)d.meta[0], d.pair_cap);
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const uint2 pr = i < n ? d.pairs[i] : make_uint2(kNoCache, 0u);
+        const uint32_t group = __match_any_sync(0xffffffffu, pr.x);
+        const uint32_t leader = (uint32_t)(__ffs(group) - 1);
+        uint32_t at = 0;
+        if (pr.x != kNoCache && lane == leader) at = atomicAdd(&d.cursor[pr.x], (uint32_t)__popc(group));
+        at = __shfl_sync(0xffffffffu, at, (int)leader);
+        if (pr.x != kNoCache) d.entries[at + __popc(group & ((1u << lane) - 1u))] = pr.y;
+    }
+}
+
+// A warp's batch of up to 32 segments in the resolve pass.
+struct alignas(16) SegStage {
+    float4 A[32], B[32];    // screen x, y, ao; A.w = RN(1/n), B.w = depth pre-test slack
+    float4 pa[32], pb[32];  // world position, view distance
+    float4 ta[32], tb[32];  // world tangent, w
+    uint32_t meta[32];      // quv | beta_q << 12
+    int32_t off[32];        // runs: first sample, in order
+    int32_t seg[32];        // runs: batch slot | DDA steps n << 8
+};
+
+__device__ __forceinline__ uint32_t shared_hi(const unsigned long long* w) {
+    return reinterpret_cast<const uint32_t*>(w)[1];
+}
+
+// Step 3.  Persistent blocks take work items v = chunk * tiles + tile from a
+// counter, so every tile's first chunk is drawn before any second one.
+__global__ void __launch_bounds__(kResolveThreads, 3) tile_resolve_kernel(const RasterArgs a, const BinDev d) {
+    __shared__ unsigned long long s_center[kBinPixels], s_cons[kBinPixels];
+    __shared__ uint32_t s_beta[kBinPixels];
+    __shared__ uint32_t s_dirty[3][kBinPixels / 32];  // cons, centre, beta words lowered here
+    __shared__ SegStage stage[kResolveWarps];
+    __shared__ uint32_t s_item;
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    const hg_hair_params& p = a.p;
+    const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
+    const uint32_t tiles = d.tiles_x * d.tiles_y;
+    const uint32_t v_end = tiles * d.meta[2];
+    const f3 cam = mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2]);
+    const f3 fwd = mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]);
+    const float cmag = fmaxf(fmaxf(fabsf(cam.x), fabsf(cam.y)), fabsf(cam.z));
+    const float inv_range = __frcp_rn(fmaxf(p.screen[3] - p.screen[2], 1e-3f));
+    const float r2_max = sqrt_bound(fmaxf(p.appearance[3], 0.05f) * 0.5f);
+    const bool ao_on = p.flags[2] != 0u;
+    const bool rev = p.pass_mode[2] == 1u;
+    SegStage& st = stage[warp];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(&d.meta[3], 1u);
+        __syncthreads();
+        const uint32_t v = s_item;
+        __syncthreads();  // s_item is rewritten at the next item
+        if (v >= v_end) break;
+        const uint32_t chunk = v / tiles, tile = v - chunk * tiles;
+        const uint32_t e_lo = d.tile_off[tile], e_hi = d.tile_off[tile + 1];
+        const uint32_t e0 = e_lo + chunk * kBinChunk;
+        if (e0 >= e_hi) continue;
+        const uint32_t e1 = min(e_hi, e0 + kBinChunk);
+        const int32_t tx = (int32_t)(tile % d.tiles_x), ty = (int32_t)(tile / d.tiles_x);
+        const int32_t ox = tx << kBinShift, oy = ty << kBinShift;
+        // The tile's words: empty for a tile's first chunk, else what global
+        // memory holds now (any upper bound of the final words is correct).
+        for (int q = threadIdx.x; q < kBinPixels; q += kResolveThreads) {
+            const int32_t x = ox + (q & (kBinSize - 1)), y = oy + (q >> kBinShift);
+            unsigned long long c = kEmptyU64, m = kEmptyU64;
+            uint32_t bw = 0xffffffffu;
+            if (chunk > 0 && x < width && y < height) {
+                const size_t gi = (size_t)y * (size_t)width + (size_t)x;
+                c = __ldcg(&a.cons[gi]);
+                m = __ldcg(&a.center[gi]);
+                bw = __ldcg(&a.beta[gi]);
+            }
+            s_cons[q] = c;
+            s_center[q] = m;
+            s_beta[q] = bw;
+        }
+        for (int q = threadIdx.x; q < 3 * kBinPixels / 32; q += kResolveThreads) (&s_dirty[0][0])[q] = 0u;
+        __syncthreads();
+
+        for (uint32_t wb = e0 + warp * 32u; wb < e1; wb += kResolveWarps * 32u) {
+            // stage this warp's segments (lane k: entry wb + k)
+            const uint32_t e = wb + lane;
+            int32_t cnt = 0;
+            if (e < e1) {
+                const uint32_t entry = d.entries[e];
+                const uint32_t r = entry >> kBinSegBits, j = entry & ((1u << kBinSegBits) - 1u);
+                const uint4 info = d.rinfo[r];
+                const float4* pos;
+                const float4* tan;
+                if (info.x != kNoCache) {
+                    pos = a.cache + (size_t)info.x * (2u * kCacheCps);
+                    tan = pos + kCacheCps;
+                } else {
+                    pos = d.cpw + (size_t)r * 256u;
+                    tan = pos + 128;
+                }
+                const float4* scr = d.scr + (size_t)r * 128u;
+                float4 A = __ldg(scr + j), B = __ldg(scr + j + 1);
+                float4 pa = __ldg(pos + j), pb = __ldg(pos + j + 1);
+                const float4 ta = __ldg(tan + j), tb = __ldg(tan + j + 1);
+                const float dx = B.x - A.x, dy = B.y - A.y;
+                const int32_t n = min(max(f2i(ceilf(fmaxf(fabsf(dx), fabsf(dy)))), 1), kMaxSteps);
+                cnt = n + 1;
+                const float m = fmaxf(fmaxf(fmaxf(fabsf(pa.x), fabsf(pa.y)), fmaxf(fabsf(pa.z), fabsf(pb.x))),
+                                      fmaxf(fabsf(pb.y), fabsf(pb.z)));
+                pa.w = dot3(sub3(xyz(pa), cam), fwd);
+                pb.w = dot3(sub3(xyz(pb), cam), fwd);
+                A.w = __frcp_rn(__int2float_rn(n));
+                B.w = 1e-5f * (m + cmag);
+                st.A[lane] = A;
+                st.B[lane] = B;
+                st.pa[lane] = pa;
+                st.pb[lane] = pb;
+                st.ta[lane] = ta;
+                st.tb[lane] = tb;
+                st.meta[lane] = info.y;
+            }
+            // runs: segment k's samples follow segment k-1's
+            int32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if ((int32_t)lane >= o) incl += y;
+            }
+            const uint32_t live = __ballot_sync(0xffffffffu, cnt > 0);
+            if (cnt > 0) {
+                const int32_t rr = __popc(live & ((1u << lane) - 1u));
+                st.off[rr] = incl - cnt;
+                st.seg[rr] = (int32_t)lane | (cnt - 1) << 8;
+            }
+            const int32_t total = __shfl_sync(0xffffffffu, incl, 31);
+            const int32_t runs = __popc(live);
+            __syncwarp();
+
+            int32_t carry_px = 0, carry_py = 0, rw = 0;
+            for (int32_t base = 0; base < total; base += 32) {
+                const int32_t s = min(base + (int32_t)lane, total - 1);
+                const bool active = base + (int32_t)lane < total;
+                // run of this lane's sample (as run_of_lane, over the stage)
+                const int32_t rk = rw + 1 + (int32_t)lane;
+                const int32_t okk = rk < runs ? st.off[rk] : 0x7fffffff;
+                const int32_t rel = okk - base;
+                const uint32_t starts = __reduce_or_sync(0xffffffffu, rel > 0 && rel < 32 ? 1u << rel : 0u);
+                const int32_t rn = rw + __popc(starts & (0xffffffffu >> (31u - lane)));
+                rw += __popc(__ballot_sync(0xffffffffu, okk <= base + 32));
+                const int32_t jn = st.seg[rn];
+                const int32_t k = jn & 0xff, i = s - st.off[rn];
+                const float4 A = st.A[k], B = st.B[k];
+                const float t = step_t(i, jn >> 8, A.w);
+                const float sx = mixf(A.x, B.x, t), sy = mixf(A.y, B.y, t);
+                const int32_t px = f2i(floorf(sx)), py = f2i(floorf(sy));
+                int32_t qx = __shfl_up_sync(0xffffffffu, px, 1), qy = __shfl_up_sync(0xffffffffu, py, 1);
+                if (lane == 0) {
+                    qx = carry_px;
+                    qy = carry_py;
+                }
+                carry_px = __shfl_sync(0xffffffffu, px, 31);
+                carry_py = __shfl_sync(0xffffffffu, py, 31);
+                if (!active) continue;
+                const bool side = i > 0 && qx != px && qy != py;
+                auto in_tile = [&](int32_t x, int32_t y) {
+                    return on_screen(x, y, width, height) && (x >> kBinShift) == tx && (y >> kBinShift) == ty;
+                };
+                const bool on0 = in_tile(px, py);
+                const bool on1 = side && in_tile(qx, py);
+                const bool on2 = side && in_tile(px, qy);
+                if (!(on0 || on1 || on2)) continue;
+                const int32_t l0 = ((py - oy) << kBinShift) + (px - ox);
+                const int32_t l1 = ((py - oy) << kBinShift) + (qx - ox);
+                const int32_t l2 = ((qy - oy) << kBinShift) + (px - ox);
+                const uint32_t cur_c0 = on0 ? shared_hi(&s_cons[l0]) : 0u;
+                const uint32_t cur_m0 = on0 ? shared_hi(&s_center[l0]) : 0u;
+                const uint32_t cur_c1 = on1 ? shared_hi(&s_cons[l1]) : 0u;
+                const uint32_t cur_c2 = on2 ? shared_hi(&s_cons[l2]) : 0u;
+                const float4 pa = st.pa[k], pb = st.pb[k];
+                {
+                    const uint32_t held = max(max(cur_c0, cur_m0), max(cur_c1, cur_c2)) >> 8u;
+                    const uint32_t bound = approx_depth(mixf(pa.w, pb.w, t) - B.w, p.screen[2], inv_range);
+                    if (bound > held + kApproxDepthSlack) continue;
+                }
+                // write_pixel (raster.wgsl:83-115), as raster_camera
+                const f3 world = mix3(xyz(pa), xyz(pb), t);
+                const float dist = dot3(sub3(world, cam), fwd);
+                if (dist <= p.screen[2]) continue;
+                const uint32_t depth = quantize_depth(dist, p.screen[2], p.screen[3]);
+                const uint32_t lower = depth << 8u;
+                bool w0 = on0 && lower <= cur_c0;
+                bool wm = on0 && depth <= cur_m0 >> 8u;
+                bool w1 = on1 && lower <= cur_c1;
+                bool w2 = on2 && lower <= cur_c2;
+                if (wm) {
+                    const float cx = __int2float_rn(px) + 0.5f, cy = __int2float_rn(py) + 0.5f;
+                    const float gx = B.x - A.x, gy = B.y - A.y;
+                    const float denom = fmaxf(gx * gx + gy * gy, 1e-6f);
+                    const float closest = clampf(__fdiv_rn((cx - A.x) * gx + (cy - A.y) * gy, denom), 0.0f, 1.0f);
+                    const float ox2 = cx - (A.x + gx * closest), oy2 = cy - (A.y + gy * closest);
+                    wm = ox2 * ox2 + oy2 * oy2 <= r2_max;
+                }
+                if (!(w0 || wm || w1 || w2)) continue;
+                if (a.scene) {
+                    const float4 clip = mat_mul(p.clip_from_world, world.x, world.y, world.z, 1.0f);
+                    const float clip_depth = __fdiv_rn(clip.z, fmaxf(clip.w, 1e-5f));
+                    auto hidden = [&](int32_t x, int32_t y) {
+                        const float scene = __ldg(&a.scene[(size_t)y * (size_t)width + (size_t)x]);
+                        return rev ? clip_depth < scene : clip_depth > scene;
+                    };
+                    if ((w0 || wm) && hidden(px, py)) w0 = wm = false;
+                    if (w1 && hidden(qx, py)) w1 = false;
+                    if (w2 && hidden(px, qy)) w2 = false;
+                    if (!(w0 || wm || w1 || w2)) continue;
+                }
+                const float4 t0 = st.ta[k], t1 = st.tb[k];
+                const f3 tangent = safe_normalize(mix3(xyz(t0), xyz(t1), t));
+                const uint32_t oct = oct_encode(tangent);
+                const uint32_t ao_q = ao_on ? f2u(clampf(mixf(A.z, B.z, t), 0.0f, 1.0f) * 63.0f + 0.5f) : 63u;
+                const uint32_t mt = st.meta[k];
+                const unsigned long long payload = pack_gb(depth, oct & 0xffu, oct >> 8u, mt & 0x3fu, (mt >> 6u) & 0x3fu,
+                                                           quant63(mixf(t0.w, t1.w, t)), ao_q);
+                const uint32_t high = (uint32_t)(payload >> 32u);
+                auto lower_word = [&](unsigned long long* w, uint32_t* mask, int32_t l) {
+                    if (payload < atomicMin(w, payload)) atomicOr(&mask[l >> 5], 1u << (l & 31));
+                };
+                if (w0 && high <= cur_c0) lower_word(&s_cons[l0], s_dirty[0], l0);
+                if (wm) {
+                    if (high <= cur_m0) lower_word(&s_center[l0], s_dirty[1], l0);
+                    const uint32_t bw = (depth << 8u) | (mt >> 12u);
+                    if (bw < atomicMin(&s_beta[l0], bw)) atomicOr(&s_dirty[2][l0 >> 5], 1u << (l0 & 31));
+                }
+                if (w1 && high <= cur_c1) lower_word(&s_cons[l1], s_dirty[0], l1);
+                if (w2 && high <= cur_c2) lower_word(&s_cons[l2], s_dirty[0], l2);
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+        // one global atomicMin per word this item lowered
+        for (int q = threadIdx.x; q < kBinPixels; q += kResolveThreads) {
+            const uint32_t bit = 1u << (q & 31);
+            const uint32_t dc = s_dirty[0][q >> 5] & bit, dm = s_dirty[1][q >> 5] & bit, db = s_dirty[2][q >> 5] & bit;
+            if (!(dc | dm | db)) continue;
+            const int32_t x = ox + (q & (kBinSize - 1)), y = oy + (q >> kBinShift);
+            const size_t gi = (size_t)y * (size_t)width + (size_t)x;
+            if (dc) atomicMin(&a.cons[gi], s_cons[q]);
+            if (dm) atomicMin(&a.center[gi], s_center[q]);
+            if (db) atomicMin(&a.beta[gi], s_beta[q]);
+        }
+        __syncthreads();
+    }
+}
+
+// The long segments: one warp each, drawn as a one-segment strand by
+// raster_camera (global atomics).
+__global__ void __launch_bounds__(kRasterThreads) long_segment_kernel(const RasterArgs a, const BinDev d) {
+    __shared__ StrandSmem smem[kRasterWarps];
+    const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
+    StrandSmem& sm = smem[warp];
+    const uint32_t n = d.meta[1];
+    const hg_hair_params& p = a.p;
+    const f3 cam = mk3(p.camera_pos[0], p.camera_pos[1], p.camera_pos[2]);
+    const f3 fwd = mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]);
+    for (uint32_t q = blockIdx.x * kRasterWarps + warp; q < n; q += gridDim.x * kRasterWarps) {
+        const uint32_t entry = d.longs[q];
+        const uint32_t r = entry >> kBinSegBits, j = entry & ((1u << kBinSegBits) - 1u);
+        const uint4 info = d.rinfo[r];
+        const hg_strand_ref ref = a.refs[info.w];
+        const hg_gpu_bundle bundle = a.bundles[ref.bundle];
+        const float2 uv = pcg_uv(ref.strand ^ (ref.bundle * 0x85ebca6bu));
+        const float beta = __fdiv_rn(__uint2float_rn(ref.n_lod), __uint2float_rn(max(bundle.strand_count, 1u)));
+        if (lane < 2u) {
+            const float4* pos;
+            const float4* tan;
+            if (info.x != kNoCache) {
+                pos = a.cache + (size_t)info.x * (2u * kCacheCps);
+                tan = pos + kCacheCps;
+            } else {
+                pos = d.cpw + (size_t)r * 256u;
+                tan = pos + 128;
+            }
+            const float4 sc = d.scr[(size_t)r * 128u + j + lane];
+            const float4 wp = pos[j + lane];
+            sm.cp[lane] = make_float4(wp.x, wp.y, wp.z, sc.w);
+            sm.ct[lane] = tan[j + lane];
+            sm.cs[lane] = make_float4(sc.x, sc.y, sc.z, 0.0f);
+            sm.vd[lane] = dot3(sub3(xyz(wp), cam), fwd);
+        }
+        __syncwarp();
+        raster_camera(a, sm, 2u, uv, beta, lane);
+        __syncwarp();
+    }
+}
+
+void free_bins(hg_bin_buffers& b) {
+    for (void* ptr : {(void*)b.scr, (void*)b.cpw, (void*)b.rinfo, (void*)b.pairs, (void*)b.entries,
+                      (void*)b.tile_count, (void*)b.tile_off, (void*)b.cursor, (void*)b.longs, (void*)b.meta})
+        if (ptr) cudaFree(ptr);
+    b = hg_bin_buffers{};
+}
+
+// The binned pass's scratch for this groom and a screen of `tiles` tiles.
+cudaError_t ensure_bins(hg_groom* g, uint32_t tiles) {
+    hg_bin_buffers& b = g->bins;
+    if (b.meta && b.ref_cap >= g->ref_capacity && b.tile_cap >= tiles) return cudaSuccess;
+    free_bins(b);
+    const size_t refs = g->ref_capacity;
+    b.pair_cap = refs * 126u * 4u;
+    cudaError_t e = cudaSuccess;
+    auto alloc = [&](auto*& ptr, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc((void**)&ptr, std::max<size_t>(bytes, 16));
+    };
+    alloc(b.scr, refs * 128u * sizeof(float4));
+    alloc(b.cpw, refs * 256u * sizeof(float4));
+    alloc(b.rinfo, refs * sizeof(uint4));
+    alloc(b.pairs, b.pair_cap * sizeof(uint2));
+    alloc(b.entries, b.pair_cap * sizeof(uint32_t));
+    alloc(b.tile_count, (size_t)tiles * 4u);
+    alloc(b.tile_off, ((size_t)tiles + 1u) * 4u);
+    alloc(b.cursor, (size_t)tiles * 4u);
+    alloc(b.longs, refs * 126u * 4u);
+    alloc(b.meta, 4u * 4u);
+    if (e != cudaSuccess) {
+        free_bins(b);
+        return e;
+    }
+    b.ref_cap = (uint32_t)refs;
+    b.tile_cap = tiles;
+    return cudaSuccess;
+}
+
+cudaError_t launch_camera_binned(hg_ctx* ctx, hg_groom* g, const RasterArgs& a) {
+    const uint32_t tiles_x = (ctx->width + kBinSize - 1) >> kBinShift;
+    const uint32_t tiles_y = (ctx->height + kBinSize - 1) >> kBinShift;
+    cudaError_t e = ensure_bins(g, tiles_x * tiles_y);
+    if (e != cudaSuccess) return e;
+    hg_bin_buffers& b = g->bins;
+    BinDev d;
+    d.scr = b.scr;
+    d.cpw = b.cpw;
+    d.rinfo = b.rinfo;
+    d.pairs = b.pairs;
+    d.entries = b.entries;
+    d.tile_count = b.tile_count;
+    d.tile_off = b.tile_off;
+    d.cursor = b.cursor;
+    d.longs = b.longs;
+    d.meta = b.meta;
+    d.pair_cap = b.pair_cap;
+    d.tiles_x = tiles_x;
+    d.tiles_y = tiles_y;
+    if ((e = cudaMemsetAsync(b.tile_count, 0, (size_t)tiles_x * tiles_y * 4u, ctx->stream)) != cudaSuccess) return e;
+    if ((e = cudaMemsetAsync(b.meta, 0, 16, ctx->stream)) != cudaSuccess) return e;
+    const int bin_blocks = (int)std::max<size_t>((g->ref_capacity + kRasterWarps - 1) / kRasterWarps, 1);
+    bin_kernel<<<bin_blocks, kRasterThreads, 0, ctx->stream>>>(a, d);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    bin_scan_kernel<<<1, kScanThreads, 0, ctx->stream>>>(d);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    bin_sort_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(d);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    tile_resolve_kernel<<<ctx->sm_count * 3, kResolveThreads, 0, ctx->stream>>>(a, d);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    long_segment_kernel<<<ctx->sm_count * 2, kRasterThreads, 0, ctx->stream>>>(a, d);
+    return cudaGetLastError();
+}
+
 int blocks_for(hg_ctx* ctx, const void* fn, int threads, size_t work_items, int per_block_items) {
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, 0);
@@ -1259,6 +1836,8 @@ cudaError_t launch_clear_arena(hg_ctx* ctx, const BatchDev& b) {
 }
 
 }  // namespace
+
+void release_bins(hg_groom* g) { free_bins(g->bins); }
 
 cudaError_t launch_clear(hg_ctx* ctx) {
     size_t pixels = (size_t)ctx->width * ctx->height;
@@ -1361,7 +1940,9 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
     // One warp per ref slot, no persistence: raster launches on different
     // streams then share the SMs through the block scheduler.
     int blocks = (int)std::max<size_t>((g->ref_capacity + kRasterWarps - 1) / kRasterWarps, 1);
-    if (mode == 0) {
+    if (mode == 0 && ctx->camera_raster == HG_CAMERA_RASTER_BINNED && g->ref_capacity <= kBinMaxSlots) {
+        return launch_camera_binned(ctx, g, a);
+    } else if (mode == 0) {
         // Refs in draw order (near bundles first), in stages; before each
         // stage after the first, the tile depths are rebuilt from the words
         // the earlier stages left, and segments behind them are skipped.

@@ -263,6 +263,12 @@ class HairRenderer:
         _check(self.lib, self.ctx,
                self.lib.hg_raster(self.ctx, groom.handle, params.ctypes.data, slot, scene_depth_ptr))
 
+    def set_camera_raster(self, mode: int) -> None:
+        """abi.CAMERA_RASTER_DIRECT (global atomics per sample, the default) or
+        abi.CAMERA_RASTER_BINNED (32x32 tiles resolved in shared memory); the
+        G-buffer words are the same."""
+        _check(self.lib, self.ctx, self.lib.hg_set_camera_raster(self.ctx, int(mode)))
+
     def shade(self, params: np.ndarray, lights: np.ndarray, exposure: float = 1.0, ortho: bool = False,
               model: int = abi.SHADE_KARIS) -> None:
         lights = np.ascontiguousarray(lights, dtype=abi.LIGHT)

@@ -258,6 +258,25 @@ hg_status hg_scan(hg_ctx* ctx, hg_groom* groom, const hg_hair_params* params, hg
  * scene_depth: device float[W*H] scene depth (raster.wgsl:93-100) or NULL. */
 hg_status hg_raster(hg_ctx* ctx, hg_groom* groom, const hg_hair_params* params,
                     hg_view_slot slot, const float* scene_depth);
+/* How hg_raster draws the camera G-buffer.  Scheduling only: both give the
+ * same words (every write is a commutative min).
+ *  HG_CAMERA_RASTER_DIRECT (the default): every sample's atomicMin goes to
+ *    global memory, after a read of the current word's high half, in two
+ *    launches (the nearest quarter of the refs, then the rest, whose segments
+ *    hidden behind per-8x8-tile depths are skipped).
+ *  HG_CAMERA_RASTER_BINNED: every segment is listed under the 32x32 screen
+ *    tiles its pixels can touch; a block per tile (and chunk of its list)
+ *    resolves the tile's centre, conservative and beta words in shared memory,
+ *    then issues one global atomicMin per word it lowered.  Segments whose
+ *    pixels span more than 2x2 tiles are drawn with global atomics.  Its
+ *    scratch (about 12.5 KiB per strand of the groom) is allocated on the
+ *    groom's first binned raster.  Slower than the direct pass on the
+ *    1920x1080 benchmark frame (1.08 vs 0.41 ms).
+ * raster.wgsl (the reference) issues every sample's atomicMin directly; the
+ * choice has no counterpart there. */
+#define HG_CAMERA_RASTER_DIRECT 0u
+#define HG_CAMERA_RASTER_BINNED 1u
+hg_status hg_set_camera_raster(hg_ctx* ctx, uint32_t mode);
 /* Strand cache: generates every strand of the groom at the full 65 control
  * points (control_points_for_lod(1.0)) in world space with
  * params->world_from_model -- the strand generation of raster.wgsl:231-317,

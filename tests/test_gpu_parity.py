@@ -575,3 +575,60 @@ def test_dom_pass_over_part_of_the_bundles(renderer):
     assert int(got["dom_indirect"][0]) < sc.mesh.strand_count()
     assert (want["dom_depth"][: sc.dom_size[0] * sc.dom_size[1]] != 0xFFFFFFFF).any()
     _check_visibility(got, want)
+
+
+def _camera_scenes():
+    """Scenes for the two camera raster kinds: a plain one, deep overdraw, the
+    camera inside the groom (segments cut by the near plane span the screen
+    and take the long-segment path), a close-up whose segments cross several
+    32x32 tiles, and forward Z with a scene depth buffer."""
+    def inside():
+        sc = configs.config2(scale=0.01)
+        c = (sc.mesh.bounds_min + sc.mesh.bounds_max) * 0.5
+        wfv = host.looking_at(c + np.array([0, 0, 20.0], np.float32), c + np.array([0, 0, -100.0], np.float32))
+        sc.view = host.View(wfv, sc.view.clip_from_view, sc.view.width, sc.view.height)
+        return sc, None
+
+    def close_up():
+        sc = configs.config1(scale=0.05)
+        sc.view = configs._camera(1024, 768, 160.0)
+        return sc, None
+
+    def dense():
+        sc = configs.config2(scale=0.25)
+        sc.view = configs._camera(384, 216, 900.0)
+        sc.dom_size = (192, 192)
+        return sc, None
+
+    def scene_depth():
+        sc = configs.config1(scale=0.05)
+        v = sc.view
+        sc.view = host.View(v.world_from_view, host.perspective_rh(math.pi / 4, v.width / v.height, 0.1, 5000.0),
+                            v.width, v.height)
+        rng = np.random.default_rng(6)
+        depth = np.where(rng.random(v.width * v.height) < 0.5, np.float32(1.0), np.float32(0.9990))
+        return sc, depth.astype(np.float32)
+
+    return {"config3": lambda: (configs.config3(scale=0.01), None), "inside": inside, "close_up": close_up,
+            "dense": dense, "scene_depth": scene_depth}
+
+
+@pytest.mark.parametrize("mode", [abi.CAMERA_RASTER_BINNED, abi.CAMERA_RASTER_DIRECT])
+@pytest.mark.parametrize("name", list(_camera_scenes()))
+def test_camera_raster_kinds_bit_exact(renderer, name, mode):
+    """hg_set_camera_raster: the binned pass (tiles resolved in shared memory)
+    and the direct pass (global atomics) both give the oracle's G-buffer."""
+    sc, scene_depth = _camera_scenes()[name]()
+    cam, _ = sc.params()
+    renderer.set_camera_raster(mode)
+    try:
+        got = _visibility(renderer, sc, cam, None, scene_depth)
+    finally:
+        renderer.set_camera_raster(abi.CAMERA_RASTER_DIRECT)
+    want = _oracle_visibility(sc, cam, None, scene_depth)
+    assert (want["center"] != EMPTY).sum() > 50
+    _check_visibility(got, want, with_dom=False)
+
+
+def test_set_camera_raster_rejects_unknown_modes(renderer):
+    assert renderer.lib.hg_set_camera_raster(renderer.ctx, 7) == abi.HG_INVALID_ARG
