@@ -178,6 +178,11 @@ hg_status hg_create(int device, void* stream, hg_ctx** out) {
     if (e == cudaSuccess) e = cudaMalloc(&ctx->err, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaMemsetAsync(ctx->err, 0, sizeof(uint32_t), ctx->stream);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->lights, sizeof(hg_light) * HG_MAX_LIGHTS);
+    if (e == cudaSuccess) {
+        ctx->dual_table = new (std::nothrow) hg_dual_table();
+        if (!ctx->dual_table) e = cudaErrorMemoryAllocation;
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->dual_table->table, sizeof(float4) * hg::kDualTableFloat4);
     if (e == cudaSuccess) e = cudaMallocHost(&ctx->lights_host, sizeof(hg_light) * HG_MAX_LIGHTS * hg_ctx::kLightSlots);
     for (int i = 0; i < hg_ctx::kLightSlots && e == cudaSuccess; ++i)
         e = cudaEventCreateWithFlags(&ctx->light_events[i], cudaEventDisableTiming);
@@ -199,6 +204,11 @@ hg_status hg_destroy(hg_ctx* ctx) {
     free_dev(ctx->env_diff);
     free_dev(ctx->err);
     free_dev(ctx->lights);
+    if (ctx->dual_table) {
+        free_dev(ctx->dual_table->table);
+        delete ctx->dual_table;
+        ctx->dual_table = nullptr;
+    }
     if (ctx->lights_host) cudaFreeHost(ctx->lights_host);
     for (int i = 0; i < hg_ctx::kLightSlots; ++i)
         if (ctx->light_events[i]) cudaEventDestroy(ctx->light_events[i]);

@@ -80,6 +80,14 @@ struct hg_mlp {
     uint64_t step = 0;
 };
 
+// Shade model 3's dual-scattering statistics (kDualTableFloat4 float4 on the
+// device) and the material (albedo rgb, roughness, tilt) they were filled for.
+struct hg_dual_table {
+    float4* table = nullptr;
+    float key[5] = {};
+    bool valid = false;
+};
+
 struct hg_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -95,8 +103,9 @@ struct hg_ctx {
     float* filtered_depth = nullptr;
     float4* color = nullptr;
     float* depth = nullptr;
-    uint32_t* hair_list = nullptr;  // pixels with hair (shade model 1), W*H
+    uint32_t* hair_list = nullptr;  // pixels with hair (shade models 1 and 3), W*H
     uint32_t* hair_count = nullptr;
+    hg_dual_table* dual_table = nullptr;  // shade model 3's dual-scattering table (shared by context copies)
     // Camera raster: per 8x8 pixel tile, the largest quantised depth held by
     // any of its G-buffer words (an upper bound once built, since the words
     // only decrease during the pass).
@@ -137,6 +146,10 @@ struct hg_ctx {
 };
 
 namespace hg {
+
+// Dual-scattering table of shade model 3 (shade.cu): 64 uvw.z levels x 129
+// view angles x 6 float4.
+constexpr size_t kDualTableFloat4 = 64u * 129u * 6u;
 
 // One view of a batched item (its camera view, or its deep-opacity view):
 // uniforms, groom buffers and targets.  A device table of these is read in

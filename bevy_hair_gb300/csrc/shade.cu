@@ -4,6 +4,8 @@
 // file compiles with FMA contraction on.
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include <algorithm>
 #include <cmath>
 #include <mutex>
@@ -775,40 +777,120 @@ __global__ void karis_lobes_kernel(const float* __restrict__ in, uint32_t n, flo
 constexpr uint32_t kLightsPerStep = 1;
 
 // Pixels whose centre word is not empty, appended in block order (one
-// atomic per block of kHairListThreads pixels, ordered within the block);
-// the others get the empty shade outputs.
-constexpr int kHairListThreads = 512;
+// atomic per block of kHairListThreads x kHairListPer pixels; each thread
+// loads its kHairListPer centre words before it looks at any); the others
+// get the empty shade outputs.
+constexpr uint32_t kHairListThreads = 256;
+constexpr uint32_t kHairListPer = 8;  // pixels per thread
+
+// The compact surrogate (shade model 3) replaces the per-light lobes; the one
+// per-pixel computation left of the Karis model's prologue is dual_scatter,
+// whose statistics only the deep-opacity-shadowed light's forward spread
+// (spread_term) uses.  Within one shade call they depend on the pixel's
+// 6-bit uvw.z (through roughness and albedo) and its view angle theta_o
+// alone, so shade model 3 reads them from a table filled before the shade
+// kernel: dual_scatter evaluated exactly at 64 uvw.z levels x kDualSteps + 1
+// angles theta_o = k pi / (2 kDualSteps), linear in theta_o between them.
+constexpr int kDualUz = 64;
+constexpr int kDualSteps = 128;
+constexpr int kDualEntries = kDualUz * (kDualSteps + 1);
+constexpr int kDualVec = 6;  // float4 per entry
+static_assert((size_t)kDualEntries * kDualVec == kDualTableFloat4, "hg_ctx::dual_table size");
+
+__global__ void __launch_bounds__(256) dual_table_kernel(const hg_hair_params p, float4* __restrict__ table) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (uint32_t)kDualEntries) return;
+    const uint32_t uz = e / (kDualSteps + 1), k = e % (kDualSteps + 1);
+    const float uvw_z = (float)uz / 63.0f;
+    const float roughness = fmaxf(p.appearance[0] * (0.65f + 0.7f * uvw_z), 0.04f);
+    const float ascale = 0.65f + 0.35f * uvw_z;
+    const f3 albedo = {p.albedo[0] * ascale, p.albedo[1] * ascale, p.albedo[2] * ascale};
+    const Shape shape = lobe_shape(roughness, p.appearance[1]);
+    const f3 sigma_a = absorption_from_color(albedo, roughness);
+    const float theta = (float)k * (0.5f * kPi / (float)kDualSteps);
+    const Dual d = dual_scatter(fmaxf(cosf(theta), 1e-3f), sigma_a, shape);
+    float4* out = table + (size_t)e * kDualVec;
+    out[0] = make_float4(d.fwd.r.x, d.fwd.r.y, d.fwd.r.z, d.a_f.x);
+    out[1] = make_float4(d.fwd.tt.x, d.fwd.tt.y, d.fwd.tt.z, d.a_f.y);
+    out[2] = make_float4(d.fwd.trt.x, d.fwd.trt.y, d.fwd.trt.z, d.a_f.z);
+    out[3] = make_float4(d.beta_f2.x, d.beta_f2.y, d.beta_f2.z, d.sigma_b2.x);
+    out[4] = make_float4(d.a_back.x, d.a_back.y, d.a_back.z, d.sigma_b2.y);
+    out[5] = make_float4(d.delta_b.x, d.delta_b.y, d.delta_b.z, d.sigma_b2.z);
+}
+
+// dual_scatter of a pixel from the table: uvw.z level uz, |sin theta_o| = |t . v|.
+__device__ __forceinline__ Dual dual_from_table(const float4* __restrict__ table, uint32_t uz, float sin_o_abs) {
+    const float pos = asinf(fminf(sin_o_abs, 1.0f)) * ((float)kDualSteps / (0.5f * kPi));
+    const int k0 = min(max((int)pos, 0), kDualSteps - 1);
+    const float f = clampf(pos - (float)k0, 0.0f, 1.0f);
+    const float4* e0 = table + ((size_t)uz * (kDualSteps + 1) + k0) * kDualVec;
+    const float4* e1 = e0 + kDualVec;
+    float4 v[kDualVec];
+#pragma unroll
+    for (int q = 0; q < kDualVec; ++q) {
+        const float4 a = __ldg(e0 + q), b = __ldg(e1 + q);
+        v[q] = make_float4(a.x + f * (b.x - a.x), a.y + f * (b.y - a.y), a.z + f * (b.z - a.z), a.w + f * (b.w - a.w));
+    }
+    Dual d;
+    d.fwd.r = mk3(v[0].x, v[0].y, v[0].z);
+    d.fwd.tt = mk3(v[1].x, v[1].y, v[1].z);
+    d.fwd.trt = mk3(v[2].x, v[2].y, v[2].z);
+    d.a_f = mk3(v[0].w, v[1].w, v[2].w);
+    d.beta_f2 = mk3(v[3].x, v[3].y, v[3].z);
+    d.a_back = mk3(v[4].x, v[4].y, v[4].z);
+    d.delta_b = mk3(v[5].x, v[5].y, v[5].z);
+    d.sigma_b2 = mk3(v[3].w, v[4].w, v[5].w);
+    return d;
+}
 
 __global__ void __launch_bounds__(kHairListThreads) hair_list_kernel(const unsigned long long* __restrict__ center,
                                                                       uint32_t pixels, uint32_t* __restrict__ list,
                                                                       uint32_t* __restrict__ count,
                                                                       float4* __restrict__ shaded,
                                                                       float* __restrict__ shaded_depth) {
-    __shared__ uint32_t warp_base[kHairListThreads / 32 + 1];
-    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
-    bool hair = false;
-    if (pix < pixels) {
-        hair = !is_empty(__ldg(&center[pix]));
-        if (!hair) {
-            shaded[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            shaded_depth[pix] = 0.0f;
-        }
-    }
+    __shared__ uint32_t warp_off[kHairListThreads / 32];
+    __shared__ uint32_t block_base;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t m = __ballot_sync(0xffffffffu, hair);
-    if (lane == 0) warp_base[warp] = (uint32_t)__popc(m);
+    const uint32_t first = blockIdx.x * (kHairListThreads * kHairListPer) + threadIdx.x;
+    // every load in flight before the first use
+    unsigned long long w[kHairListPer];
+#pragma unroll
+    for (uint32_t k = 0; k < kHairListPer; ++k) {
+        const uint32_t px = first + k * kHairListThreads;
+        w[k] = px < pixels ? __ldg(&center[px]) : kEmptyU64;
+    }
+    uint32_t mine = 0, total = 0;
+    uint32_t mask[kHairListPer];
+#pragma unroll
+    for (uint32_t k = 0; k < kHairListPer; ++k) {
+        const uint32_t px = first + k * kHairListThreads;
+        const bool hair = px < pixels && !is_empty(w[k]);
+        if (px < pixels && !hair) {
+            shaded[px] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            shaded_depth[px] = 0.0f;
+        }
+        mask[k] = __ballot_sync(0xffffffffu, hair);
+        mine |= hair ? 1u << k : 0u;
+        total += (uint32_t)__popc(mask[k]);
+    }
+    if (lane == 0) warp_off[warp] = total;
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t sum = 0;
-        for (uint32_t w = 0; w < blockDim.x / 32u; ++w) {
-            const uint32_t c = warp_base[w];
-            warp_base[w] = sum;
+        for (uint32_t v = 0; v < kHairListThreads / 32u; ++v) {
+            const uint32_t c = warp_off[v];
+            warp_off[v] = sum;
             sum += c;
         }
-        warp_base[kHairListThreads / 32] = sum ? atomicAdd(count, sum) : 0u;
+        block_base = sum ? atomicAdd(count, sum) : 0u;
     }
     __syncthreads();
-    if (hair) list[warp_base[kHairListThreads / 32] + warp_base[warp] + __popc(m & ((1u << lane) - 1u))] = pix;
+    uint32_t at = block_base + warp_off[warp];
+#pragma unroll
+    for (uint32_t k = 0; k < kHairListPer; ++k) {
+        if (mine & (1u << k)) list[at + __popc(mask[k] & ((1u << lane) - 1u))] = first + k * kHairListThreads;
+        at += (uint32_t)__popc(mask[k]);
+    }
 }
 
 __global__ void __launch_bounds__(mlp::tc::kThreads, 1)
@@ -1077,15 +1159,18 @@ __device__ __forceinline__ void compact_relu(const float acc[][4][4], uint32_t a
 // m-tiles evaluated together (2) or one after the other (1): one after the
 // other leaves room for three blocks per SM.
 constexpr int kCompactTiles = 1;
+// Resident blocks per SM of the compact shade kernel.
+constexpr int kCompactBlocks = 4;
 
 __device__ __forceinline__ float4 bias_quad(const float* b, int nt, int t) {
     const float lo = b[nt * 8 + 2 * t], hi = b[nt * 8 + 2 * t + 1];
     return make_float4(lo, hi, lo, hi);
 }
 
-__global__ void __launch_bounds__(kCompactWarps * 32, 3)
+__global__ void __launch_bounds__(kCompactWarps * 32, kCompactBlocks)
     shade_compact_kernel(const ShadeArgs a, const __half* __restrict__ w16, const float* __restrict__ mparams,
-                         const EnvArgs env, const uint32_t* __restrict__ list, const uint32_t* __restrict__ count) {
+                         const EnvArgs env, const uint32_t* __restrict__ list, const uint32_t* __restrict__ count,
+                         const float4* __restrict__ dual_table) {
     __shared__ __align__(16) CompactSmem sm;
     {
         const int tid = threadIdx.x, nth = blockDim.x;
@@ -1193,8 +1278,7 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 3)
             const float depth = -logf(fmaxf(dom_visibility(p, a.dom, world, beta), 1e-6f));
             dom_direct = expf(-depth);
             if (depth > 1e-3f) {
-                const float tv = dot3(tangent, view);
-                const Dual ds = dual_scatter(sqrtf(fmaxf(1.0f - tv * tv, 1e-6f)), sigma_a, shape);
+                const Dual ds = dual_from_table(dual_table, (low >> 6u) & 0x3fu, fabsf(dot3(tangent, view)));
                 const Geometry gm = light_geometry(t_n, v_n, mk3(L.dir.x, L.dir.y, L.dir.z));
                 color = vmul(spread_term(shape, ds, gm.theta_h, depth, dom_direct),
                              mk3(L.color.x, L.color.y, L.color.z));
@@ -1280,12 +1364,29 @@ __global__ void __launch_bounds__(kCompactWarps * 32, 3)
     }
 }
 
+// The dual-scattering table of shade model 3 for the material of p (albedo,
+// roughness, tilt), refilled only when that material differs from the one
+// it holds; the refill is ordered on the stream before the shade kernel.
+cudaError_t ensure_dual_table(hg_ctx* ctx, const hg_hair_params& p) {
+    hg_dual_table& d = *ctx->dual_table;
+    const float key[5] = {p.albedo[0], p.albedo[1], p.albedo[2], p.appearance[0], p.appearance[1]};
+    if (d.valid && std::memcmp(d.key, key, sizeof(key)) == 0) return cudaSuccess;
+    d.valid = false;
+    dual_table_kernel<<<(kDualEntries + 255) / 256, 256, 0, ctx->stream>>>(p, d.table);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    std::memcpy(d.key, key, sizeof(key));
+    d.valid = true;
+    return cudaSuccess;
+}
+
 // The hair-pixel list of shade models 1 and 3 (and the empty pixels' outputs).
 cudaError_t launch_hair_list(hg_ctx* ctx) {
     const uint32_t pixels = ctx->width * ctx->height;
     cudaError_t e = cudaMemsetAsync(ctx->hair_count, 0, sizeof(uint32_t), ctx->stream);
     if (e != cudaSuccess) return e;
-    hair_list_kernel<<<(pixels + kHairListThreads - 1) / kHairListThreads, kHairListThreads, 0, ctx->stream>>>(
+    const uint32_t per_block = kHairListThreads * kHairListPer;
+    hair_list_kernel<<<(pixels + per_block - 1) / per_block, kHairListThreads, 0, ctx->stream>>>(
         ctx->center, pixels, ctx->hair_list, ctx->hair_count, ctx->shaded, ctx->shaded_depth);
     return cudaGetLastError();
 }
@@ -1391,10 +1492,11 @@ cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights
     }
     if (model == 3u) {
         const uint32_t pixels = ctx->width * ctx->height;
-        cudaError_t e = launch_hair_list(ctx);
+        cudaError_t e = ensure_dual_table(ctx, p);
         if (e != cudaSuccess) return e;
-        // three resident blocks per SM (the kernel's launch bounds), grid-striding over 32-pixel chunks
-        uint32_t blocks = (uint32_t)ctx->sm_count * 3u;
+        if ((e = launch_hair_list(ctx)) != cudaSuccess) return e;
+        // kCompactBlocks resident blocks per SM (the kernel's launch bounds), grid-striding over 32-pixel chunks
+        uint32_t blocks = (uint32_t)ctx->sm_count * (uint32_t)kCompactBlocks;
         const uint32_t max_chunks = (pixels + 31u) / 32u;
         const uint32_t needed = (max_chunks + kCompactWarps - 1) / kCompactWarps;
         if (blocks > needed) blocks = needed;
@@ -1415,7 +1517,8 @@ cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights
         return cudaLaunchKernelEx(&cfg, shade_compact_kernel, a, reinterpret_cast<const __half*>(ctx->surrogate->w16),
                                   static_cast<const float*>(ctx->surrogate->params), env,
                                   static_cast<const uint32_t*>(ctx->hair_list),
-                                  static_cast<const uint32_t*>(ctx->hair_count));
+                                  static_cast<const uint32_t*>(ctx->hair_count),
+                                  static_cast<const float4*>(ctx->dual_table->table));
     }
     dim3 block(32, 8);
     dim3 grid((ctx->width + 31) / 32, (ctx->height + 7) / 8);
