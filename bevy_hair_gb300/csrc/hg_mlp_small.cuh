@@ -85,19 +85,6 @@ __device__ __forceinline__ void forward(const Weights& w, mlp::WarpIo& io, const
 }
 
 // ---------------------------------------------------------------- training
-// One thread per sample on the CUDA cores, in FP32, with the forward pass's
-// roundings those of the mma.sync network: FP16 inputs, weights and
-// post-ReLU activations, FP32 sums.  The weights arrive FP16-rounded in
-// shared memory as floats.
-struct TrainWeights {
-    float w1[kHid][kIn];
-    float w2[kHid][kHid];
-    float w3[kOut][kHid];
-    float b1[kHid], b2[kHid], b3[kOut];
-};
-
-__device__ __forceinline__ float round_half(float v) { return __half2float(__float2half_rn(v)); }
-
 // Training target of channel c from the twelve transformed FP64 lobes of
 // hg_mlp_samples (log1p(lobe / 1e-3)): log1p(bsdf / 1e-3) with bsdf =
 // R + TT + TRT + kBack * B.

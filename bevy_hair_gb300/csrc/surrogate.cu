@@ -1,11 +1,14 @@
 // Learned shading surrogate: FP64 training samples of the hair lobes, the
 // FP16 tensor-core networks' inference and training kernels (4 x 64: forward
-// + backward per warp, split-K weight gradients, Adam; compact 2 x 32: one
-// sample per thread, block-summed weight gradients, Adam), and their C entry
+// + backward per warp, split-K weight gradients, Adam; compact 2 x 32:
+// forward, backward and weight gradients per warp on mma.sync, block-summed
+// gradients, Adam), and their C entry
 // points.  The reference has no counterpart; the shading it replaces is the
 // Karis fit of shade.wesl:94-190.
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
+
+#include <cstddef>
 
 #include <cmath>
 #include <cstring>
@@ -291,12 +294,22 @@ __global__ void __launch_bounds__(kWarps * 32) infer_small_kernel(const InferArg
     }
 }
 
-// Training of the compact network: one thread per sample (32 per block) runs
-// the forward pass with the inference roundings and the backward pass in
-// FP32; the block then sums its samples' weight gradients (each thread a
-// strided set of parameters, over the block's 32 samples) into `grad`.  The
-// targets are the twelve transformed lobes of hg_mlp_samples; the kernel
-// forms the three BSDF targets from them (mlps::bsdf_target).
+// Training of the compact network on the tensor cores (mma.sync m16n8k16,
+// FP16 operands, FP32 accumulation).  A warp takes 32 samples at a time:
+//  forward   the inference network itself (mlps::forward's layers), keeping
+//            the FP16 activations and the ReLU masks;
+//  backward  dY = 2 (y - target) for the three BSDF channels, then
+//            dZ2 = (dY W3) . [Z2 > 0] and dZ1 = (dZ2 W2) . [Z1 > 0], each a
+//            product with a transposed weight matrix held in shared memory;
+//  gradients dW = dZ^T A over the warp's samples, with the activations and
+//            deltas transposed to [unit][sample] in shared memory so the
+//            sample dimension is the MMAs' K; bias gradients are the row sums
+//            of the transposed deltas.
+// The deltas enter the MMAs rounded to FP16 (the usual mixed-precision
+// backward); the block sums its warps' gradients in shared memory and adds
+// them to `grad` once.  The loss is the sum over samples and the three
+// channels of (y - target)^2; the targets are formed from the twelve lobes
+// of hg_mlp_samples (mlps::bsdf_target).
 struct SmallTrainArgs {
     const float* inputs;   // [n][10] raw
     const float* targets;  // [n][12] transformed lobes
@@ -307,112 +320,233 @@ struct SmallTrainArgs {
     float* loss;  // += sum of squared errors
 };
 
-constexpr int kSmallTrainThreads = 32;
+constexpr int kSmallTrainWarps = 4;
+constexpr int kSampPad = 40;  // halves per transposed row: 32 samples + 8 (conflict-free ldmatrix)
 
-__global__ void __launch_bounds__(kSmallTrainThreads) small_train_kernel(const SmallTrainArgs a) {
-    __shared__ mlps::TrainWeights w;
-    __shared__ float s_x[kSmallTrainThreads][mlps::kIn], s_a1[kSmallTrainThreads][mlps::kHid], s_a2[kSmallTrainThreads][mlps::kHid];
-    __shared__ float s_d1[kSmallTrainThreads][mlps::kHid], s_d2[kSmallTrainThreads][mlps::kHid], s_dy[kSmallTrainThreads][mlps::kOut];
-    const int tid = threadIdx.x;
-    for (int i = tid; i < mlps::kHid * mlps::kIn; i += kSmallTrainThreads) (&w.w1[0][0])[i] = __half2float(a.w16[mlps::kW1 + i]);
-    for (int i = tid; i < mlps::kHid * mlps::kHid; i += kSmallTrainThreads) (&w.w2[0][0])[i] = __half2float(a.w16[mlps::kW2 + i]);
-    for (int i = tid; i < mlps::kOut * mlps::kHid; i += kSmallTrainThreads) (&w.w3[0][0])[i] = __half2float(a.w16[mlps::kW3 + i]);
-    for (int i = tid; i < mlps::kHid; i += kSmallTrainThreads) {
-        w.b1[i] = a.params[mlps::kB1 + i];
-        w.b2[i] = a.params[mlps::kB2 + i];
-        if (i < mlps::kOut) w.b3[i] = a.params[mlps::kB3 + i];
+// Per-warp transposes: [unit][sample].
+struct SmallStage {
+    __half x[mlps::kIn][kSampPad];
+    __half a1[mlps::kHid][kSampPad];
+    __half a2[mlps::kHid][kSampPad];
+    __half dy[mlps::kOut][kSampPad];
+    __half dz2[mlps::kHid][kSampPad];
+    __half dz1[mlps::kHid][kSampPad];
+};
+
+// Every array that ldmatrix reads starts on a 16-byte boundary (its rows are
+// multiples of 16 bytes), which the static_asserts below check.
+struct SmallTrainSmem {
+    alignas(16) mlps::Weights w;                        // forward weights (padded rows) and biases
+    alignas(16) __half w3t[mlps::kHid][mlps::kPadIn];  // W3^T: [hidden][output]
+    alignas(16) __half w2t[mlps::kHid][mlps::kPadHid]; // W2^T: [hidden 1][hidden 2]
+    float zero[mlps::kHid];
+    float grad[mlps::kParams];
+    float loss;
+    alignas(16) mlp::WarpIo io[kSmallTrainWarps];
+    alignas(16) SmallStage st[kSmallTrainWarps];
+};
+static_assert(offsetof(SmallTrainSmem, w) % 16 == 0 && offsetof(SmallTrainSmem, w3t) % 16 == 0 &&
+                  offsetof(SmallTrainSmem, w2t) % 16 == 0 && offsetof(SmallTrainSmem, st) % 16 == 0 &&
+                  offsetof(SmallTrainSmem, io) % 16 == 0,
+              "ldmatrix operands on 16-byte boundaries");
+static_assert(offsetof(mlps::Weights, w2) % 16 == 0 && offsetof(mlps::Weights, w3) % 16 == 0, "weight rows");
+static_assert(sizeof(SmallStage) % 16 == 0 && offsetof(SmallStage, a1) % 16 == 0 && offsetof(SmallStage, a2) % 16 == 0 &&
+                  offsetof(SmallStage, dy) % 16 == 0 && offsetof(SmallStage, dz2) % 16 == 0 &&
+                  offsetof(SmallStage, dz1) % 16 == 0 && (kSampPad * 2) % 16 == 0,
+              "transposed rows on 16-byte boundaries");
+static_assert((mlps::kPadIn * 2) % 16 == 0 && (mlps::kPadHid * 2) % 16 == 0, "padded weight rows");
+constexpr size_t kSmallTrainSmem = sizeof(SmallTrainSmem);
+
+// A packed FP16 pair of A fragment a[mt][kt][r] (rows = samples) into the
+// transpose dst[unit][sample].
+template <int KT>
+__device__ __forceinline__ void stage_frags(__half (*dst)[kSampPad], const uint32_t a[2][KT][4], int g, int t) {
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int kt = 0; kt < KT; ++kt)
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int unit = kt * 16 + 2 * t + ((r >> 1) ? 8 : 0);
+                const int sample = mt * 16 + g + ((r & 1) ? 8 : 0);
+                const __half2 v = *reinterpret_cast<const __half2*>(&a[mt][kt][r]);
+                dst[unit][sample] = __low2half(v);
+                dst[unit + 1][sample] = __high2half(v);
+            }
+}
+
+// C fragments of a 32-wide layer times a 32-bit mask (bit (mt*4 + nt)*4 + e)
+// -> FP16 A fragments.
+__device__ __forceinline__ void masked_to_a(const float acc[2][4][4], uint32_t mask, uint32_t a[2][2][4]) {
+    auto m = [&](int mt, int nt, int e) { return (mask >> ((mt * 4 + nt) * 4 + e)) & 1u ? acc[mt][nt][e] : 0.0f; };
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int kt = 0; kt < 2; ++kt) {
+            a[mt][kt][0] = mlp::pack_h2(m(mt, 2 * kt, 0), m(mt, 2 * kt, 1));
+            a[mt][kt][1] = mlp::pack_h2(m(mt, 2 * kt, 2), m(mt, 2 * kt, 3));
+            a[mt][kt][2] = mlp::pack_h2(m(mt, 2 * kt + 1, 0), m(mt, 2 * kt + 1, 1));
+            a[mt][kt][3] = mlp::pack_h2(m(mt, 2 * kt + 1, 2), m(mt, 2 * kt + 1, 3));
+        }
+}
+
+__device__ __forceinline__ uint32_t positive_mask(const float acc[2][4][4]) {
+    uint32_t m = 0;
+#pragma unroll
+    for (int mt = 0; mt < 2; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < 4; ++nt)
+#pragma unroll
+            for (int e = 0; e < 4; ++e) m |= (acc[mt][nt][e] > 0.0f ? 1u : 0u) << ((mt * 4 + nt) * 4 + e);
+    return m;
+}
+
+// dW[m][n] += sum over the 32 samples of A[m][s] B[n][s] for MT 16-row tiles
+// of A (rows m0..) and NT 8-row tiles of B, both [unit][sample], added to the
+// shared gradient at grad[(m) * ld + n].
+template <int MT, int NT>
+__device__ __forceinline__ void wgrad(const __half (*A)[kSampPad], const __half (*B)[kSampPad], float* grad, int ld,
+                                      int lane) {
+    const int g = lane >> 2, t = lane & 3, mat = lane >> 3, r = lane & 7;
+    float acc[MT][NT][4];
+#pragma unroll
+    for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) acc[mt][nt][0] = acc[mt][nt][1] = acc[mt][nt][2] = acc[mt][nt][3] = 0.0f;
+#pragma unroll
+    for (int kt = 0; kt < 2; ++kt) {
+        uint32_t af[MT][4];
+#pragma unroll
+        for (int mt = 0; mt < MT; ++mt)
+            mlp::ldsm_x4(af[mt], &A[mt * 16 + (lane & 7) + ((lane >> 3) & 1) * 8][kt * 16 + (lane >> 4) * 8]);
+#pragma unroll
+        for (int nt = 0; nt < NT; nt += 2) {
+            uint32_t b[4];
+            mlp::ldsm_x4(b, &B[(nt + (mat >> 1)) * 8 + r][kt * 16 + (mat & 1) * 8]);
+#pragma unroll
+            for (int mt = 0; mt < MT; ++mt) {
+                mlp::mma(acc[mt][nt], af[mt], b[0], b[1]);
+                mlp::mma(acc[mt][nt + 1], af[mt], b[2], b[3]);
+            }
+        }
     }
+#pragma unroll
+    for (int mt = 0; mt < MT; ++mt)
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt) {
+            const int row = mt * 16 + g, col = nt * 8 + 2 * t;
+            atomicAdd(&grad[row * ld + col], acc[mt][nt][0]);
+            atomicAdd(&grad[row * ld + col + 1], acc[mt][nt][1]);
+            atomicAdd(&grad[(row + 8) * ld + col], acc[mt][nt][2]);
+            atomicAdd(&grad[(row + 8) * ld + col + 1], acc[mt][nt][3]);
+        }
+}
+
+__global__ void __launch_bounds__(kSmallTrainWarps * 32) small_train_kernel(const SmallTrainArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_small[];
+    SmallTrainSmem& S = *reinterpret_cast<SmallTrainSmem*>(smem_small);
+    const int tid = threadIdx.x, nth = blockDim.x;
+    mlps::load(S.w, a.w16, a.params, tid, nth);
+    for (int i = tid; i < mlps::kHid * mlps::kOut; i += nth) {
+        const int j = i / mlps::kOut, o = i % mlps::kOut;  // W3^T[j][o] = W3[o][j]
+        S.w3t[j][o] = a.w16[mlps::kW3 + o * mlps::kHid + j];
+    }
+    for (int i = tid; i < mlps::kHid * mlps::kHid; i += nth) {
+        const int j1 = i / mlps::kHid, j2 = i % mlps::kHid;  // W2^T[j1][j2] = W2[j2][j1]
+        S.w2t[j1][j2] = a.w16[mlps::kW2 + j2 * mlps::kHid + j1];
+    }
+    for (int i = tid; i < mlps::kHid; i += nth) S.zero[i] = 0.0f;
+    for (int i = tid; i < mlps::kParams; i += nth) S.grad[i] = 0.0f;
+    if (tid == 0) S.loss = 0.0f;
     __syncthreads();
-    const uint32_t k = blockIdx.x * kSmallTrainThreads + tid;
-    const bool valid = k < a.n;
-    float raw[10], xn[10];
-    load_raw(a.inputs, k, valid, raw);
-    normalise(raw, xn);
-    float x[mlps::kIn];
-#pragma unroll
-    for (int i = 0; i < mlps::kIn; ++i) x[i] = i < mlp::kUsedIn ? mlps::round_half(xn[i]) : 0.0f;
-    float a1[mlps::kHid], a2[mlps::kHid];
-#pragma unroll
-    for (int j = 0; j < mlps::kHid; ++j) {
-        float z = w.b1[j];
-#pragma unroll
-        for (int i = 0; i < mlps::kIn; ++i) z += w.w1[j][i] * x[i];
-        a1[j] = mlps::round_half(fmaxf(z, 0.0f));
-    }
-#pragma unroll
-    for (int j = 0; j < mlps::kHid; ++j) {
-        float z = w.b2[j];
-#pragma unroll
-        for (int i = 0; i < mlps::kHid; ++i) z += w.w2[j][i] * a1[i];
-        a2[j] = mlps::round_half(fmaxf(z, 0.0f));
-    }
-    float t12[12];
-#pragma unroll
-    for (int o = 0; o < 12; ++o) t12[o] = valid ? __ldg(&a.targets[(size_t)k * 12 + o]) : 0.0f;
-    float dy[mlps::kOut];
+    const int warp = tid >> 5, lane = tid & 31, g = lane >> 2, t = lane & 3;
+    mlp::WarpIo& io = S.io[warp];
+    SmallStage& st = S.st[warp];
     float loss = 0.0f;
+    bool any = false;
+    for (uint32_t base = (blockIdx.x * kSmallTrainWarps + warp) * 32u; base < a.n;
+         base += gridDim.x * kSmallTrainWarps * 32u) {
+        any = true;
+        const uint32_t k = base + lane;
+        const bool valid = k < a.n;
+        float raw[10], xn[10];
+        load_raw(a.inputs, k, valid, raw);
+        normalise(raw, xn);
+        // forward (the inference roundings: FP16 inputs, weights and activations)
+        uint32_t a0[2][1][4];
+        mlp::input_frags(io, xn, a0, lane, g, t);
+        float acc[2][4][4];
+        uint32_t a1[2][2][4], a2[2][2][4];
+        mlp::layer_ldsm<4, 1, mlps::kPadIn>(acc, a0, S.w.w1, S.w.b1, lane);
+        const uint32_t mask1 = positive_mask(acc);
+        mlps::relu_to_a(acc, a1);
+        mlp::layer_ldsm<4, 2, mlps::kPadHid>(acc, a1, S.w.w2, S.w.b2, lane);
+        const uint32_t mask2 = positive_mask(acc);
+        mlps::relu_to_a(acc, a2);
+        float out[2][2][4];
+        mlp::layer_ldsm<2, 2, mlps::kPadHid>(out, a2, S.w.w3, S.w.b3, lane);
+        float y[mlp::kUsedOut];  // output_rows fills 12 columns; the first mlps::kUsedOut are outputs
+        mlp::output_rows(io, out, y, lane, g, t);
+        // dY of this lane's sample, as the next product's A operand
+        float dy[mlps::kUsedOut];
 #pragma unroll
-    for (int o = 0; o < mlps::kOut; ++o) {
-        float y = w.b3[o];
+        for (int o = 0; o < mlps::kUsedOut; ++o) {
+            float d = 0.0f;
+            if (valid) {
+                float t12[12];
 #pragma unroll
-        for (int j = 0; j < mlps::kHid; ++j) y += w.w3[o][j] * a2[j];
-        const float d = valid && o < mlps::kUsedOut ? y - mlps::bsdf_target(t12, o) : 0.0f;
-        loss += d * d;
-        dy[o] = 2.0f * d;
+                for (int c = 0; c < 12; ++c) t12[c] = __ldg(&a.targets[(size_t)k * 12 + c]);
+                d = y[o] - mlps::bsdf_target(t12, o);
+            }
+            loss += d * d;
+            dy[o] = 2.0f * d;
+        }
+        float dyx[mlp::kUsedIn];
+#pragma unroll
+        for (int c = 0; c < mlp::kUsedIn; ++c) dyx[c] = c < mlps::kUsedOut ? dy[c] : 0.0f;
+        uint32_t ady[2][1][4];
+        mlp::input_frags(io, dyx, ady, lane, g, t);
+        // backward through the layers
+        mlp::layer_ldsm<4, 1, mlps::kPadIn>(acc, ady, S.w3t, S.zero, lane);  // dY W3
+        uint32_t dz2[2][2][4], dz1[2][2][4];
+        masked_to_a(acc, mask2, dz2);
+        mlp::layer_ldsm<4, 2, mlps::kPadHid>(acc, dz2, S.w2t, S.zero, lane);  // dZ2 W2
+        masked_to_a(acc, mask1, dz1);
+        // transposes [unit][sample]
+        stage_frags<1>(st.x, a0, g, t);
+        stage_frags<2>(st.a1, a1, g, t);
+        stage_frags<2>(st.a2, a2, g, t);
+        stage_frags<1>(st.dy, ady, g, t);
+        stage_frags<2>(st.dz2, dz2, g, t);
+        stage_frags<2>(st.dz1, dz1, g, t);
+        __syncwarp();
+        // weight gradients over the warp's samples, then bias gradients
+        wgrad<1, 4>(st.dy, st.a2, S.grad + mlps::kW3, mlps::kHid, lane);
+        wgrad<2, 4>(st.dz2, st.a1, S.grad + mlps::kW2, mlps::kHid, lane);
+        wgrad<2, 2>(st.dz1, st.x, S.grad + mlps::kW1, mlps::kIn, lane);
+        {
+            float s1 = 0.0f, s2 = 0.0f, s3 = 0.0f;
+#pragma unroll 8
+            for (int q = 0; q < 32; ++q) {
+                s1 += __half2float(st.dz1[lane][q]);
+                s2 += __half2float(st.dz2[lane][q]);
+                if (lane < mlps::kOut) s3 += __half2float(st.dy[lane][q]);
+            }
+            atomicAdd(&S.grad[mlps::kB1 + lane], s1);
+            atomicAdd(&S.grad[mlps::kB2 + lane], s2);
+            if (lane < mlps::kOut) atomicAdd(&S.grad[mlps::kB3 + lane], s3);
+        }
+        __syncwarp();
     }
-    float d2[mlps::kHid], d1[mlps::kHid];
-#pragma unroll
-    for (int j = 0; j < mlps::kHid; ++j) {
-        float s = 0.0f;
-#pragma unroll
-        for (int o = 0; o < mlps::kOut; ++o) s += w.w3[o][j] * dy[o];
-        d2[j] = a2[j] > 0.0f ? s : 0.0f;
-    }
-#pragma unroll
-    for (int i = 0; i < mlps::kHid; ++i) {
-        float s = 0.0f;
-#pragma unroll
-        for (int j = 0; j < mlps::kHid; ++j) s += w.w2[j][i] * d2[j];
-        d1[i] = a1[i] > 0.0f ? s : 0.0f;
-    }
-#pragma unroll
-    for (int i = 0; i < mlps::kIn; ++i) s_x[tid][i] = x[i];
-#pragma unroll
-    for (int j = 0; j < mlps::kHid; ++j) {
-        s_a1[tid][j] = a1[j];
-        s_a2[tid][j] = a2[j];
-        s_d1[tid][j] = d1[j];
-        s_d2[tid][j] = d2[j];
-    }
-#pragma unroll
-    for (int o = 0; o < mlps::kOut; ++o) s_dy[tid][o] = dy[o];
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, off);
-    if (tid == 0) atomicAdd(a.loss, loss);
+    if (lane == 0 && any) atomicAdd(&S.loss, loss);
     __syncthreads();
-    for (int p = tid; p < mlps::kParams; p += kSmallTrainThreads) {
-        float g = 0.0f;
-        if (p < mlps::kB1) {
-            const int r = p / mlps::kIn, c = p - r * mlps::kIn;
-            for (int s = 0; s < kSmallTrainThreads; ++s) g += s_d1[s][r] * s_x[s][c];
-        } else if (p < mlps::kW2) {
-            const int r = p - mlps::kB1;
-            for (int s = 0; s < kSmallTrainThreads; ++s) g += s_d1[s][r];
-        } else if (p < mlps::kB2) {
-            const int r = (p - mlps::kW2) / mlps::kHid, c = (p - mlps::kW2) - r * mlps::kHid;
-            for (int s = 0; s < kSmallTrainThreads; ++s) g += s_d2[s][r] * s_a1[s][c];
-        } else if (p < mlps::kW3) {
-            const int r = p - mlps::kB2;
-            for (int s = 0; s < kSmallTrainThreads; ++s) g += s_d2[s][r];
-        } else if (p < mlps::kB3) {
-            const int r = (p - mlps::kW3) / mlps::kHid, c = (p - mlps::kW3) - r * mlps::kHid;
-            for (int s = 0; s < kSmallTrainThreads; ++s) g += s_dy[s][r] * s_a2[s][c];
-        } else {
-            const int r = p - mlps::kB3;
-            for (int s = 0; s < kSmallTrainThreads; ++s) g += s_dy[s][r];
-        }
-        if (g != 0.0f) atomicAdd(&a.grad[p], g);
+    for (int i = tid; i < mlps::kParams; i += nth) {
+        const float gv = S.grad[i];
+        if (gv != 0.0f) atomicAdd(&a.grad[i], gv);
     }
+    if (tid == 0 && S.loss != 0.0f) atomicAdd(a.loss, S.loss);
 }
 
 // The same evaluation on tcgen05: four chains of two 128-row evaluations per CTA.
@@ -816,6 +950,9 @@ cudaError_t ensure_device_setup(int device) {
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(infer_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)tc::kSmemBytes);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(small_train_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kSmallTrainSmem);
         if (e != cudaSuccess) return e;
         g_attr_ready[device] = true;
     }
@@ -886,8 +1023,11 @@ cudaError_t run_gradients(hg_mlp* m, const float* inputs, const float* targets, 
         s.params = m->params;
         s.grad = m->grad;
         s.loss = m->loss;
-        small_train_kernel<<<(n + kSmallTrainThreads - 1) / kSmallTrainThreads, kSmallTrainThreads, 0,
-                             m->ctx->stream>>>(s);
+        // persistent warps: each takes several 32-sample tiles, each block adds its sums once
+        const uint32_t tiles = (n + 31u) / 32u;
+        const uint32_t want = (tiles + kSmallTrainWarps - 1) / kSmallTrainWarps;
+        const uint32_t blocks = std::max(1u, std::min(want, (uint32_t)m->ctx->sm_count * 4u));
+        small_train_kernel<<<blocks, kSmallTrainWarps * 32, kSmallTrainSmem, m->ctx->stream>>>(s);
         return cudaGetLastError();
     }
     const uint32_t ld = m->ld_capacity;
