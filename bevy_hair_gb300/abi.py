@@ -71,7 +71,7 @@ CAMERA_RASTER_DIRECT, CAMERA_RASTER_BINNED = 0, 1
 BUF_CENTER, BUF_CONSERVATIVE, BUF_BETA, BUF_DOM = 0, 1, 2, 3
 BUF_SHADED, BUF_SHADED_DEPTH, BUF_FILTERED, BUF_FILTERED_DEPTH = 4, 5, 6, 7
 BUF_COLOR, BUF_DEPTH = 8, 9
-GBUF_LOD, GBUF_REFS, GBUF_INDIRECT = 0, 1, 2
+GBUF_LOD, GBUF_REFS, GBUF_INDIRECT, GBUF_STRAND_CACHE = 0, 1, 2, 3
 
 STATUS = {
     0: "ok", 1: "invalid argument", 2: "out of device memory", 3: "CUDA error",

@@ -515,6 +515,10 @@ hg_status hg_groom_buffer(hg_ctx* ctx, hg_groom* g, hg_view_slot slot, hg_groom_
         case HG_GBUF_LOD: p = g->lod[slot]; n = (size_t)std::max<uint32_t>(g->bundle_count, 1u) * 16; break;
         case HG_GBUF_REFS: p = g->refs[slot]; n = (size_t)g->ref_capacity * 16; break;
         case HG_GBUF_INDIRECT: p = g->indirect[slot]; n = 16; break;
+        case HG_GBUF_STRAND_CACHE:
+            p = g->cache;
+            n = g->cache ? (size_t)g->strand_total * 2u * hg::kStrandCacheCps * sizeof(float4) : 0;
+            break;
         default: return fail(ctx, HG_INVALID_ARG, "unknown groom buffer id");
     }
     if (device_ptr) *device_ptr = p;

@@ -84,12 +84,15 @@ class GpuGroom:
         return p.value or 0, n.value
 
     def read(self, slot: int, which: int) -> np.ndarray:
-        """Copy the slot's LodRecords, StrandRefs or indirect words to the host."""
+        """Copy the slot's LodRecords, StrandRefs or indirect words (or the
+        strand cache, as float32 [strands, 130, 4]) to the host."""
         _, nbytes = self.buffer(slot, which)
         host = np.empty(nbytes, dtype=np.uint8)
         lib = self.renderer.lib
         _check(lib, self.renderer.ctx, lib.hg_groom_copy_out(self.renderer.ctx, self.handle, slot, which,
                                                              abi.ptr(host), nbytes))
+        if which == abi.GBUF_STRAND_CACHE:
+            return host.view(np.float32).reshape(-1, 130, 4)
         dt = {abi.GBUF_LOD: abi.LOD_RECORD, abi.GBUF_REFS: abi.STRAND_REF, abi.GBUF_INDIRECT: np.uint32}[which]
         return host.view(dt)
 

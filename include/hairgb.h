@@ -174,7 +174,10 @@ typedef enum hg_buffer_id {
 typedef enum hg_groom_buffer_id {
     HG_GBUF_LOD = 0,        /* hg_lod_record[bundle_count] of the slot */
     HG_GBUF_REFS = 1,       /* hg_strand_ref[max(strands,1)] of the slot */
-    HG_GBUF_INDIRECT = 2    /* u32[4]: (total refs, 1, 1, 0) of the slot */
+    HG_GBUF_INDIRECT = 2,   /* u32[4]: (total refs, 1, 1, 0) of the slot */
+    HG_GBUF_STRAND_CACHE = 3 /* float4[strands * 130] from hg_generate (slot ignored): per strand, in
+                                upload order, 65 (world position, ao) then 65 (world tangent, w);
+                                a null pointer and size 0 before the first hg_generate */
 } hg_groom_buffer_id;
 
 typedef struct hg_ctx hg_ctx;
