@@ -253,6 +253,7 @@ _SIGNATURES = {
 
 _BAKE_SIGNATURES = {
     "hg_bake": (_VP, [_VP, _U32, _VP, _VP, _U32, _U32]),
+    "hg_bake_scalp": (_VP, [_VP, _U32, _VP, _VP, _U32, _VP, _U32, _VP, _U32, _U32]),
     "hg_bake_bundle_count": (_U32, [_VP]),
     "hg_bake_layer_count": (_U32, [_VP]),
     "hg_bake_style_count": (_U32, [_VP]),

@@ -128,6 +128,26 @@ def config3(scale: float = 1.0) -> Scene:
                  [host.Directional(np.asarray(KEY_DIR, dtype=F), True)])
 
 
+def real_groom(hair_path, scalp_path=None, width: int = 1920, height: int = 1080, dom: int = 1024) -> Scene:
+    """A groom from a HAIR file (e.g. the Cem Yuksel grooms the reference ships
+    in assets/hair, 50,000 strands each), baked against its scalp mesh when an
+    OBJ is given, framed by a camera on the mesh's bounds, with config 2's
+    material and lights."""
+    from pathlib import Path
+
+    strands = groom.parse_hair(Path(hair_path).read_bytes())
+    scalp = groom.parse_obj(Path(scalp_path).read_text()) if scalp_path else None
+    mesh = groom.bake(strands, ambient_occlusion=True, scalp=scalp)
+    centre = 0.5 * (mesh.bounds_min + mesh.bounds_max)
+    radius = float(np.linalg.norm(mesh.bounds_max - mesh.bounds_min)) * 0.5
+    g = host.HairGroom(lam=3.0, albedo=(0.16, 0.07, 0.035), roughness=0.3, tilt=0.08, lod=True, filter=True,
+                       ambient_occlusion=True, deep_opacity=True, center_diameter=1.0)
+    key = Light(kind=abi.LIGHT_DIRECTIONAL, color=(3.0, 2.9, 2.7), direction=KEY_DIR, casts_shadows=True)
+    lights = [key] + _ring_lights(8, 4.0 * radius, 0.3 * radius, 6.0e4 * (radius / 500.0) ** 2, SEED_BASE + 6)
+    return Scene(Path(hair_path).stem, mesh, g, _camera(width, height, 2.6 * radius, target=tuple(centre.tolist())),
+                 (dom, dom), lights, [host.Directional(np.asarray(KEY_DIR, dtype=F), True)])
+
+
 @dataclass
 class BatchScene:
     name: str

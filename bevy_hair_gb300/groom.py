@@ -49,17 +49,66 @@ class Strands:
         return int(len(self.first))
 
 
-def bake(strands: Strands, ambient_occlusion: bool = True) -> HairMesh:
-    """Bake explicit strands into bundle cages with the native baker
-    (restating bake_hair_mesh, src/bake.rs:89-213)."""
+@dataclass
+class Scalp:
+    """Triangle mesh the strands grow from: vertices float32 [n, 3], triangles uint32 [m, 3]."""
+    vertices: np.ndarray
+    triangles: np.ndarray
+
+
+def parse_obj(text: str) -> Scalp:
+    """Positions and faces of a Wavefront OBJ file (``v`` and ``f`` records;
+    face corners ``i``, ``i/t`` or ``i/t/n`` with 1-based or negative indices;
+    polygons split into triangle fans), the head mesh the reference's example
+    bakes against (src/obj.rs:12-44)."""
+    verts: list[tuple[float, float, float]] = []
+    tris: list[tuple[int, int, int]] = []
+    for raw in text.splitlines():
+        line = raw.strip()
+        if line.startswith("v "):
+            parts = line[2:].split()
+            xyz = []
+            for k in range(3):
+                try:
+                    xyz.append(float(parts[k]))
+                except (IndexError, ValueError):
+                    xyz.append(0.0)
+            verts.append((xyz[0], xyz[1], xyz[2]))
+        elif line.startswith("f "):
+            corners = []
+            for c in line[2:].split():
+                try:
+                    i = int(c.split("/")[0])
+                except ValueError:
+                    continue
+                if i > 0:
+                    corners.append(i - 1)
+                elif i < 0:
+                    corners.append(len(verts) + i)
+            for k in range(1, len(corners) - 1):
+                tris.append((corners[0], corners[k], corners[k + 1]))
+    return Scalp(np.asarray(verts, dtype=F).reshape(-1, 3), np.asarray(tris, dtype=np.uint32).reshape(-1, 3))
+
+
+def bake(strands: Strands, ambient_occlusion: bool = True, scalp: Scalp | None = None) -> HairMesh:
+    """Bake explicit strands (and optionally the scalp mesh they grow from)
+    into bundle cages with the native baker (the interface of
+    bake_hair_mesh_with_scalp, src/bake.rs:89-213; include/hairgb_bake.h)."""
     lib = abi.load_bake()
     pts = np.ascontiguousarray(strands.points, dtype=F)
     first = np.ascontiguousarray(strands.first, dtype=np.uint32)
     count = np.ascontiguousarray(strands.count, dtype=np.uint32)
     flags = 1 if ambient_occlusion else 0
-    r = lib.hg_bake(pts.ctypes.data, len(pts), first.ctypes.data, count.ctypes.data, len(first), flags)
+    if scalp is not None and len(scalp.triangles):
+        sv = np.ascontiguousarray(scalp.vertices, dtype=F)
+        si = np.ascontiguousarray(scalp.triangles, dtype=np.uint32)
+        r = lib.hg_bake_scalp(pts.ctypes.data, len(pts), first.ctypes.data, count.ctypes.data, len(first),
+                              sv.ctypes.data, len(sv), si.ctypes.data, si.size, flags)
+    else:
+        r = lib.hg_bake(pts.ctypes.data, len(pts), first.ctypes.data, count.ctypes.data, len(first), flags)
     if not r:
-        raise ValueError("hg_bake rejected the strands (a strand lies outside the point array)")
+        raise ValueError("the baker rejected the input (a strand outside the point array or a scalp index "
+                         "outside the vertex array)")
     try:
         nb, nl, ns = lib.hg_bake_bundle_count(r), lib.hg_bake_layer_count(r), lib.hg_bake_style_count(r)
         bundles = np.zeros(nb, dtype=abi.GPU_BUNDLE)

@@ -7,6 +7,8 @@ SHADE_RTOL / SHADE_ATOL; the filter's coverage alpha is exact and its colour
 within FILTER_RTOL.
 """
 import math
+import os
+from pathlib import Path
 
 import numpy as np
 import pytest
@@ -632,3 +634,34 @@ def test_camera_raster_kinds_bit_exact(renderer, name, mode):
 
 def test_set_camera_raster_rejects_unknown_modes(renderer):
     assert renderer.lib.hg_set_camera_raster(renderer.ctx, 7) == abi.HG_INVALID_ARG
+
+
+_REF = os.environ.get("BEVY_HAIR_REFERENCE")
+
+
+@pytest.mark.skipif(not _REF or not (Path(_REF) / "assets" / "hair" / "woman.obj").exists(),
+                    reason="the reference's grooms are not present (set BEVY_HAIR_REFERENCE)")
+@pytest.mark.parametrize("name", ["wStraight", "wCurly"])
+def test_reference_groom_frame_against_the_oracle(renderer, name):
+    """A real groom (the reference's Yuksel asset, 50,000 strands, baked
+    against woman.obj) through hg_groom_frame at 960x540: LOD records, G-buffer
+    words and the deep opacity map bit-exact with the oracle's frame, colour
+    within the shading tolerance."""
+    hair = Path(_REF) / "assets" / "hair"
+    if not (hair / f"{name}.hair").exists():
+        pytest.skip(f"{name}.hair is not present")
+    sc = configs.real_groom(hair / f"{name}.hair", hair / "woman.obj", 960, 540, 512)
+    cam, dom = sc.params()
+    lights = sc.light_array()
+    renderer.ensure_targets(sc.view.width, sc.view.height, *sc.dom_size)
+    g = renderer.upload(sc.mesh)
+    renderer.render_groom(g, cam, dom, lights)
+    assert renderer.synchronize() == 0
+    want = oracle.frame(sc.mesh, cam, dom, lights)
+    _assert_equal("center", renderer.read(abi.BUF_CENTER), want["center"])
+    _assert_equal("conservative", renderer.read(abi.BUF_CONSERVATIVE), want["cons"])
+    _assert_equal("beta", renderer.read(abi.BUF_BETA), want["beta"])
+    _assert_equal("dom", renderer.read(abi.BUF_DOM), want["dom"])
+    assert (want["center"] != EMPTY).sum() > 20_000
+    np.testing.assert_allclose(renderer.read(abi.BUF_SHADED), want["shaded"], rtol=2e-3, atol=1e-5)
+    g.close()
