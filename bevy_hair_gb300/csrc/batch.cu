@@ -37,6 +37,8 @@ struct hg_batch {
     // another on the context's stream: sized for the largest item.
     uint32_t* tile_depth = nullptr;
     uint32_t* hair_list = nullptr;
+    // 8x8 tile depths of every camera view (the batched two-stage raster)
+    uint32_t* tdepth = nullptr;
     uint32_t* hair_count = nullptr;
     uint64_t total_px = 0, total_dom = 0;
     // tables: pinned host copies and their device twins
@@ -100,7 +102,7 @@ uint64_t round_up64(uint64_t v) { return (v + 63u) & ~uint64_t(63u); }
 // prefix (n + 1), tile prefix (n + 1), filter-tile prefix (n + 1), DOM word
 // prefix (n + 1).
 struct TabOffsets {
-    size_t bundle, strand, tile, ftile, dom, total;
+    size_t bundle, strand, tile, ftile, dom, tdepth, total;
 };
 
 TabOffsets tab_offsets(uint32_t n, uint32_t n_views) {
@@ -110,9 +112,13 @@ TabOffsets tab_offsets(uint32_t n, uint32_t n_views) {
     t.tile = t.strand + n + 1;
     t.ftile = t.tile + n + 1;
     t.dom = t.ftile + n + 1;
-    t.total = t.dom + n + 1;
+    t.tdepth = t.dom + n + 1;
+    t.total = t.tdepth + n + 1;
     return t;
 }
+
+// 8x8 tile-depth words of a w x h camera view.
+uint32_t tdepth_tiles(uint32_t w, uint32_t h) { return ((w + 7u) / 8u) * ((h + 7u) / 8u); }
 
 void free_batch(hg_batch* b) {
     if (b->ctx && b->ctx->copy_stream) cudaStreamSynchronize(b->ctx->copy_stream);
@@ -131,6 +137,7 @@ void free_batch(hg_batch* b) {
     free_dev(b->color);
     free_dev(b->depth);
     free_dev(b->tile_depth);
+    free_dev(b->tdepth);
     free_dev(b->hair_list);
     free_dev(b->hair_count);
     free_dev(b->d_views);
@@ -166,6 +173,13 @@ void build_tables(hg_batch* b) {
             v.offsets = g->offsets[slot];
             v.indirect = g->indirect[slot];
             v.refs = g->refs[slot];
+            if (slot == 0) {
+                v.sorted = g->sorted[0];
+                v.sorted_off = g->sorted_off[0];
+                v.draw_order = g->draw_order[0];
+                v.order_meta = g->order_meta[0];
+                v.tiles_x = (b->w[i] + 7u) / 8u;
+            }
             v.cache = g->cache;
             v.strand_base = g->strand_base;
             v.strand_bundle = g->strand_bundle;
@@ -197,8 +211,10 @@ void build_tables(hg_batch* b) {
     for (uint32_t v = 0; v < n_views; ++v) t[to.bundle + v + 1] = t[to.bundle + v] + b->h_views[v].count;
     const uint32_t tw = b->tuning.tile_w, th = b->tuning.tile_h;
     const uint32_t fx = b->tuning.filter_tile == 1 ? 16u : 32u, fy = b->tuning.filter_tile == 1 ? 16u : 8u;
-    t[to.strand] = t[to.tile] = t[to.ftile] = t[to.dom] = 0;
+    t[to.strand] = t[to.tile] = t[to.ftile] = t[to.dom] = t[to.tdepth] = 0;
     for (uint32_t i = 0; i < n; ++i) {
+        t[to.tdepth + i + 1] = t[to.tdepth + i] + tdepth_tiles(b->w[i], b->h[i]);
+        b->h_views[i].tile_depth = b->tdepth + t[to.tdepth + i];
         t[to.strand + i + 1] = t[to.strand + i] + b->grooms[i]->strand_total;
         t[to.tile + i + 1] = t[to.tile + i] + ((b->w[i] + tw - 1) / tw) * ((b->h[i] + th - 1) / th);
         t[to.ftile + i + 1] = t[to.ftile + i] + ((b->w[i] + fx - 1) / fx) * ((b->h[i] + fy - 1) / fy);
@@ -214,6 +230,8 @@ void build_tables(hg_batch* b) {
     d.tile_prefix = b->d_tab + to.tile;
     d.ftile_prefix = b->d_tab + to.ftile;
     d.dom_prefix = b->d_tab + to.dom;
+    d.tdepth_prefix = b->d_tab + to.tdepth;
+    d.total_tdepth = t[to.tdepth + n];
     d.total_bundles = t[to.bundle + n_views];
     d.total_strands = t[to.strand + n];
     d.total_tiles = t[to.tile + n];
@@ -519,12 +537,15 @@ hg_status hg_batch_create(hg_ctx* ctx, const hg_batch_item* items, uint32_t coun
         max_tiles = std::max(max_tiles, (size_t)((b->w[i] + 7) / 8) * ((b->h[i] + 7) / 8));
     }
     alloc(b->tile_depth, max_tiles * 4);
+    uint64_t tdepth_words = 0;
+    for (uint32_t i = 0; i < count; ++i) tdepth_words += tdepth_tiles(b->w[i], b->h[i]);
+    alloc(b->tdepth, tdepth_words * 4);
     alloc(b->hair_list, max_px * 4);
     alloc(b->hair_count, 16);
     alloc(b->d_views, sizeof(hg::BatchView) * n_views);
     alloc(b->d_tab, sizeof(uint32_t) * to.total);
     alloc(b->d_lights, sizeof(hg_light) * HG_MAX_LIGHTS);
-    alloc(b->d_counters, sizeof(uint32_t) * 2);
+    alloc(b->d_counters, sizeof(uint32_t) * 3);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_views, sizeof(hg::BatchView) * n_views);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_tab, sizeof(uint32_t) * to.total);
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_lights, sizeof(hg_light) * HG_MAX_LIGHTS);
@@ -638,7 +659,8 @@ hg_status hg_batch_launches(hg_batch* b, hg_batch_mode mode, uint32_t* launches)
     k += d.total_bundles ? 2 : 0;                   // lod, scan expand
     k += 1;                                         // scan offsets
     k += d.total_strands ? 1 : 0;                   // generate
-    k += 1 + (d.n_views > d.n_cam ? 1 : 0);         // raster (+ DOM layers)
+    k += 2 + (d.total_tdepth ? 1 : 0);              // raster stages 1 and 2 (+ tile depths between them)
+    k += d.n_views > d.n_cam ? 1 : 0;               // DOM layers
     k += d.total_tiles ? 1 : 0;                     // shade
     k += d.filter ? 1 : 0;                          // filter
     k += 2;                                         // clear colour, composite

@@ -165,6 +165,14 @@ struct BatchView {
     uint32_t* offsets;
     uint32_t* indirect;
     hg_strand_ref* refs;
+    // camera views: front-to-back draw order (as the single-view scan builds
+    // it) and the per-8x8-tile depths between the two raster stages
+    uint32_t* sorted;
+    uint32_t* sorted_off;
+    uint32_t* draw_order;
+    uint32_t* order_meta;
+    uint32_t* tile_depth;
+    uint32_t tiles_x;
     float4* cache;                 // strand cache of the item's groom
     const uint32_t* strand_base;
     const uint32_t* strand_bundle;
@@ -199,6 +207,8 @@ struct BatchDev {
     const uint32_t* tile_prefix = nullptr;    // n_cam + 1, tile_w x tile_h pixel tiles
     const uint32_t* ftile_prefix = nullptr;   // n_cam + 1, filter tiles
     const uint32_t* dom_prefix = nullptr;     // n_cam + 1, DOM words (front + counters) per item
+    const uint32_t* tdepth_prefix = nullptr;  // n_cam + 1, 8x8 tile-depth words per camera view
+    uint32_t total_tdepth = 0;
     uint32_t total_bundles = 0, total_strands = 0, total_tiles = 0, total_ftiles = 0;
     uint64_t total_px = 0, total_dom_words = 0;
     unsigned long long* center = nullptr;     // arenas: every camera view's slice, concatenated
@@ -207,7 +217,7 @@ struct BatchDev {
     uint32_t* dom = nullptr;
     float4* color = nullptr;
     float* depth = nullptr;
-    uint32_t* counters = nullptr;             // work counters of the two raster launches
+    uint32_t* counters = nullptr;             // work counters of the three raster launches
     const hg_light* lights = nullptr;
     uint32_t n_lights = 0, ortho = 0;
     float exposure = 1.0f, depth_clear = 0.0f;

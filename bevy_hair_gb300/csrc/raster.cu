@@ -716,7 +716,8 @@ __device__ __forceinline__ int32_t run_of_lane(const StrandSmem& sm, int32_t run
 // Pixels per side of a tile of the camera pass's tile-depth buffer.
 constexpr int kTileShift = 3;
 // Stage boundaries of the camera pass over the refs in draw order, in 1/256ths.
-constexpr uint32_t kCameraStages[] = {0, 64, 256};
+constexpr uint32_t kCameraFirstStage = 64;
+constexpr uint32_t kCameraStages[] = {0, kCameraFirstStage, 256};
 constexpr int kCameraStageCount = sizeof(kCameraStages) / sizeof(kCameraStages[0]);
 
 // True when no sample of segment (pa, pb) (world, in sm.cp) / (A, B) (screen)
@@ -1126,6 +1127,12 @@ __global__ void __launch_bounds__(kRasterThreads, raster_min_blocks<MODE>()) ras
 // one launch each.  Work is indexed across views through prefix tables; a
 // view's arguments are read in place from the device view table.
 
+// Refs of a camera view drawn in the first stage: the nearest quarter
+// (kCameraStages), as the single-view pass splits them.
+__device__ __forceinline__ uint32_t camera_stage_split(uint32_t total) {
+    return (uint32_t)(((unsigned long long)total * kCameraFirstStage) >> 8);
+}
+
 // Largest v in [0, n) with prefix[v] <= x, for x < prefix[n].  Plain loads:
 // the prefix is in global memory for some callers and shared for others.
 __device__ __forceinline__ uint32_t find_view(const uint32_t* prefix, uint32_t n, uint32_t x) {
@@ -1157,9 +1164,12 @@ __global__ void batch_lod_kernel(const BatchView* __restrict__ views, const uint
     lod_bundle(a.p, a.bundles, a.layers, a.lod, a.depth_key, w - prefix[v], lane);
 }
 
+// Camera views also get the front-to-back draw order of the single-view scan.
 __global__ void __launch_bounds__(kScanThreads) batch_scan_offsets_kernel(const BatchView* __restrict__ views) {
     const BatchView& a = views[blockIdx.x];
-    scan_offsets_block(a.lod, a.count, a.capacity, a.offsets, a.indirect, nullptr, nullptr, nullptr, nullptr);
+    const bool cam = a.p.pass_mode[0] == 0u && a.sorted;
+    scan_offsets_block(a.lod, a.count, a.capacity, a.offsets, a.indirect, cam ? a.depth_key : nullptr,
+                       cam ? a.sorted : nullptr, a.sorted_off, a.order_meta);
 }
 
 __global__ void batch_scan_expand_kernel(const BatchView* __restrict__ views, const uint32_t* __restrict__ prefix,
@@ -1168,14 +1178,46 @@ __global__ void batch_scan_expand_kernel(const BatchView* __restrict__ views, co
     if (w >= total) return;
     const uint32_t v = find_view(prefix, n_views, w);
     const BatchView& a = views[v];
-    const uint32_t b = w - prefix[v];
+    const uint32_t k = w - prefix[v];
+    // camera views: warp k expands the k-th live bundle in draw order and
+    // writes its draw-order entries; other views: bundle k
+    const bool cam = a.p.pass_mode[0] == 0u && a.sorted;
+    if (cam && k >= a.order_meta[0]) return;
+    const uint32_t b = cam ? a.sorted[k] : k;
+    const bool order = cam && a.order_meta[1] != 0u;
     const hg_lod_record rec = a.lod[b];
-    const uint32_t off = a.offsets[b];
+    const uint32_t off = a.offsets[b], dpos = cam ? a.sorted_off[k] : 0u;
     for (uint32_t s = lane; s < rec.n_lod; s += 32u) {
         const uint32_t i = off + s;
         if (i >= a.capacity) break;
         reinterpret_cast<uint4*>(a.refs)[i] = make_uint4(b, s, rec.n_lod, rec.control_points);
+        if (order) a.draw_order[dpos + s] = i;
     }
+}
+
+// 8x8 tile depths of every camera view (tile_depth_kernel per view): warp per
+// tile of the concatenated tile space.
+__global__ void __launch_bounds__(256) batch_tile_depth_kernel(const BatchView* __restrict__ views,
+                                                               const uint32_t* __restrict__ prefix, uint32_t n_cam,
+                                                               uint32_t total) {
+    const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
+    if (w >= total) return;
+    const uint32_t v = find_view(prefix, n_cam, w);
+    const BatchView& a = views[v];
+    const uint32_t tile = w - prefix[v];
+    const uint32_t tx = tile % a.tiles_x, ty = tile / a.tiles_x;
+    uint32_t held = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < 2; ++k) {
+        const uint32_t x = (tx << kTileShift) + (lane & 7u), y = (ty << kTileShift) + (lane >> 3) + 4u * k;
+        if (x < a.width && y < a.height) {
+            const size_t i = (size_t)y * a.width + x;
+            held = max(held, max(hi_word(&a.cons[i]) >> 8, hi_word(&a.center[i]) >> 8));
+            held = max(held, __ldcg(&a.beta[i]) >> 8);
+        }
+    }
+    held = __reduce_max_sync(0xffffffffu, held);
+    if (lane == 0) a.tile_depth[tile] = held;
 }
 
 __global__ void __launch_bounds__(kRasterThreads) batch_generate_kernel(const BatchView* __restrict__ views,
@@ -1194,9 +1236,12 @@ __global__ void __launch_bounds__(kRasterThreads) batch_generate_kernel(const Ba
 
 // Persistent raster over the refs of views [first, first + n): warps take
 // `chunk` consecutive refs of the concatenated ref space at a time from a
-// global counter, so grooms of very different sizes share the SMs.  PHASE 0
-// runs camera views (pass_mode.x 0) and DOM depth views; PHASE 1 runs the
-// DOM views' layer pass.
+// global counter, so grooms of very different sizes share the SMs.  Camera
+// views draw their refs front to back (the scan's draw order) in two stages,
+// as the single-view pass does: PHASE 0 runs the nearest quarter of every
+// camera view's refs and every DOM depth view; PHASE 2 the rest of the camera
+// refs, skipping segments hidden behind the tile depths built between the
+// two; PHASE 1 the DOM views' layer pass.
 template <int PHASE>
 __global__ void __launch_bounds__(kRasterThreads, 6) batch_raster_kernel(const BatchView* __restrict__ views,
                                                                          uint32_t first, uint32_t n,
@@ -1212,7 +1257,14 @@ __global__ void __launch_bounds__(kRasterThreads, 6) batch_raster_kernel(const B
 #pragma unroll
         for (int k = 0; k < (int)(kBatchMaxViews / 32); ++k) {
             const uint32_t v = lane * (kBatchMaxViews / 32) + k;
-            t[k] = v < n ? min(views[first + v].indirect[0], views[first + v].capacity) : 0u;
+            uint32_t c = 0;
+            if (v < n) {
+                const BatchView& a = views[first + v];
+                const uint32_t total = min(a.indirect[0], a.capacity);
+                if (PHASE == 1 || a.p.pass_mode[0] != 0u) c = PHASE == 2 ? 0u : total;
+                else c = PHASE == 0 ? camera_stage_split(total) : total - camera_stage_split(total);
+            }
+            t[k] = c;
             sum += t[k];
         }
         uint32_t incl = sum;
@@ -1242,7 +1294,13 @@ __global__ void __launch_bounds__(kRasterThreads, 6) batch_raster_kernel(const B
         for (uint32_t r = start; r < end; ++r) {
             if (r < prefix[v] || r >= prefix[v + 1]) v = find_view(prefix, n, r);
             const BatchView& a = views[first + v];
-            const hg_strand_ref ref = a.refs[r - prefix[v]];
+            const bool cam = PHASE != 1 && a.p.pass_mode[0] == 0u;
+            uint32_t pos = r - prefix[v];
+            if (cam) {
+                if (PHASE == 2) pos += camera_stage_split(min(a.indirect[0], a.capacity));
+                if (a.sorted && a.order_meta[1]) pos = a.draw_order[pos];
+            }
+            const hg_strand_ref ref = a.refs[pos];
             if (ref.bundle >= a.bundle_count) {
                 if (lane == 0) atomicOr(a.err, kErrBadRef);
                 continue;
@@ -1252,10 +1310,10 @@ __global__ void __launch_bounds__(kRasterThreads, 6) batch_raster_kernel(const B
             if (PHASE == 1) {
                 const uint32_t ncp = generate_strand<2>(a, sm, ref, bundle, uv, lane);
                 raster_dom<2>(a, sm, ncp, lane);
-            } else if (a.p.pass_mode[0] == 0u) {
+            } else if (cam) {
                 const uint32_t ncp = generate_strand<0>(a, sm, ref, bundle, uv, lane);
                 float beta = __fdiv_rn(__uint2float_rn(ref.n_lod), __uint2float_rn(max(bundle.strand_count, 1u)));
-                raster_camera(a, sm, ncp, uv, beta, lane);
+                raster_camera(a, sm, ncp, uv, beta, lane, PHASE == 2 ? a.tile_depth : nullptr, a.tiles_x);
             } else {
                 const uint32_t ncp = generate_strand<1>(a, sm, ref, bundle, uv, lane);
                 raster_dom<1>(a, sm, ncp, lane);
@@ -2014,12 +2072,21 @@ cudaError_t batch_occupancy(uint32_t* raster_per_sm, uint32_t* gen_per_sm) {
 }
 
 cudaError_t launch_batch_raster(hg_ctx* ctx, const BatchDev& b) {
-    cudaError_t e = cudaMemsetAsync(b.counters, 0, 2 * sizeof(uint32_t), ctx->stream);
+    cudaError_t e = cudaMemsetAsync(b.counters, 0, 3 * sizeof(uint32_t), ctx->stream);
     if (e != cudaSuccess) return e;
     const uint32_t per_sm = std::max(1u, b.raster_blocks_per_sm);
     const int blocks = ctx->sm_count * (int)per_sm;
     const uint32_t chunk = b.raster_chunk ? b.raster_chunk : 1u;
+    // stage 1: nearest quarter of the camera refs + DOM depth views
     batch_raster_kernel<0><<<blocks, kRasterThreads, 0, ctx->stream>>>(b.views, 0u, b.n_views, b.counters, chunk);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    // tile depths of the camera views, then stage 2: the rest of the camera refs
+    if (b.total_tdepth) {
+        const uint32_t tblocks = (b.total_tdepth + 7u) / 8u;
+        batch_tile_depth_kernel<<<tblocks, 256, 0, ctx->stream>>>(b.views, b.tdepth_prefix, b.n_cam, b.total_tdepth);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    batch_raster_kernel<2><<<blocks, kRasterThreads, 0, ctx->stream>>>(b.views, 0u, b.n_cam, b.counters + 2, chunk);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if (b.n_views > b.n_cam) {
         batch_raster_kernel<1><<<blocks, kRasterThreads, 0, ctx->stream>>>(b.views, b.n_cam, b.n_views - b.n_cam,
