@@ -367,6 +367,9 @@ struct alignas(16) StrandSmem {
     float4 ct[128];  // camera: world tangent xyz + w (uvw.z)
     float4 cs[128];  // screen xy, ao; camera: RN(1/n) for the segment's DDA step count n
     float vd[128];   // camera: view distance of the control point (project_world)
+    hg_strand_ref next_ref;  // the warp's next ref, copied ahead (cp.async)
+    uint32_t next_idx;       // the draw-order entry after it
+    uint32_t pad_[3];
     union {
         struct {
             float4 lp[16];  // layer sample: position, ao
@@ -654,6 +657,12 @@ __device__ __forceinline__ float sqrt_bound(float r) {
     return x;
 }
 
+// The centre-disk test's bound on |o|^2: length(o) <= diameter / 2
+// (raster.wgsl:206-212), the diameter at least 0.05.
+__device__ __forceinline__ float camera_r2_max(const hg_hair_params& p) {
+    return sqrt_bound(fmaxf(p.appearance[3], 0.05f) * 0.5f);
+}
+
 // High 32 bits of a G-buffer word, read through L2 (little endian: the second u32).
 __device__ __forceinline__ uint32_t hi_word(const unsigned long long* w) {
     return __ldcg(reinterpret_cast<const unsigned int*>(w) + 1);
@@ -676,24 +685,43 @@ __device__ __forceinline__ bool on_screen(int32_t x, int32_t y, int32_t w, int32
 // strand into samples and hand them to the 32 lanes 32 at a time; segments
 // with samples ("runs") are listed in order with their first sample.
 
-// Appends this round's 32 segments (one per lane, cnt samples each, tag
-// stored with the run) to the run list.  Every lane of the warp calls it.
-__device__ __forceinline__ void append_runs(StrandSmem& sm, int32_t cnt, int32_t tag, uint32_t lane,
-                                            int32_t& carry, int32_t& runs) {
-    int32_t incl = cnt;
+// Lists a strand's runs: segment lane + 32 k has cnt[k] samples, and each
+// segment with samples is appended in segment order with its first sample
+// (sm.u.run.off) and its index | (cnt - 1) << 8 (sm.u.run.seg).  The four
+// rounds' exclusive offsets come from two warp prefix sums, two rounds
+// sharing a 32-bit word 16 bits each (a round's total is at most
+// 32 (kMaxSteps + 1) < 2^16).  Leaves the strand's sample total and run
+// count.  Every lane of the warp calls it.
+__device__ __forceinline__ void append_runs4(StrandSmem& sm, const int32_t (&cnt)[4], uint32_t lane, int32_t& total,
+                                             int32_t& runs) {
+    static_assert(32 * (kMaxSteps + 1) < 65536, "a round's sample count must fit 16 bits");
+    uint32_t w01 = (uint32_t)cnt[0] | (uint32_t)cnt[1] << 16u, w23 = (uint32_t)cnt[2] | (uint32_t)cnt[3] << 16u;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        int32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-        if ((int32_t)lane >= o) incl += y;
+        const uint32_t y01 = __shfl_up_sync(0xffffffffu, w01, o), y23 = __shfl_up_sync(0xffffffffu, w23, o);
+        if ((int32_t)lane >= o) {
+            w01 += y01;
+            w23 += y23;
+        }
     }
-    const uint32_t live = __ballot_sync(0xffffffffu, cnt > 0);
-    if (cnt > 0) {
-        const int32_t r = runs + __popc(live & ((1u << lane) - 1u));
-        sm.u.run.off[r] = carry + incl - cnt;
-        sm.u.run.seg[r] = tag;
+    const uint32_t t01 = __shfl_sync(0xffffffffu, w01, 31), t23 = __shfl_sync(0xffffffffu, w23, 31);
+    const uint32_t below = (1u << lane) - 1u;
+    int32_t carry = 0;
+    runs = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t sh = 16u * (uint32_t)(k & 1);
+        const int32_t incl = (int32_t)(((k < 2 ? w01 : w23) >> sh) & 0xffffu);
+        const uint32_t live = __ballot_sync(0xffffffffu, cnt[k] > 0);
+        if (cnt[k] > 0) {
+            const int32_t r = runs + __popc(live & below);
+            sm.u.run.off[r] = carry + incl - cnt[k];
+            sm.u.run.seg[r] = ((int32_t)lane + 32 * k) | (cnt[k] - 1) << 8;
+        }
+        carry += (int32_t)(((k < 2 ? t01 : t23) >> sh) & 0xffffu);
+        runs += __popc(live);
     }
-    carry += __shfl_sync(0xffffffffu, incl, 31);
-    runs += __popc(live);
+    total = carry;
 }
 
 // The run holding sample base + lane, for the window of samples [base,
@@ -716,7 +744,12 @@ __device__ __forceinline__ int32_t run_of_lane(const StrandSmem& sm, int32_t run
 // Pixels per side of a tile of the camera pass's tile-depth buffer.
 constexpr int kTileShift = 3;
 // Stage boundaries of the camera pass over the refs in draw order, in 1/256ths.
-constexpr uint32_t kCameraFirstStage = 64;
+// The first stage draws the nearest 7/16 without tile depths; the tile depths
+// it leaves then hide most of the rest.  Measured on 100k wavy strands at
+// 1920x1080 (camera raster ms): first stage 1/8 0.440, 1/4 0.380, 3/8 0.352,
+// 7/16 0.352, 1/2 0.352, 5/8 0.376, 3/4 0.401; three stages (3/8, 11/16)
+// 0.369.
+constexpr uint32_t kCameraFirstStage = 112;
 constexpr uint32_t kCameraStages[] = {0, kCameraFirstStage, 256};
 constexpr int kCameraStageCount = sizeof(kCameraStages) / sizeof(kCameraStages[0]);
 
@@ -734,7 +767,9 @@ constexpr int kCameraStageCount = sizeof(kCameraStages) / sizeof(kCameraStages[0
 //    1e-5 (M + C), about 5x their sum, and quantize_depth is monotone;
 //  - a word with depth D < the sample's depth d rejects the sample's
 //    payload (depth in the high bits) and its beta word (d << 8 | beta) alike.
-// Non-finite or very large coordinates are never rejected.
+// Non-finite or very large coordinates are never rejected, nor are segments
+// whose pixel box spans more than 2 x 2 tiles (four fixed loads keep the test
+// branch-free; it measured faster than walking up to six tiles).
 __device__ __forceinline__ bool hidden_segment(const hg_hair_params& p, const uint32_t* tile_depth, uint32_t tiles_x,
                                                int32_t width, int32_t height, float4 pa, float4 pb, float4 A, float4 B,
                                                f3 cam, f3 fwd) {
@@ -745,16 +780,17 @@ __device__ __forceinline__ bool hidden_segment(const hg_hair_params& p, const ui
     if (x0 > x1 || y0 > y1) return true;  // nothing on screen
     if (!tile_depth) return false;
     const int32_t tx0 = x0 >> kTileShift, tx1 = x1 >> kTileShift, ty0 = y0 >> kTileShift, ty1 = y1 >> kTileShift;
-    if ((tx1 - tx0 + 1) * (ty1 - ty0 + 1) > 6) return false;
+    if (tx1 - tx0 > 1 || ty1 - ty0 > 1) return false;
     const float d0 = dot3(sub3(xyz(pa), cam), fwd), d1 = dot3(sub3(xyz(pb), cam), fwd);
     const float m = fmaxf(fmaxf(fmaxf(fabsf(pa.x), fabsf(pa.y)), fmaxf(fabsf(pa.z), fabsf(pb.x))),
                           fmaxf(fabsf(pb.y), fabsf(pb.z)));
     const float c = fmaxf(fmaxf(fabsf(cam.x), fabsf(cam.y)), fabsf(cam.z));
     if (!(fabsf(d0) < 1e30f && fabsf(d1) < 1e30f && m < 1e30f)) return false;
     const uint32_t lower = quantize_depth(fminf(d0, d1) - 1e-5f * (m + c), p.screen[2], p.screen[3]);
-    uint32_t held = 0;
-    for (int32_t ty = ty0; ty <= ty1; ++ty)
-        for (int32_t tx = tx0; tx <= tx1; ++tx) held = max(held, __ldg(&tile_depth[(uint32_t)ty * tiles_x + tx]));
+    // at most 2 x 2 tiles, read as four loads (repeats when the box spans one)
+    const uint32_t* row0 = tile_depth + (uint32_t)ty0 * tiles_x;
+    const uint32_t* row1 = tile_depth + (uint32_t)ty1 * tiles_x;
+    const uint32_t held = max(max(__ldg(row0 + tx0), __ldg(row0 + tx1)), max(__ldg(row1 + tx0), __ldg(row1 + tx1)));
     return lower > held;
 }
 
@@ -808,8 +844,8 @@ __global__ void __launch_bounds__(256) tile_depth_kernel(const unsigned long lon
 // diagonal step, the two side pixels.
 template <class Args>
 __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uint32_t ncp, float2 uv,
-                                              float beta, uint32_t lane, const uint32_t* tile_depth = nullptr,
-                                              uint32_t tiles_x = 0) {
+                                              float beta, uint32_t lane, float r2_max,
+                                              const uint32_t* tile_depth = nullptr, uint32_t tiles_x = 0) {
     const hg_hair_params& p = a.p;
     const int32_t nseg = (int32_t)ncp - 1;
     const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
@@ -818,12 +854,13 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
     // Sample offsets: a segment with both ends behind the camera, or hidden
     // behind the tile depths, has no samples, every other one n + 1 >= 2; the
     // non-empty segments are listed in order with their first sample.
-    int32_t carry = 0, runs = 0;
+    int32_t cnts[4];
     float mag = 0.0f;  // largest |coordinate| of the strand's control points
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         int32_t j = (int32_t)lane + 32 * k;
-        int32_t cnt = 0;
+        int32_t& cnt = cnts[k];
+        cnt = 0;
         if (j < nseg) {
             float4 pa = sm.cp[j], pb = sm.cp[j + 1];
             mag = fmaxf(mag, fmaxf(fmaxf(fmaxf(fabsf(pa.x), fabsf(pa.y)), fmaxf(fabsf(pa.z), fabsf(pb.x))),
@@ -839,11 +876,11 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
             }
             sm.cs[j].w = n > 0 ? __frcp_rn(__int2float_rn(n)) : 0.0f;
         }
-        append_runs(sm, cnt, j | (cnt - 1) << 8, lane, carry, runs);
     }
+    int32_t total, runs;
+    append_runs4(sm, cnts, lane, total, runs);
     __syncwarp();
 
-    const int32_t total = carry;
     // Depth pre-test.  A sample's computed view distance lies within
     // 42 u (M + C) (u = 2^-24; M, C: largest control-point and camera
     // coordinate) of mix(vd[j], vd[j+1], t) computed in floats: 21 u (M + C)
@@ -856,7 +893,6 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
     const float cmag = fmaxf(fmaxf(fabsf(cam.x), fabsf(cam.y)), fabsf(cam.z));
     const float slack = 1e-5f * (__uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(mag))) + cmag);
     const float inv_range = __frcp_rn(fmaxf(p.screen[3] - p.screen[2], 1e-3f));
-    const float r2_max = sqrt_bound(fmaxf(p.appearance[3], 0.05f) * 0.5f);
     const uint32_t beta_q = f2u(clampf(beta, 0.0f, 1.0f) * 255.0f + 0.5f);
     const bool ao_on = p.flags[2] != 0u;
     const uint32_t quv = quant63(uv.x) | quant63(uv.y) << 6u;
@@ -1089,6 +1125,37 @@ __global__ void __launch_bounds__(kRasterThreads) generate_kernel(const GenArgs 
         generate_one(a, g, lp[warp], lt[warp], ls[warp], lane);
 }
 
+// Asynchronous global -> shared copies (cp.async) of the ref loop's next
+// entries; the issuing lane waits for them before it or its warp reads them.
+__device__ __forceinline__ void copy_async16(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void copy_async4(void* dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(dst)), "l"(src)
+                 : "memory");
+}
+__device__ __forceinline__ void copy_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void copy_async_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// sm.next_idx = the ref index drawn at position k: order[k], or k itself.
+__device__ __forceinline__ void fetch_order(StrandSmem& sm, const uint32_t* order, uint32_t k) {
+    if (order) copy_async4(&sm.next_idx, order + k);
+    else sm.next_idx = k;
+}
+
+// Prefetches the strand cache slot of `ref` (both of its arrays, 2 x 65
+// float4, contiguous) into L2 with one bulk prefetch.  Slots are 2,080 bytes
+// apart from a 256-byte aligned base: the address and the size are multiples
+// of 16 bytes as the instruction requires.  A hint only: nothing waits on it.
+template <class Args>
+__device__ __forceinline__ void prefetch_cache_slot(const Args& a, const hg_strand_ref& ref) {
+    if (!a.cache || ref.control_points != kCacheCps || ref.bundle >= a.bundle_count) return;
+    const float4* slot = a.cache + (size_t)(a.strand_base[ref.bundle] + ref.strand) * (2u * kCacheCps);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(slot), "r"((uint32_t)(2u * kCacheCps * 16u))
+                 : "memory");
+}
+
 // raster.wgsl:225-337: one warp per strand ref, persistent over the refs.
 template <int MODE>
 __global__ void __launch_bounds__(kRasterThreads, raster_min_blocks<MODE>()) raster_kernel(const RasterArgs a) {
@@ -1103,8 +1170,30 @@ __global__ void __launch_bounds__(kRasterThreads, raster_min_blocks<MODE>()) ras
     // full_order expects.
     if (MODE == 1 && a.full_order && total == (unsigned long long)a.full_total) order = a.full_order;
     const uint32_t nwarps = gridDim.x * kRasterWarps;
-    for (uint32_t r = r0 + blockIdx.x * kRasterWarps + warp; r < r1; r += nwarps) {
-        const hg_strand_ref ref = a.refs[order ? order[r] : r];
+    const float r2_max = MODE == 0 ? camera_r2_max(a.p) : 0.0f;
+    // Software-pipelined over the refs: the draw-order entry two steps ahead
+    // and the ref one step ahead are loaded before they are needed, and the
+    // next strand's cache slot is prefetched into L2 while this strand is
+    // drawn.  Without that every strand starts with a chain of dependent
+    // loads (draw order, ref, strand base, cache slot) the warp waits on.
+    uint32_t r = r0 + blockIdx.x * kRasterWarps + warp;
+    if (lane == 0) {
+        if (r < r1) copy_async16(&sm.next_ref, &a.refs[order ? order[r] : r]);
+        if (r + nwarps < r1) fetch_order(sm, order, r + nwarps);
+        copy_async_commit();
+    }
+    for (; r < r1; r += nwarps) {
+        if (lane == 0) copy_async_wait();
+        __syncwarp();
+        const hg_strand_ref ref = sm.next_ref;
+        const uint32_t next_idx = sm.next_idx;
+        __syncwarp();
+        const bool more = r + nwarps < r1;
+        if (lane == 0) {
+            if (more) copy_async16(&sm.next_ref, &a.refs[next_idx]);
+            if (r + 2u * nwarps < r1) fetch_order(sm, order, r + 2u * nwarps);
+            copy_async_commit();
+        }
         if (ref.bundle >= a.bundle_count) {
             if (lane == 0) atomicOr(a.err, kErrBadRef);
             continue;
@@ -1112,9 +1201,13 @@ __global__ void __launch_bounds__(kRasterThreads, raster_min_blocks<MODE>()) ras
         const hg_gpu_bundle bundle = a.bundles[ref.bundle];
         const float2 uv = pcg_uv(ref.strand ^ (ref.bundle * 0x85ebca6bu));
         const uint32_t ncp = generate_strand<MODE>(a, sm, ref, bundle, uv, lane);
+        if (lane == 0 && more) {
+            copy_async_wait();
+            prefetch_cache_slot(a, sm.next_ref);
+        }
         if (MODE == 0) {
             float beta = __fdiv_rn(__uint2float_rn(ref.n_lod), __uint2float_rn(max(bundle.strand_count, 1u)));
-            raster_camera(a, sm, ncp, uv, beta, lane, a.tile_depth, a.tiles_x);
+            raster_camera(a, sm, ncp, uv, beta, lane, r2_max, a.tile_depth, a.tiles_x);
         } else {
             raster_dom<MODE>(a, sm, ncp, lane);
         }
@@ -1127,8 +1220,8 @@ __global__ void __launch_bounds__(kRasterThreads, raster_min_blocks<MODE>()) ras
 // one launch each.  Work is indexed across views through prefix tables; a
 // view's arguments are read in place from the device view table.
 
-// Refs of a camera view drawn in the first stage: the nearest quarter
-// (kCameraStages), as the single-view pass splits them.
+// Refs of a camera view drawn in the first stage: the nearest
+// kCameraFirstStage / 256, as the single-view pass splits them.
 __device__ __forceinline__ uint32_t camera_stage_split(uint32_t total) {
     return (uint32_t)(((unsigned long long)total * kCameraFirstStage) >> 8);
 }
@@ -1238,7 +1331,7 @@ __global__ void __launch_bounds__(kRasterThreads) batch_generate_kernel(const Ba
 // `chunk` consecutive refs of the concatenated ref space at a time from a
 // global counter, so grooms of very different sizes share the SMs.  Camera
 // views draw their refs front to back (the scan's draw order) in two stages,
-// as the single-view pass does: PHASE 0 runs the nearest quarter of every
+// as the single-view pass does: PHASE 0 runs the nearest 7/16 of every
 // camera view's refs and every DOM depth view; PHASE 2 the rest of the camera
 // refs, skipping segments hidden behind the tile depths built between the
 // two; PHASE 1 the DOM views' layer pass.
@@ -1313,7 +1406,8 @@ __global__ void __launch_bounds__(kRasterThreads, 6) batch_raster_kernel(const B
             } else if (cam) {
                 const uint32_t ncp = generate_strand<0>(a, sm, ref, bundle, uv, lane);
                 float beta = __fdiv_rn(__uint2float_rn(ref.n_lod), __uint2float_rn(max(bundle.strand_count, 1u)));
-                raster_camera(a, sm, ncp, uv, beta, lane, PHASE == 2 ? a.tile_depth : nullptr, a.tiles_x);
+                raster_camera(a, sm, ncp, uv, beta, lane, camera_r2_max(a.p), PHASE == 2 ? a.tile_depth : nullptr,
+                              a.tiles_x);
             } else {
                 const uint32_t ncp = generate_strand<1>(a, sm, ref, bundle, uv, lane);
                 raster_dom<1>(a, sm, ncp, lane);
@@ -1545,7 +1639,7 @@ __global__ void __launch_bounds__(kResolveThreads, 3) tile_resolve_kernel(const 
     const f3 fwd = mk3(p.camera_forward[0], p.camera_forward[1], p.camera_forward[2]);
     const float cmag = fmaxf(fmaxf(fabsf(cam.x), fabsf(cam.y)), fabsf(cam.z));
     const float inv_range = __frcp_rn(fmaxf(p.screen[3] - p.screen[2], 1e-3f));
-    const float r2_max = sqrt_bound(fmaxf(p.appearance[3], 0.05f) * 0.5f);
+    const float r2_max = camera_r2_max(p);
     const bool ao_on = p.flags[2] != 0u;
     const bool rev = p.pass_mode[2] == 1u;
     SegStage& st = stage[warp];
@@ -1787,7 +1881,7 @@ __global__ void __launch_bounds__(kRasterThreads) long_segment_kernel(const Rast
             sm.vd[lane] = dot3(sub3(xyz(wp), cam), fwd);
         }
         __syncwarp();
-        raster_camera(a, sm, 2u, uv, beta, lane);
+        raster_camera(a, sm, 2u, uv, beta, lane, camera_r2_max(a.p));
         __syncwarp();
     }
 }
@@ -1995,8 +2089,10 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
     a.tile_depth = nullptr;
     a.tiles_x = 0;
     uint32_t mode = p.pass_mode[0];
-    // One warp per ref slot, no persistence: raster launches on different
-    // streams then share the SMs through the block scheduler.
+    // Persistent: as many blocks as stay resident (at most one warp per ref
+    // slot), each warp walking the refs with a stride of the grid's warps,
+    // which lets it fetch its next ref and prefetch that strand's cache slot
+    // while it draws the current one.
     int blocks = (int)std::max<size_t>((g->ref_capacity + kRasterWarps - 1) / kRasterWarps, 1);
     if (mode == 0 && ctx->camera_raster == HG_CAMERA_RASTER_BINNED && g->ref_capacity <= kBinMaxSlots) {
         return launch_camera_binned(ctx, g, a);
@@ -2019,15 +2115,17 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
                 a.tiles_x = tiles_x;
             }
             const size_t part = (g->ref_capacity * (a.part_hi - a.part_lo) + 255) / 256 + 1;
-            const int stage_blocks = (int)std::max<size_t>((part + kRasterWarps - 1) / kRasterWarps, 1);
+            const int stage_blocks = (int)std::max<size_t>(
+                std::min<size_t>((part + kRasterWarps - 1) / kRasterWarps, (size_t)ctx->sm_count * raster_min_blocks<0>()),
+                1);
             raster_kernel<0><<<stage_blocks, kRasterThreads, 0, ctx->stream>>>(a);
             cudaError_t e = cudaGetLastError();
             if (e != cudaSuccess) return e;
         }
     } else if (mode == 1) {
-        raster_kernel<1><<<blocks, kRasterThreads, 0, ctx->stream>>>(a);
+        raster_kernel<1><<<std::min(blocks, ctx->sm_count * raster_min_blocks<1>()), kRasterThreads, 0, ctx->stream>>>(a);
     } else {
-        raster_kernel<2><<<blocks, kRasterThreads, 0, ctx->stream>>>(a);
+        raster_kernel<2><<<std::min(blocks, ctx->sm_count * raster_min_blocks<2>()), kRasterThreads, 0, ctx->stream>>>(a);
     }
     return cudaGetLastError();
 }
@@ -2077,7 +2175,7 @@ cudaError_t launch_batch_raster(hg_ctx* ctx, const BatchDev& b) {
     const uint32_t per_sm = std::max(1u, b.raster_blocks_per_sm);
     const int blocks = ctx->sm_count * (int)per_sm;
     const uint32_t chunk = b.raster_chunk ? b.raster_chunk : 1u;
-    // stage 1: nearest quarter of the camera refs + DOM depth views
+    // stage 1: nearest 7/16 of the camera refs + DOM depth views
     batch_raster_kernel<0><<<blocks, kRasterThreads, 0, ctx->stream>>>(b.views, 0u, b.n_views, b.counters, chunk);
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     // tile depths of the camera views, then stage 2: the rest of the camera refs
