@@ -327,7 +327,7 @@ hg_status hg_ensure_targets(hg_ctx* ctx, uint32_t width, uint32_t height, uint32
     alloc(ctx->depth, px * 4);
     alloc(ctx->hair_list, px * 4);
     alloc(ctx->hair_count, 16);
-    alloc(ctx->tile_depth, (size_t)((width + 7) / 8) * ((height + 7) / 8) * 4);
+    alloc(ctx->tile_depth, (size_t)hg::tiles_along(width) * hg::tiles_along(height) * 4);
     if (e != cudaSuccess) {
         free_targets(ctx);
         return cuda_fail(ctx, e, "allocating screen targets");

@@ -117,8 +117,8 @@ TabOffsets tab_offsets(uint32_t n, uint32_t n_views) {
     return t;
 }
 
-// 8x8 tile-depth words of a w x h camera view.
-uint32_t tdepth_tiles(uint32_t w, uint32_t h) { return ((w + 7u) / 8u) * ((h + 7u) / 8u); }
+// Tile-depth words of a w x h camera view.
+uint32_t tdepth_tiles(uint32_t w, uint32_t h) { return hg::tiles_along(w) * hg::tiles_along(h); }
 
 void free_batch(hg_batch* b) {
     if (b->ctx && b->ctx->copy_stream) cudaStreamSynchronize(b->ctx->copy_stream);
@@ -178,7 +178,7 @@ void build_tables(hg_batch* b) {
                 v.sorted_off = g->sorted_off[0];
                 v.draw_order = g->draw_order[0];
                 v.order_meta = g->order_meta[0];
-                v.tiles_x = (b->w[i] + 7u) / 8u;
+                v.tiles_x = hg::tiles_along(b->w[i]);
             }
             v.cache = g->cache;
             v.strand_base = g->strand_base;
@@ -534,7 +534,7 @@ hg_status hg_batch_create(hg_ctx* ctx, const hg_batch_item* items, uint32_t coun
     size_t max_px = 0, max_tiles = 0;
     for (uint32_t i = 0; i < count; ++i) {
         max_px = std::max(max_px, (size_t)b->w[i] * b->h[i]);
-        max_tiles = std::max(max_tiles, (size_t)((b->w[i] + 7) / 8) * ((b->h[i] + 7) / 8));
+        max_tiles = std::max(max_tiles, (size_t)tdepth_tiles(b->w[i], b->h[i]));
     }
     alloc(b->tile_depth, max_tiles * 4);
     uint64_t tdepth_words = 0;

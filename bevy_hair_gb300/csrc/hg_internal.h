@@ -239,6 +239,11 @@ cudaError_t launch_generate(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p);
 void release_bins(hg_groom* g);  // frees the binned camera raster's scratch
 constexpr uint32_t kStrandCacheCps = 65;
 
+// Pixels per side of a tile of the camera pass's tile-depth buffer, as a
+// shift, and the tile count of a w x h view.
+constexpr uint32_t kTileShift = 3;
+constexpr uint32_t tiles_along(uint32_t n) { return (n + (1u << kTileShift) - 1u) >> kTileShift; }
+
 // shade.cu
 cudaError_t launch_shade(hg_ctx* ctx, const hg_hair_params& p, uint32_t n_lights, uint32_t ortho, float exposure,
                          uint32_t model);

@@ -370,6 +370,7 @@ struct alignas(16) StrandSmem {
     hg_strand_ref next_ref;  // the warp's next ref, copied ahead (cp.async)
     uint32_t next_idx;       // the draw-order entry after it
     uint32_t pad_[3];
+    uint32_t finm[4];        // camera: bit l of word k set when control point 32 k + l is finite
     union {
         struct {
             float4 lp[16];  // layer sample: position, ao
@@ -579,9 +580,16 @@ __device__ __forceinline__ f3 cp_world_tangent(const hg_hair_params& p, uint32_t
     return dir_world(p, safe_normalize(calc_tangent(idx, ncp, pp, curr, nn)));
 }
 
-// Projection and shared-memory layout of one control point.
+__device__ __forceinline__ bool finite3(float a, float b, float c) {
+    const float inf = __int_as_float(0x7f800000);
+    return fabsf(a) < inf && fabsf(b) < inf && fabsf(c) < inf;
+}
+
+// Projection and shared-memory layout of one control point.  Returns, for
+// the camera pass, whether every value the camera raster mixes (world
+// position, tangent, w, screen position, ao) is finite.
 template <int MODE>
-__device__ __forceinline__ void store_cp(const hg_hair_params& p, StrandSmem& sm, uint32_t idx, f3 wp, f3 wt, float w,
+__device__ __forceinline__ bool store_cp(const hg_hair_params& p, StrandSmem& sm, uint32_t idx, f3 wp, f3 wt, float w,
                                          float ao) {
     const Projected pr = project_world(p, wp);
     sm.cp[idx] = make_float4(wp.x, wp.y, wp.z, pr.in_front ? 1.0f : 0.0f);
@@ -589,9 +597,11 @@ __device__ __forceinline__ void store_cp(const hg_hair_params& p, StrandSmem& sm
         sm.ct[idx] = make_float4(wt.x, wt.y, wt.z, w);
         sm.cs[idx] = make_float4(pr.screen.x, pr.screen.y, ao, 0.0f);
         sm.vd[idx] = pr.view_dist;
-    } else {
-        sm.cs[idx] = make_float4(pr.screen.x, pr.screen.y, 0.0f, 0.0f);
+        return finite3(wp.x, wp.y, wp.z) && finite3(wt.x, wt.y, wt.z) && finite3(w, ao, pr.screen.x) &&
+               finite3(pr.screen.y, 0.0f, 0.0f);
     }
+    sm.cs[idx] = make_float4(pr.screen.x, pr.screen.y, 0.0f, 0.0f);
+    return false;
 }
 
 template <int K, int MODE>
@@ -600,10 +610,15 @@ __device__ __forceinline__ void generate_slot(const hg_hair_params& p, StrandSme
     const uint32_t idx = lane + 32u * K;
     f3 prev = mp[K], next = mp[K];
     if (MODE == 0) cp_neighbours<K>(mp, lane, prev, next);
+    bool fin = false;
     if (idx < ncp) {
         const f3 wp = to_world(p, mp[K]);
         const f3 wt = MODE == 0 ? cp_world_tangent(p, idx, ncp, prev, mp[K], next) : mk3(0.0f, 0.0f, 0.0f);
-        store_cp<MODE>(p, sm, idx, wp, wt, wk[K], aok[K]);
+        fin = store_cp<MODE>(p, sm, idx, wp, wt, wk[K], aok[K]);
+    }
+    if (MODE == 0) {
+        const uint32_t m = __ballot_sync(0xffffffffu, fin);
+        if (lane == 0) sm.finm[K] = m;
     }
 }
 
@@ -623,12 +638,18 @@ __device__ __forceinline__ uint32_t generate_strand(const Args& a, StrandSmem& s
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const uint32_t idx = lane + 32u * k;
+            bool fin = false;
             if (idx < kCacheCps) {
                 const float4 wp = __ldg(pos + idx);
                 const float4 wt = MODE == 0 ? __ldg(tan + idx) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-                store_cp<MODE>(p, sm, idx, xyz(wp), xyz(wt), wt.w, wp.w);
+                fin = store_cp<MODE>(p, sm, idx, xyz(wp), xyz(wt), wt.w, wp.w);
+            }
+            if (MODE == 0) {
+                const uint32_t m = __ballot_sync(0xffffffffu, fin);
+                if (lane == 0) sm.finm[k] = m;
             }
         }
+        if (MODE == 0 && lane == 0) sm.finm[3] = 0u;
         __syncwarp();
         return ncp;
     }
@@ -687,13 +708,13 @@ __device__ __forceinline__ bool on_screen(int32_t x, int32_t y, int32_t w, int32
 
 // Lists a strand's runs: segment lane + 32 k has cnt[k] samples, and each
 // segment with samples is appended in segment order with its first sample
-// (sm.u.run.off) and its index | (cnt - 1) << 8 (sm.u.run.seg).  The four
+// (sm.u.run.off) and tag[k] (sm.u.run.seg).  The four
 // rounds' exclusive offsets come from two warp prefix sums, two rounds
 // sharing a 32-bit word 16 bits each (a round's total is at most
 // 32 (kMaxSteps + 1) < 2^16).  Leaves the strand's sample total and run
 // count.  Every lane of the warp calls it.
-__device__ __forceinline__ void append_runs4(StrandSmem& sm, const int32_t (&cnt)[4], uint32_t lane, int32_t& total,
-                                             int32_t& runs) {
+__device__ __forceinline__ void append_runs4(StrandSmem& sm, const int32_t (&cnt)[4], const int32_t (&tag)[4],
+                                             uint32_t lane, int32_t& total, int32_t& runs) {
     static_assert(32 * (kMaxSteps + 1) < 65536, "a round's sample count must fit 16 bits");
     uint32_t w01 = (uint32_t)cnt[0] | (uint32_t)cnt[1] << 16u, w23 = (uint32_t)cnt[2] | (uint32_t)cnt[3] << 16u;
 #pragma unroll
@@ -716,7 +737,7 @@ __device__ __forceinline__ void append_runs4(StrandSmem& sm, const int32_t (&cnt
         if (cnt[k] > 0) {
             const int32_t r = runs + __popc(live & below);
             sm.u.run.off[r] = carry + incl - cnt[k];
-            sm.u.run.seg[r] = ((int32_t)lane + 32 * k) | (cnt[k] - 1) << 8;
+            sm.u.run.seg[r] = tag[k];
         }
         carry += (int32_t)(((k < 2 ? t01 : t23) >> sh) & 0xffffu);
         runs += __popc(live);
@@ -741,8 +762,6 @@ __device__ __forceinline__ int32_t run_of_lane(const StrandSmem& sm, int32_t run
     return r;
 }
 
-// Pixels per side of a tile of the camera pass's tile-depth buffer.
-constexpr int kTileShift = 3;
 // Stage boundaries of the camera pass over the refs in draw order, in 1/256ths.
 // The first stage draws the nearest 7/16 without tile depths; the tile depths
 // it leaves then hide most of the rest.  Measured on 100k wavy strands at
@@ -794,6 +813,17 @@ __device__ __forceinline__ bool hidden_segment(const hg_hair_params& p, const ui
     return lower > held;
 }
 
+// Centre-disk test of segment (A, B) (screen) for the pixel centre (cx, cy)
+// (raster.wgsl:206-212): length(o) <= r is sqrt_rn(|o|^2) <= r, i.e.
+// |o|^2 <= r2_max.
+__device__ __forceinline__ bool in_centre_disk(float4 A, float4 B, float cx, float cy, float r2_max) {
+    const float gx = B.x - A.x, gy = B.y - A.y;
+    const float denom = fmaxf(gx * gx + gy * gy, 1e-6f);
+    const float closest = clampf(__fdiv_rn((cx - A.x) * gx + (cy - A.y) * gy, denom), 0.0f, 1.0f);
+    const float ox = cx - (A.x + gx * closest), oy = cy - (A.y + gy * closest);
+    return ox * ox + oy * oy <= r2_max;
+}
+
 // A lower bound of quantize_depth(d) for every d >= dist, within a few units
 // of it and without a division: (dist - near) times a rounded reciprocal of
 // the range differs from the correctly rounded quotient by at most 3 ulp of a
@@ -808,7 +838,27 @@ __device__ __forceinline__ uint32_t approx_depth(float dist, float near_, float 
     return r < 0x00fffffeu ? r : 0x00fffffeu;
 }
 
-// One warp per 8x8 tile: the largest quantised depth among the tile's
+// The largest quantised depth among the words of tile (tx, ty), pixels
+// (tx, ty) << kTileShift onwards (one warp, every lane gets it).
+__device__ __forceinline__ uint32_t tile_max_depth(const unsigned long long* center, const unsigned long long* cons,
+                                                   const uint32_t* beta, uint32_t width, uint32_t height, uint32_t tx,
+                                                   uint32_t ty, uint32_t lane) {
+    constexpr uint32_t kSide = 1u << kTileShift, kPixels = kSide * kSide;
+    uint32_t held = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < (kPixels + 31u) / 32u; ++k) {
+        const uint32_t q = 32u * k + lane;
+        const uint32_t x = (tx << kTileShift) + (q & (kSide - 1u)), y = (ty << kTileShift) + (q >> kTileShift);
+        if (q < kPixels && x < width && y < height) {
+            const size_t i = (size_t)y * width + x;
+            held = max(held, max(hi_word(&cons[i]) >> 8, hi_word(&center[i]) >> 8));
+            held = max(held, __ldcg(&beta[i]) >> 8);
+        }
+    }
+    return __reduce_max_sync(0xffffffffu, held);
+}
+
+// One warp per tile: the largest quantised depth among the tile's
 // conservative, centre and beta words (empty words count as the far value
 // 0xffffff, which rejects nothing; pixels beyond the screen edge are never
 // written and count as 0).
@@ -819,18 +869,7 @@ __global__ void __launch_bounds__(256) tile_depth_kernel(const unsigned long lon
                                                          uint32_t* __restrict__ tile_depth) {
     const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31u;
     if (tile >= tiles) return;
-    const uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
-    uint32_t held = 0;
-#pragma unroll
-    for (uint32_t k = 0; k < 2; ++k) {
-        const uint32_t x = (tx << kTileShift) + (lane & 7u), y = (ty << kTileShift) + (lane >> 3) + 4u * k;
-        if (x < width && y < height) {
-            const size_t i = (size_t)y * width + x;
-            held = max(held, max(hi_word(&cons[i]) >> 8, hi_word(&center[i]) >> 8));
-            held = max(held, __ldcg(&beta[i]) >> 8);
-        }
-    }
-    held = __reduce_max_sync(0xffffffffu, held);
+    const uint32_t held = tile_max_depth(center, cons, beta, width, height, tile % tiles_x, tile / tiles_x, lane);
     if (lane == 0) tile_depth[tile] = held;
 }
 
@@ -877,8 +916,40 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
             sm.cs[j].w = n > 0 ? __frcp_rn(__int2float_rn(n)) : 0.0f;
         }
     }
+    // A segment's first sample (t = 0) is the previous segment's last (t = 1):
+    // mix(a, b, 1) and mix(b, c, 0) both give b exactly when a and c are
+    // finite, so position, depth, tangent, w and ao, hence the payload, agree,
+    // and a first sample never writes side pixels.  Only the centre-disk test
+    // differs (it measures against each segment).  So when the previous
+    // segment has samples and both outer control points are finite, the
+    // segment starts at its second sample, and the previous segment's last
+    // sample takes the centre disk of either segment (tag bit 15).
+    uint32_t livem[4], finm[4], skipm[4];
+    int32_t tags[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        livem[k] = __ballot_sync(0xffffffffu, cnts[k] > 0);
+        finm[k] = sm.finm[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t prev_live = lane > 0 ? livem[k] >> (lane - 1u) & 1u : (k > 0 ? livem[k > 0 ? k - 1 : 0] >> 31 : 0u);
+        const uint32_t fin_prev = lane > 0 ? finm[k] >> (lane - 1u) & 1u : (k > 0 ? finm[k > 0 ? k - 1 : 0] >> 31 : 0u);
+        const uint32_t fin_next = lane < 31 ? finm[k] >> (lane + 1u) & 1u : (k < 3 ? finm[k < 3 ? k + 1 : 3] & 1u : 0u);
+        skipm[k] = __ballot_sync(0xffffffffu, cnts[k] > 0 && (prev_live & fin_prev & fin_next) != 0u);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t skip = skipm[k] >> lane & 1u;
+        const uint32_t dup_next = lane < 31 ? skipm[k] >> (lane + 1u) & 1u : (k < 3 ? skipm[k < 3 ? k + 1 : 3] & 1u : 0u);
+        tags[k] = 0;
+        if (cnts[k] > 0) {
+            tags[k] = ((int32_t)lane + 32 * k) | (int32_t)(skip << 7) | (cnts[k] - 1) << 8 | (int32_t)(dup_next << 15);
+            cnts[k] -= (int32_t)skip;
+        }
+    }
     int32_t total, runs;
-    append_runs4(sm, cnts, lane, total, runs);
+    append_runs4(sm, cnts, tags, lane, total, runs);
     __syncwarp();
 
     // Depth pre-test.  A sample's computed view distance lies within
@@ -903,9 +974,9 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
         const bool active = base + (int32_t)lane < total;
         const int32_t r = run_of_lane(sm, runs, rw, base, lane);
         const int32_t jn = sm.u.run.seg[r];
-        const int32_t j = jn & 0xff, i = s - sm.u.run.off[r];
+        const int32_t j = jn & 0x7f, n = (jn >> 8) & 0x7f, i = s - sm.u.run.off[r] + ((jn >> 7) & 1);
         const float4 A = sm.cs[j], B = sm.cs[j + 1];
-        const float t = step_t(i, jn >> 8, A.w);
+        const float t = step_t(i, n, A.w);
         const float sx = mixf(A.x, B.x, t), sy = mixf(A.y, B.y, t);
         const int32_t px = f2i(floorf(sx)), py = f2i(floorf(sy));
         int32_t qx = __shfl_up_sync(0xffffffffu, px, 1), qy = __shfl_up_sync(0xffffffffu, py, 1);
@@ -952,14 +1023,10 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
         bool w1 = on1 && lower <= cur_c1;
         bool w2 = on2 && lower <= cur_c2;
         if (wm) {
-            // centre-disk test (raster.wgsl:206-212); length(o) <= r is
-            // sqrt_rn(|o|^2) <= r, i.e. |o|^2 <= r2_max
             const float cx = __int2float_rn(px) + 0.5f, cy = __int2float_rn(py) + 0.5f;
-            const float gx = B.x - A.x, gy = B.y - A.y;
-            const float denom = fmaxf(gx * gx + gy * gy, 1e-6f);
-            const float closest = clampf(__fdiv_rn((cx - A.x) * gx + (cy - A.y) * gy, denom), 0.0f, 1.0f);
-            const float ox = cx - (A.x + gx * closest), oy = cy - (A.y + gy * closest);
-            wm = ox * ox + oy * oy <= r2_max;
+            wm = in_centre_disk(A, B, cx, cy, r2_max);
+            // the next segment's dropped first sample: its own segment's disk
+            if (!wm && i == n && (jn >> 15) != 0) wm = in_centre_disk(B, sm.cs[j + 2], cx, cy, r2_max);
         }
         if (!(w0 || wm || w1 || w2)) continue;
         if (a.scene) {
@@ -1298,18 +1365,8 @@ __global__ void __launch_bounds__(256) batch_tile_depth_kernel(const BatchView* 
     const uint32_t v = find_view(prefix, n_cam, w);
     const BatchView& a = views[v];
     const uint32_t tile = w - prefix[v];
-    const uint32_t tx = tile % a.tiles_x, ty = tile / a.tiles_x;
-    uint32_t held = 0;
-#pragma unroll
-    for (uint32_t k = 0; k < 2; ++k) {
-        const uint32_t x = (tx << kTileShift) + (lane & 7u), y = (ty << kTileShift) + (lane >> 3) + 4u * k;
-        if (x < a.width && y < a.height) {
-            const size_t i = (size_t)y * a.width + x;
-            held = max(held, max(hi_word(&a.cons[i]) >> 8, hi_word(&a.center[i]) >> 8));
-            held = max(held, __ldcg(&a.beta[i]) >> 8);
-        }
-    }
-    held = __reduce_max_sync(0xffffffffu, held);
+    const uint32_t held =
+        tile_max_depth(a.center, a.cons, a.beta, a.width, a.height, tile % a.tiles_x, tile / a.tiles_x, lane);
     if (lane == 0) a.tile_depth[tile] = held;
 }
 
@@ -1880,6 +1937,7 @@ __global__ void __launch_bounds__(kRasterThreads) long_segment_kernel(const Rast
             sm.cs[lane] = make_float4(sc.x, sc.y, sc.z, 0.0f);
             sm.vd[lane] = dot3(sub3(xyz(wp), cam), fwd);
         }
+        if (lane < 4u) sm.finm[lane] = 0u;  // a lone segment: no shared endpoint
         __syncwarp();
         raster_camera(a, sm, 2u, uv, beta, lane, camera_r2_max(a.p));
         __syncwarp();
@@ -2092,7 +2150,8 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
     // Persistent: as many blocks as stay resident (at most one warp per ref
     // slot), each warp walking the refs with a stride of the grid's warps,
     // which lets it fetch its next ref and prefetch that strand's cache slot
-    // while it draws the current one.
+    // while it draws the current one.  (Handing refs out by atomic ticket
+    // instead, one or a few at a time, measured 1.3-2x slower.)
     int blocks = (int)std::max<size_t>((g->ref_capacity + kRasterWarps - 1) / kRasterWarps, 1);
     if (mode == 0 && ctx->camera_raster == HG_CAMERA_RASTER_BINNED && g->ref_capacity <= kBinMaxSlots) {
         return launch_camera_binned(ctx, g, a);
@@ -2100,8 +2159,8 @@ cudaError_t launch_raster(hg_ctx* ctx, hg_groom* g, const hg_hair_params& p, int
         // Refs in draw order (near bundles first), in stages; before each
         // stage after the first, the tile depths are rebuilt from the words
         // the earlier stages left, and segments behind them are skipped.
-        const uint32_t tiles_x = (ctx->width + (1u << kTileShift) - 1) >> kTileShift;
-        const uint32_t tiles = tiles_x * ((ctx->height + (1u << kTileShift) - 1) >> kTileShift);
+        const uint32_t tiles_x = tiles_along(ctx->width);
+        const uint32_t tiles = tiles_x * tiles_along(ctx->height);
         for (int k = 0; k + 1 < kCameraStageCount; ++k) {
             a.part_lo = kCameraStages[k];
             a.part_hi = kCameraStages[k + 1];
