@@ -1064,7 +1064,7 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
 // the segment p0-p1 (screen a -> a + seg).
 template <int MODE, class Args>
 __device__ __forceinline__ void dom_write(const Args& a, int32_t px, int32_t py, int32_t width, int32_t height,
-                                          float2 A, float2 seg, float seg_len2, f3 p0, f3 p1) {
+                                          float2 A, float2 seg, float seg_len2, f3 p0, f3 p1, float thickness) {
     const hg_hair_params& p = a.p;
     if (px < 0 || py < 0 || px >= width || py >= height) return;
     const uint32_t dom_w = f2u(p.dom_info[0]);
@@ -1087,7 +1087,6 @@ __device__ __forceinline__ void dom_write(const Args& a, int32_t px, int32_t py,
         return;
     }
     const float z_front = dequantize_depth(cur, near_, far_);
-    const float thickness = __fdiv_rn(fmaxf(far_ - near_, 1e-3f), (float)kDomLayers);
     const float tt = __fdiv_rn(fmaxf(dist - z_front, 0.0f), thickness);
     const uint32_t slice = min(f2u(tt), kDomLayers - 1u);
     const uint32_t pixels = dom_w * f2u(p.dom_info[1]);
@@ -1105,6 +1104,8 @@ template <int MODE, class Args>
 __device__ __forceinline__ void raster_dom(const Args& a, StrandSmem& sm, uint32_t ncp, uint32_t lane) {
     const hg_hair_params& p = a.p;
     const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
+    // slice thickness of the layers pass (write_dom_pixel), the same for every texel
+    const float thickness = __fdiv_rn(fmaxf(p.screen[3] - p.screen[2], 1e-3f), (float)kDomLayers);
     for (uint32_t j = lane; j + 1u < ncp; j += 32u) {
         float4 c0 = sm.cp[j], c1 = sm.cp[j + 1u];
         if (c0.w == 0.0f && c1.w == 0.0f) continue;
@@ -1121,7 +1122,7 @@ __device__ __forceinline__ void raster_dom(const Args& a, StrandSmem& sm, uint32
         f3 p0 = xyz(c0), p1 = xyz(c1);
         const int32_t ndy = (int32_t)(0u - (uint32_t)dy);
         for (int step = 0; step < 1024; ++step) {
-            if (!skip) dom_write<MODE>(a, x0, y0, width, height, A, seg, seg_len2, p0, p1);
+            if (!skip) dom_write<MODE>(a, x0, y0, width, height, A, seg, seg_len2, p0, p1, thickness);
             skip = false;
             if (x0 == x1 && y0 == y1) break;
             int32_t e2 = iadd(err, err);
@@ -1211,16 +1212,18 @@ __device__ __forceinline__ void fetch_order(StrandSmem& sm, const uint32_t* orde
     else sm.next_idx = k;
 }
 
-// Prefetches the strand cache slot of `ref` (both of its arrays, 2 x 65
-// float4, contiguous) into L2 with one bulk prefetch.  Slots are 2,080 bytes
-// apart from a 256-byte aligned base: the address and the size are multiples
-// of 16 bytes as the instruction requires.  A hint only: nothing waits on it.
-template <class Args>
+// Prefetches the strand cache slot of `ref` into L2 with one bulk prefetch:
+// both of its arrays (2 x 65 float4, contiguous) for the camera pass, the
+// positions for the deep-opacity passes.  Slots are 2,080 bytes apart from a
+// 256-byte aligned base: the address and the size are multiples of 16 bytes
+// as the instruction requires.  A hint only: nothing waits on it.
+template <int MODE, class Args>
 __device__ __forceinline__ void prefetch_cache_slot(const Args& a, const hg_strand_ref& ref) {
     if (!a.cache || ref.control_points != kCacheCps || ref.bundle >= a.bundle_count) return;
     const float4* slot = a.cache + (size_t)(a.strand_base[ref.bundle] + ref.strand) * (2u * kCacheCps);
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(slot), "r"((uint32_t)(2u * kCacheCps * 16u))
-                 : "memory");
+    // the deep-opacity passes read the positions only (1,040 bytes)
+    const uint32_t bytes = (MODE == 0 ? 2u : 1u) * kCacheCps * 16u;
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(slot), "r"(bytes) : "memory");
 }
 
 // raster.wgsl:225-337: one warp per strand ref, persistent over the refs.
@@ -1270,7 +1273,7 @@ __global__ void __launch_bounds__(kRasterThreads, raster_min_blocks<MODE>()) ras
         const uint32_t ncp = generate_strand<MODE>(a, sm, ref, bundle, uv, lane);
         if (lane == 0 && more) {
             copy_async_wait();
-            prefetch_cache_slot(a, sm.next_ref);
+            prefetch_cache_slot<MODE>(a, sm.next_ref);
         }
         if (MODE == 0) {
             float beta = __fdiv_rn(__uint2float_rn(ref.n_lod), __uint2float_rn(max(bundle.strand_count, 1u)));
