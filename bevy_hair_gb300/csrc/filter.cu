@@ -51,58 +51,79 @@ __device__ __forceinline__ float sqrt_bound(float r) {
 // staged in shared memory once: per texel the centre word's normalised depth
 // f32(depth)/16777214 (the exact value filter.wgsl:94 computes per tap; -1
 // marks an empty centre with a conservative hit, -2 both empty) and the shaded
-// colour.  Coverage decisions use exact arithmetic; the colour weights only
+// colour.  Pixels without hair are written at once; the tile's hair pixels
+// are then listed and handed to the first threads, one each, so the 121-tap
+// loop runs in full warps instead of the lanes of the hair pixels of every
+// row.  Coverage decisions use exact arithmetic; the colour weights only
 // scale colour, so they use the fast exponential.
 template <int TX, int TY, class V>
 __device__ __forceinline__ void filter_tile(const V& a, int32_t bx, int32_t by) {
     constexpr int kHaloX = TX + 2 * kFilterRadius, kHaloY = TY + 2 * kFilterRadius;
+    constexpr int kWarps = TX * TY / 32;
+    static_assert(TX * TY % 32 == 0, "whole warps per tile");
     __shared__ float s_norm[kHaloY][kHaloX];
     __shared__ float4 s_col[kHaloY][kHaloX];
+    __shared__ uint16_t s_list[TX * TY];
+    __shared__ int s_warp_hair[kWarps];
     const hg_hair_params& p = a.p;
     const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
     const int32_t x0 = bx * TX - kFilterRadius, y0 = by * TY - kFilterRadius;
     const int tid = threadIdx.y * TX + threadIdx.x;
-    const int32_t px = bx * TX + threadIdx.x, py = by * TY + threadIdx.y;
-    const bool inside = px < width && py < height;
-    const uint32_t pix = (uint32_t)py * (uint32_t)width + (uint32_t)px;
-    const unsigned long long center_word = inside ? __ldg(&a.center[pix]) : kEmptyU64;
-    const unsigned long long cons_word = inside ? __ldg(&a.cons[pix]) : kEmptyU64;
-    const bool center_hit = !is_empty(center_word), cons_hit = !is_empty(cons_word);
-    // A tile without hair writes zeros and needs no halo.
-    if (!__syncthreads_or(center_hit || cons_hit)) {
-        if (inside) {
-            a.filtered[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            a.filtered_depth[pix] = 0.0f;
+    {
+        const int32_t ox = bx * TX + threadIdx.x, oy = by * TY + threadIdx.y;
+        const bool own_inside = ox < width && oy < height;
+        const uint32_t own = (uint32_t)oy * (uint32_t)width + (uint32_t)ox;
+        const bool own_hair = own_inside && (!is_empty(__ldg(&a.center[own])) || !is_empty(__ldg(&a.cons[own])));
+        // pixels without hair (and every pixel of a tile without hair, which
+        // needs no halo) are written now
+        if (own_inside && !own_hair) {
+            a.filtered[own] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            a.filtered_depth[own] = 0.0f;
         }
-        return;
-    }
-    for (int i = tid; i < kHaloX * kHaloY; i += TX * TY) {
-        int hx = i % kHaloX, hy = i / kHaloX;
-        int32_t gx = x0 + hx, gy = y0 + hy;
-        float nrm = -2.0f;
-        float4 col = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        if (gx >= 0 && gy >= 0 && gx < width && gy < height) {
-            size_t q = (size_t)gy * width + gx;
-            unsigned long long c = __ldg(&a.center[q]);
-            if (!is_empty(c)) {
-                nrm = __fdiv_rn(__uint2float_rn((uint32_t)(c >> 40)), 16777214.0f);
-                col = __ldg(&a.shaded[q]);
-            } else if (!is_empty(__ldg(&a.cons[q]))) {
-                nrm = -1.0f;
+        const uint32_t ballot = __ballot_sync(0xffffffffu, own_hair);
+        if ((tid & 31) == 0) s_warp_hair[tid >> 5] = __popc(ballot);
+        __syncthreads();
+        int base = 0, total = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const int c = s_warp_hair[w];
+            base += w < (tid >> 5) ? c : 0;
+            total += c;
+        }
+        if (total == 0) return;
+        if (own_hair) s_list[base + __popc(ballot & ((1u << (tid & 31)) - 1u))] = (uint16_t)tid;
+        // the halo: per texel the normalised centre depth (or -1 / -2) and
+        // the shaded colour, as the tap loop reads them
+        for (int i = tid; i < kHaloX * kHaloY; i += TX * TY) {
+            const int hx = i % kHaloX, hy = i / kHaloX;
+            const int32_t gx = x0 + hx, gy = y0 + hy;
+            float nrm = -2.0f;
+            float4 col = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            if (gx >= 0 && gy >= 0 && gx < width && gy < height) {
+                const size_t q = (size_t)gy * width + gx;
+                const unsigned long long c = __ldg(&a.center[q]);
+                if (!is_empty(c)) {
+                    nrm = __fdiv_rn(__uint2float_rn((uint32_t)(c >> 40)), 16777214.0f);
+                    col = __ldg(&a.shaded[q]);
+                } else if (!is_empty(__ldg(&a.cons[q]))) {
+                    nrm = -1.0f;
+                }
             }
+            s_norm[hy][hx] = nrm;
+            s_col[hy][hx] = col;
         }
-        s_norm[hy][hx] = nrm;
-        s_col[hy][hx] = col;
+        __syncthreads();
+        if (tid >= total) return;  // no hair pixel left for this thread
     }
-    __syncthreads();
-
-    if (!inside) return;
-    if (!center_hit && !cons_hit) {
-        a.filtered[pix] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        a.filtered_depth[pix] = 0.0f;
-        return;
-    }
-    const int lx = threadIdx.x + kFilterRadius, ly = threadIdx.y + kFilterRadius;
+    // this thread's hair pixel
+    const int src = s_list[tid];
+    const int sx = src % TX, sy = src / TX;
+    const int32_t px = bx * TX + sx, py = by * TY + sy;
+    const uint32_t pix = (uint32_t)py * (uint32_t)width + (uint32_t)px;
+    const unsigned long long center_word = __ldg(&a.center[pix]);
+    const unsigned long long cons_word = __ldg(&a.cons[pix]);
+    const bool center_hit = !is_empty(center_word), cons_hit = !is_empty(cons_word);
+    const int lx = sx + kFilterRadius, ly = sy + kFilterRadius;
     const unsigned long long w = center_hit ? center_word : cons_word;
     const uint32_t high = (uint32_t)(w >> 32), low = (uint32_t)w;
     const f3 tangent = oct_decode(high & 0xffu, low >> 24u);
