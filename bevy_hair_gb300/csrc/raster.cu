@@ -626,22 +626,27 @@ __device__ __forceinline__ void generate_slot(const hg_hair_params& p, StrandSme
 // control points (+ in_front), screen positions and, for the camera pass,
 // world tangents, w and ao in shared memory.  Strands at kCacheCps control
 // points come from the frame's strand cache when one is given; the DOM passes
-// need positions only.
+// need positions only.  With a non-null `deferred`, a cached camera strand's
+// tangents (and w) are not read: *deferred gets their address in the cache
+// for load_tangents, and sm.ct holds zeros until then.
 template <int MODE, class Args>
 __device__ __forceinline__ uint32_t generate_strand(const Args& a, StrandSmem& sm, const hg_strand_ref& ref,
-                                                    const hg_gpu_bundle& bundle, float2 uv, uint32_t lane) {
+                                                    const hg_gpu_bundle& bundle, float2 uv, uint32_t lane,
+                                                    const float4** deferred = nullptr) {
     const hg_hair_params& p = a.p;
     const uint32_t ncp = min(max(ref.control_points, 2u), 127u);
     if (a.cache && ncp == kCacheCps) {
         const float4* pos = a.cache + (size_t)(a.strand_base[ref.bundle] + ref.strand) * (2u * kCacheCps);
         const float4* tan = pos + kCacheCps;
+        const bool defer = MODE == 0 && deferred != nullptr;
+        if (defer) *deferred = tan;
 #pragma unroll
         for (int k = 0; k < 3; ++k) {
             const uint32_t idx = lane + 32u * k;
             bool fin = false;
             if (idx < kCacheCps) {
                 const float4 wp = __ldg(pos + idx);
-                const float4 wt = MODE == 0 ? __ldg(tan + idx) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+                const float4 wt = MODE == 0 && !defer ? __ldg(tan + idx) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
                 fin = store_cp<MODE>(p, sm, idx, xyz(wp), xyz(wt), wt.w, wp.w);
             }
             if (MODE == 0) {
@@ -676,6 +681,24 @@ __device__ __forceinline__ float sqrt_bound(float r) {
         x = up;
     }
     return x;
+}
+
+// The tangents (xyz, w) of a cached camera strand whose load generate_strand
+// deferred, into sm.ct, and the finiteness of each into finm (and with the
+// positions' bits).  Every lane of the warp calls it.
+__device__ __forceinline__ void load_tangents(StrandSmem& sm, const float4* tan, uint32_t lane, uint32_t (&finm)[4]) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const uint32_t idx = lane + 32u * k;
+        bool fin = false;
+        if (idx < kCacheCps) {
+            const float4 wt = __ldg(tan + idx);
+            sm.ct[idx] = wt;
+            fin = finite3(wt.x, wt.y, wt.z) && finite3(wt.w, 0.0f, 0.0f);
+        }
+        finm[k] &= __ballot_sync(0xffffffffu, fin);
+    }
+    __syncwarp();
 }
 
 // The centre-disk test's bound on |o|^2: length(o) <= diameter / 2
@@ -884,7 +907,8 @@ __global__ void __launch_bounds__(256) tile_depth_kernel(const unsigned long lon
 template <class Args>
 __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uint32_t ncp, float2 uv,
                                               float beta, uint32_t lane, float r2_max,
-                                              const uint32_t* tile_depth = nullptr, uint32_t tiles_x = 0) {
+                                              const uint32_t* tile_depth = nullptr, uint32_t tiles_x = 0,
+                                              const float4* deferred_tan = nullptr) {
     const hg_hair_params& p = a.p;
     const int32_t nseg = (int32_t)ncp - 1;
     const int32_t width = f2i(p.screen[0]), height = f2i(p.screen[1]);
@@ -930,6 +954,12 @@ __device__ __forceinline__ void raster_camera(const Args& a, StrandSmem& sm, uin
     for (int k = 0; k < 4; ++k) {
         livem[k] = __ballot_sync(0xffffffffu, cnts[k] > 0);
         finm[k] = sm.finm[k];
+    }
+    if (deferred_tan) {
+        // tangents only for a strand with samples (most strands of the
+        // second stage have none)
+        if ((livem[0] | livem[1] | livem[2] | livem[3]) == 0u) return;
+        load_tangents(sm, deferred_tan, lane, finm);
     }
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
@@ -1270,14 +1300,18 @@ __global__ void __launch_bounds__(kRasterThreads, raster_min_blocks<MODE>()) ras
         }
         const hg_gpu_bundle bundle = a.bundles[ref.bundle];
         const float2 uv = pcg_uv(ref.strand ^ (ref.bundle * 0x85ebca6bu));
-        const uint32_t ncp = generate_strand<MODE>(a, sm, ref, bundle, uv, lane);
+        // the second camera stage reads a cached strand's tangents only when
+        // some segment of it is not hidden
+        const float4* deferred = nullptr;
+        const uint32_t ncp =
+            generate_strand<MODE>(a, sm, ref, bundle, uv, lane, MODE == 0 && a.tile_depth ? &deferred : nullptr);
         if (lane == 0 && more) {
             copy_async_wait();
             prefetch_cache_slot<MODE>(a, sm.next_ref);
         }
         if (MODE == 0) {
             float beta = __fdiv_rn(__uint2float_rn(ref.n_lod), __uint2float_rn(max(bundle.strand_count, 1u)));
-            raster_camera(a, sm, ncp, uv, beta, lane, r2_max, a.tile_depth, a.tiles_x);
+            raster_camera(a, sm, ncp, uv, beta, lane, r2_max, a.tile_depth, a.tiles_x, deferred);
         } else {
             raster_dom<MODE>(a, sm, ncp, lane);
         }
@@ -1464,10 +1498,11 @@ __global__ void __launch_bounds__(kRasterThreads, 6) batch_raster_kernel(const B
                 const uint32_t ncp = generate_strand<2>(a, sm, ref, bundle, uv, lane);
                 raster_dom<2>(a, sm, ncp, lane);
             } else if (cam) {
-                const uint32_t ncp = generate_strand<0>(a, sm, ref, bundle, uv, lane);
+                const float4* deferred = nullptr;
+                const uint32_t ncp = generate_strand<0>(a, sm, ref, bundle, uv, lane, PHASE == 2 ? &deferred : nullptr);
                 float beta = __fdiv_rn(__uint2float_rn(ref.n_lod), __uint2float_rn(max(bundle.strand_count, 1u)));
                 raster_camera(a, sm, ncp, uv, beta, lane, camera_r2_max(a.p), PHASE == 2 ? a.tile_depth : nullptr,
-                              a.tiles_x);
+                              a.tiles_x, deferred);
             } else {
                 const uint32_t ncp = generate_strand<1>(a, sm, ref, bundle, uv, lane);
                 raster_dom<1>(a, sm, ncp, lane);
