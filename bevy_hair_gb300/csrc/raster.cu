@@ -1183,10 +1183,24 @@ struct GenArgs {
     uint32_t strands;
 };
 
-// Strand g of a groom into its cache slot (one warp).
+// The last control point (index 64) of up to 32 strands, finished together
+// one per lane: the model-space point and its neighbour 63, w and ao, from
+// generate_one, and the strand (and batch view) it belongs to.
+struct CacheTails {
+    float4 a[32];  // model point 64 xyz, ao
+    float4 b[32];  // model point 63 xyz, w
+    uint32_t strand[32];
+    uint32_t view[32];
+};
+
+// Strand g of a groom into its cache slot (one warp): control points 0..63
+// on the 32 lanes in two rounds.  Point 64 alone would take a third round at
+// one lane in 32, so its inputs go to tails slot `slot` instead, and
+// finish_tails completes 32 strands' last points in one round.
 template <class Args>
 __device__ __forceinline__ void generate_one(const Args& a, uint32_t g, float4* lp, float4* lt, float4* ls,
-                                             uint32_t lane) {
+                                             uint32_t lane, CacheTails& tails, uint32_t slot, uint32_t view) {
+    static_assert(kCacheCps == 65, "two full rounds of 32 control points and one tail point");
     const uint32_t b = a.strand_bundle[g];
     const uint32_t s = g - a.strand_base[b];
     const hg_gpu_bundle bundle = a.bundles[b];
@@ -1197,30 +1211,59 @@ __device__ __forceinline__ void generate_one(const Args& a, uint32_t g, float4* 
     float4* pos = a.cache + (size_t)g * (2u * kCacheCps);
     float4* tan = pos + kCacheCps;
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
+    for (int k = 0; k < 2; ++k) {
         f3 prev, next;
         if (k == 0) cp_neighbours<0>(mp, lane, prev, next);
         if (k == 1) cp_neighbours<1>(mp, lane, prev, next);
-        if (k == 2) cp_neighbours<2>(mp, lane, prev, next);
         const uint32_t idx = lane + 32u * k;
-        if (idx < kCacheCps) {
-            const f3 wp = to_world(a.p, mp[k]);
-            const f3 wt = cp_world_tangent(a.p, idx, kCacheCps, prev, mp[k], next);
-            pos[idx] = make_float4(wp.x, wp.y, wp.z, aok[k]);
-            tan[idx] = make_float4(wt.x, wt.y, wt.z, wk[k]);
-        }
+        const f3 wp = to_world(a.p, mp[k]);
+        const f3 wt = cp_world_tangent(a.p, idx, kCacheCps, prev, mp[k], next);
+        pos[idx] = make_float4(wp.x, wp.y, wp.z, aok[k]);
+        tan[idx] = make_float4(wt.x, wt.y, wt.z, wk[k]);
+    }
+    // point 64 is slot 2 of lane 0; its neighbour 63 is slot 1 of lane 31
+    const f3 p63 = shfl_idx3(mp[1], 31);
+    if (lane == 0) {
+        tails.a[slot] = make_float4(mp[2].x, mp[2].y, mp[2].z, aok[2]);
+        tails.b[slot] = make_float4(p63.x, p63.y, p63.z, wk[2]);
+        tails.strand[slot] = g;
+        tails.view[slot] = view;
     }
     __syncwarp();
+}
+
+// Control point 64 of the strand in tails slot `slot` (a: that strand's
+// arguments), written as generate_one's third round would (cp_world_tangent
+// of the last point uses its previous neighbour and itself).  The lanes of a
+// warp finish up to 32 slots at once.
+template <class Args>
+__device__ __forceinline__ void finish_tail(const Args& a, const CacheTails& tails, uint32_t slot) {
+    const float4 ta = tails.a[slot], tb = tails.b[slot];
+    const f3 curr = mk3(ta.x, ta.y, ta.z), prev = mk3(tb.x, tb.y, tb.z);
+    const uint32_t idx = kCacheCps - 1u;
+    const f3 wp = to_world(a.p, curr);
+    const f3 wt = cp_world_tangent(a.p, idx, kCacheCps, prev, curr, curr);
+    float4* pos = a.cache + (size_t)tails.strand[slot] * (2u * kCacheCps);
+    pos[idx] = make_float4(wp.x, wp.y, wp.z, ta.w);
+    pos[kCacheCps + idx] = make_float4(wt.x, wt.y, wt.z, tb.w);
 }
 
 __global__ void __launch_bounds__(kRasterThreads) generate_kernel(const GenArgs a) {
     __shared__ float4 lp[kRasterWarps][16];
     __shared__ float4 lt[kRasterWarps][16];
     __shared__ float4 ls[kRasterWarps][16];
+    __shared__ CacheTails tails[kRasterWarps];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t nwarps = gridDim.x * kRasterWarps;
-    for (uint32_t g = blockIdx.x * kRasterWarps + warp; g < a.strands; g += nwarps)
-        generate_one(a, g, lp[warp], lt[warp], ls[warp], lane);
+    uint32_t n = 0;
+    for (uint32_t g = blockIdx.x * kRasterWarps + warp; g < a.strands; g += nwarps) {
+        generate_one(a, g, lp[warp], lt[warp], ls[warp], lane, tails[warp], n, 0u);
+        if (++n == 32u || g + nwarps >= a.strands) {
+            if (lane < n) finish_tail(a, tails[warp], lane);
+            __syncwarp();
+            n = 0;
+        }
+    }
 }
 
 // Asynchronous global -> shared copies (cp.async) of the ref loop's next
@@ -1413,11 +1456,18 @@ __global__ void __launch_bounds__(kRasterThreads) batch_generate_kernel(const Ba
     __shared__ float4 lp[kRasterWarps][16];
     __shared__ float4 lt[kRasterWarps][16];
     __shared__ float4 ls[kRasterWarps][16];
+    __shared__ CacheTails tails[kRasterWarps];
     const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31u;
     const uint32_t nwarps = gridDim.x * kRasterWarps;
+    uint32_t n = 0;
     for (uint32_t g = blockIdx.x * kRasterWarps + warp; g < total; g += nwarps) {
         const uint32_t v = find_view(prefix, n_cam, g);
-        generate_one(views[v], g - prefix[v], lp[warp], lt[warp], ls[warp], lane);
+        generate_one(views[v], g - prefix[v], lp[warp], lt[warp], ls[warp], lane, tails[warp], n, v);
+        if (++n == 32u || g + nwarps >= total) {
+            if (lane < n) finish_tail(views[tails[warp].view[lane]], tails[warp], lane);
+            __syncwarp();
+            n = 0;
+        }
     }
 }
 
