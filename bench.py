@@ -317,7 +317,7 @@ def surrogate_section(r, cam, lights, flush, stream, reps: int, karis_ms: float,
 
 
 # Algorithmic bytes of each pass per launch (what roofline.achieved counts).
-def survey_bytes(sc, seg_refs: dict) -> dict:
+def compulsory_bytes(sc, seg_refs: dict) -> dict:
     """Compulsory bytes of the raster passes as the path's measurement plan
     states them: one final write of the pass's targets (G-buffer 20 B/px; DOM
     front plane 4 B/texel; front plane read + 16 counters 68 B/texel) plus one
@@ -693,7 +693,7 @@ def run_ours(args, rank, world, local):
             "gbs": round(nbytes[p] / (acc[p] * 1e-3) / 1e9, 1) if acc[p] > 0 else None,
             "frac_of_hbm": round(nbytes[p] / (acc[p] * 1e-3) / 1e9 / peak, 4) if acc[p] > 0 else None}
         for p in nbytes}
-    sbytes = survey_bytes(sc, {"camera_refs": ref_c, "dom_refs": ref_d})
+    sbytes = compulsory_bytes(sc, {"camera_refs": ref_c, "dom_refs": ref_d})
     if dominant in sbytes:
         # the measurement plan's compulsory bytes; the strand-cache-aware count beside it
         headline_bytes, bytes_kind = sbytes[dominant], "compulsory (groom + refs + one write of the targets)"
